@@ -1,0 +1,214 @@
+"""Synthetic speckle volumes, ROI point clouds and `dvc` input files.
+
+No public dataset is used anywhere in this project: every volume is a seeded
+synthetic speckle pattern (Gaussian blobs plus Gaussian noise), and the
+correlate volume is the same blob field rendered at the inverse-deformed
+position of each voxel, with fresh noise. The displacement convention is the
+reference's `.disp` one: u = target position - reference position
+(Core/InputRead.cpp `print_manual_output`).
+
+This module is the small-volume (numpy, CPU) generator used by tests. Large
+benchmark volumes use the device generator `dvc_gpu_synth_volume` in
+libdvcgpu.so, which follows the same definition.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+# --------------------------------------------------------------- deformations
+@dataclass
+class Affine:
+    """u(X) = t + E (X - c)."""
+    t: tuple = (0.0, 0.0, 0.0)
+    E: tuple = ((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+    c: tuple = (0.0, 0.0, 0.0)
+
+    def u(self, X):
+        X = np.asarray(X, dtype=np.float64)
+        return np.asarray(self.t) + (X - np.asarray(self.c)) @ np.asarray(self.E).T
+
+    def inverse(self, x):
+        """X with X + u(X) = x."""
+        A = np.eye(3) + np.asarray(self.E)
+        rhs = np.asarray(x, np.float64) - np.asarray(self.t) - np.asarray(self.c)
+        return np.asarray(self.c) + rhs @ np.linalg.inv(A).T
+
+    def coef(self):
+        return [*self.t, *np.asarray(self.E).ravel(), *self.c]
+
+    kind = 1
+
+
+@dataclass
+class Sinusoid:
+    """u_i(X) = A sin(2 pi X_j / L) with j = (i+1) mod 3."""
+    A: float = 3.0
+    L: float = 400.0
+
+    def u(self, X):
+        X = np.asarray(X, dtype=np.float64)
+        return self.A * np.sin(2.0 * np.pi * np.roll(X, -1, axis=-1) / self.L)
+
+    def inverse(self, x, iters: int = 30):
+        x = np.asarray(x, np.float64)
+        X = x.copy()
+        for _ in range(iters):
+            X = x - self.u(X)
+        return X
+
+    def coef(self):
+        return [self.A, self.L]
+
+    kind = 2
+
+
+@dataclass
+class Identity:
+    def u(self, X):
+        return np.zeros_like(np.asarray(X, np.float64))
+
+    def inverse(self, x):
+        return np.asarray(x, np.float64)
+
+    def coef(self):
+        return []
+
+    kind = 0
+
+
+# ----------------------------------------------------------------- speckle ---
+def blobs(shape_xyz, n_blobs, sigma=(1.5, 3.0), amp=(40.0, 200.0), seed=1):
+    """Random blob list [n, 5]: x, y, z, sigma, amplitude (float64)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape_xyz
+    b = np.empty((n_blobs, 5))
+    b[:, 0] = rng.uniform(0, nx, n_blobs)
+    b[:, 1] = rng.uniform(0, ny, n_blobs)
+    b[:, 2] = rng.uniform(0, nz, n_blobs)
+    b[:, 3] = rng.uniform(*sigma, n_blobs)
+    b[:, 4] = rng.uniform(*amp, n_blobs)
+    return b
+
+
+def render(shape_xyz, blob_list, deform=None, noise_sigma=2.0, noise_seed=2, background=0.0,
+           dtype=np.uint8, vmax=None, reach=4.0):
+    """Volume [z, y, x] of the blob field at the inverse-deformed voxel positions.
+
+    Each blob contributes amp * exp(-|X(x) - b|^2 / (2 sigma^2)) within `reach`
+    sigmas, X(x) the reference position of voxel x. Noise N(0, noise_sigma) is
+    added, then the field is rounded and clipped to [0, vmax].
+    """
+    deform = deform or Identity()
+    nx, ny, nz = shape_xyz
+    field = np.full((nz, ny, nx), background, dtype=np.float64)
+    for bx, by, bz, s, a in blob_list:
+        centre = np.array([bx, by, bz]) + deform.u(np.array([bx, by, bz]))
+        r = reach * s * 1.1 + 1.0
+        lo = np.maximum(np.floor(centre - r).astype(int), 0)
+        hi = np.minimum(np.ceil(centre + r).astype(int) + 1, [nx, ny, nz])
+        if np.any(hi <= lo):
+            continue
+        zz, yy, xx = np.meshgrid(np.arange(lo[2], hi[2]), np.arange(lo[1], hi[1]),
+                                 np.arange(lo[0], hi[0]), indexing="ij")
+        x = np.stack([xx, yy, zz], axis=-1).astype(np.float64)
+        X = deform.inverse(x)
+        d2 = np.sum((X - np.array([bx, by, bz])) ** 2, axis=-1)
+        w = np.where(d2 <= (reach * s) ** 2, a * np.exp(-d2 / (2 * s * s)), 0.0)
+        field[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]] += w
+    if noise_sigma > 0:
+        rng = np.random.default_rng(noise_seed)
+        field += rng.normal(0.0, noise_sigma, field.shape)
+    if vmax is None:
+        vmax = float(np.iinfo(dtype).max)
+    return np.clip(np.rint(field), 0, vmax).astype(dtype)
+
+
+def grid_points(n_xyz, spacing, centre):
+    """Regular grid, x fastest; returns [N,3] float64."""
+    nx, ny, nz = n_xyz
+    off = [(np.arange(m) - (m - 1) / 2.0) * spacing for m in (nx, ny, nz)]
+    zz, yy, xx = np.meshgrid(off[2] + centre[2], off[1] + centre[1], off[0] + centre[0],
+                             indexing="ij")
+    return np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+
+
+# -------------------------------------------------------------------- files ---
+def write_raw(path, vol, header_bytes=0, big_endian=False):
+    with open(path, "wb") as f:
+        f.write(b"\0" * header_bytes)
+        v = vol
+        if vol.dtype == np.uint16 and big_endian:
+            v = vol.astype(">u2")
+        f.write(np.ascontiguousarray(v).tobytes())
+
+
+def write_roi(path, pts, labels=None):
+    labels = np.arange(1, len(pts) + 1) if labels is None else labels
+    with open(path, "w") as f:
+        for lab, p in zip(labels, pts):
+            f.write(f"{int(lab)}\t{p[0]:.3f}\t{p[1]:.3f}\t{p[2]:.3f}\n")
+
+
+@dataclass
+class RunSpec:
+    """The `dvc` input-file keys (Core/InputRead.cpp:123-455)."""
+    reference_filename: str
+    correlate_filename: str
+    point_cloud_filename: str
+    output_filename: str
+    vol_bit_depth: int
+    vol_wide: int
+    vol_high: int
+    vol_tall: int
+    subvol_geom: str = "cube"
+    subvol_size: int = 31
+    subvol_npts: int = 2000
+    disp_max: int = 12
+    num_srch_dof: int = 6
+    obj_function: str = "znssd"
+    interp_type: str = "tricubic"
+    vol_hdr_lngth: int = 0
+    vol_endian: str = "little"
+    basin_radius: float = 0.0
+    rigid_trans: tuple = (0.0, 0.0, 0.0)
+    subvol_aspect: tuple = (1.0, 1.0, 1.0)
+    num_points_to_process: int = 0
+    starting_point: tuple | None = None
+    extra: dict = field(default_factory=dict)
+
+    def write(self, path):
+        L = ["# dvc input file (synthetic)",
+             f"reference_filename\t{self.reference_filename}\t### reference volume",
+             f"correlate_filename\t{self.correlate_filename}\t### correlate volume",
+             f"point_cloud_filename\t{self.point_cloud_filename}\t### ROI points",
+             f"output_filename\t{self.output_filename}\t### output base",
+             f"vol_bit_depth\t{self.vol_bit_depth}"]
+        if self.vol_bit_depth != 8:
+            L.append(f"vol_endian\t{self.vol_endian}")
+        L += [f"vol_hdr_lngth\t{self.vol_hdr_lngth}",
+              f"vol_wide\t{self.vol_wide}", f"vol_high\t{self.vol_high}",
+              f"vol_tall\t{self.vol_tall}",
+              f"subvol_geom\t{self.subvol_geom}", f"subvol_size\t{self.subvol_size}",
+              f"subvol_npts\t{self.subvol_npts}", "subvol_thresh\toff",
+              f"disp_max\t{self.disp_max}", f"num_srch_dof\t{self.num_srch_dof}",
+              f"obj_function\t{self.obj_function}", f"interp_type\t{self.interp_type}",
+              "rigid_trans\t{:.6f} {:.6f} {:.6f}".format(*self.rigid_trans),
+              f"basin_radius\t{self.basin_radius}",
+              "subvol_aspect\t{} {} {}".format(*self.subvol_aspect),
+              f"num_points_to_process\t{self.num_points_to_process}"]
+        if self.starting_point is not None:
+            L.append("starting_point\t{} {} {}".format(*self.starting_point))
+        for k, v in self.extra.items():
+            L.append(f"{k}\t{v}")
+        with open(path, "w") as f:
+            f.write("\n".join(L) + "\n")
+
+
+def cube_subvol_count(npts: int) -> int:
+    """Samples of a cube subvolume (Core/Search.cpp:30): ceil(npts^(1/3))^3."""
+    return int(math.pow(math.ceil(math.pow(float(npts), 1.0 / 3.0)), 3.0))

@@ -1,0 +1,193 @@
+/*
+ * dvc_gpu.h — C ABI of the GB300 digital-volume-correlation engine
+ * (libdvcgpu.so). Plain C types only: caller-owned host (or device) buffers,
+ * status integers, no exceptions and no C++/torch types across the boundary.
+ *
+ * The reference (TomographicImaging/DigitalVolumeCorrelation) has no library
+ * API: its hot path is the C++ class seam Search::process_point
+ * (Core/Search.cpp:95-192), called serially by the `dvc` executable
+ * (Core/dvc.cpp:233-303), signalling results by throwing Point_Good /
+ * Range_Fail / Convg_Fail (Core/Utility.h:76-79). Each entry point below
+ * names the reference function it replaces. Function-level entry points
+ * (interpolation, objective, strain) exist so each reference function can be
+ * checked on its own against the FP64 oracle.
+ *
+ * Error convention: every function returns DVC_OK (0) or a negative DVC_E_*
+ * code; dvc_gpu_last_error() returns a message for the calling thread.
+ * Per-point search results use the reference's status integers
+ * (Core/Utility.h:38-41).
+ */
+#ifndef DVC_GPU_H
+#define DVC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DVC_ABI_VERSION 1
+
+/* per-point status, identical to Core/Utility.h:38-41 */
+#define DVC_POINT_GOOD 0
+#define DVC_RANGE_FAIL (-1)
+#define DVC_CONVG_FAIL (-2)
+#define DVC_NOT_SEARCH (-3)
+
+/* return codes */
+#define DVC_OK 0
+#define DVC_E_ARG (-10)      /* invalid argument (sizes, enums, limits)        */
+#define DVC_E_CUDA (-11)     /* CUDA runtime error                              */
+#define DVC_E_NOMEM (-12)    /* device allocation failed                        */
+#define DVC_E_TIMEOUT (-13)  /* a bounded device-side wait gave up              */
+#define DVC_E_RANGE (-14)    /* interpolation request outside the active box    */
+
+/* enums: same numbering as the reference's (Core/Utility.h:51-88) */
+enum dvc_objfcn { DVC_SAD = 0, DVC_SSD = 1, DVC_ZSSD = 2, DVC_NSSD = 3, DVC_ZNSSD = 4 };
+enum dvc_interp { DVC_NEAREST = 0, DVC_TRILINEAR = 1, DVC_TRICUBIC = 2 };
+enum dvc_geom { DVC_CUBE = 0, DVC_SPHERE = 1 };
+
+/* how each point's starting translation is chosen */
+enum dvc_seed_mode {
+  /* reference semantics (Core/Search.cpp:277-377): mean (u,v,w) of the
+     already-processed good points among the point's neighbour list, else
+     rigid_trans. Points run in `order`; a point waits for the neighbours
+     that precede it. */
+  DVC_SEED_NEIGHBOURS = 0,
+  /* caller supplies one (u,v,w) seed per point; points are independent */
+  DVC_SEED_GIVEN = 1,
+  /* every point starts from rigid_trans; points are independent */
+  DVC_SEED_RIGID = 2
+};
+
+/* Search configuration: the `dvc` input-file keys that shape the hot path
+   (Core/Utility.h:90-134 RunControl; limits Core/InputRead.cpp:519-631). */
+typedef struct dvc_params {
+  int vol_wide, vol_high, vol_tall; /* voxels; x fastest, then y, then z      */
+  int bytes_per_voxel;              /* 1 (uint8) or 2 (uint16, native endian) */
+  int subvol_geom;                  /* dvc_geom                               */
+  int subvol_size;                  /* cube side / sphere diameter, voxels    */
+  int subvol_npts;                  /* 1..50000                               */
+  double subvol_aspect[3];          /* default 1 1 1                          */
+  int disp_max;                     /* voxels                                 */
+  int num_srch_dof;                 /* 3, 6 or 12                             */
+  int obj_function;                 /* dvc_objfcn                             */
+  int interp_type;                  /* dvc_interp                             */
+  double basin_radius;              /* 0 = no coarse grid search              */
+  double rigid_trans[3];            /* default 0 0 0                          */
+  unsigned int sphere_seed;         /* mt19937 seed of sphere subvolumes; the
+                                       reference's reproducible test mode uses 1
+                                       (Core/Search.cpp:102-105)               */
+} dvc_params;
+
+/* Run statistics returned by dvc_gpu_process. */
+typedef struct dvc_stats {
+  int n_processed;        /* points searched                                   */
+  int n_good, n_range_fail, n_convg_fail;
+  long long n_evaluations; /* objective evaluations (grid + GN + ref + final)  */
+  long long n_gn_iterations;
+  double kernel_ms;       /* device time of the search launch (CUDA events)    */
+  double total_ms;        /* wall time of the call                             */
+} dvc_stats;
+
+typedef struct dvc_engine dvc_engine; /* opaque: device state for one volume pair */
+
+/* ---- library ------------------------------------------------------------ */
+const char *dvc_gpu_version(void);
+const char *dvc_gpu_last_error(void);
+int dvc_gpu_abi_version(void);
+
+/* ---- engine: both volumes resident in HBM -------------------------------
+ * Replaces Search::Search (Core/Search.cpp:24-82) plus the per-point volume
+ * reads of Interpolate::kernels (Core/Interpolate.cpp:144-258): the reference
+ * re-reads two est_box regions from disk for every point; here each volume is
+ * uploaded once. `ref_vox`/`cor_vox` are host buffers of
+ * vol_wide*vol_high*vol_tall voxels (header already skipped). For 16-bit data
+ * `big_endian` != 0 byte-swaps on upload (Core/Interpolate.cpp:233-242). */
+int dvc_gpu_create(dvc_engine **out, const dvc_params *p, const void *ref_vox,
+                   const void *cor_vox, int big_endian);
+/* Same, for volumes already in device memory (the engine keeps the pointers;
+   the caller keeps the buffers alive). */
+int dvc_gpu_create_device(dvc_engine **out, const dvc_params *p, const void *ref_vox_dev,
+                          const void *cor_vox_dev);
+void dvc_gpu_destroy(dvc_engine *e);
+
+/* ---- the search: Search::process_point for many points ------------------
+ * Replaces the serial loop of Core/dvc.cpp:233-303 over
+ * Search::process_point (Core/Search.cpp:95-192): per point the reference
+ * subvolume interpolation, the start estimate (starting_param), the coarse
+ * translation grid (trgrid_global, :934-1043), the Gauss-Newton refinement
+ * (min_Lev_Mar, :194-246) and the final objective (:187).
+ *   points    [n_points*3] x,y,z of every ROI point (host)
+ *   order     [n_process]  indices into points, processing order (host)
+ *   neigh     [n_points*n_neigh] neighbour indices incl. self (host); used by
+ *             DVC_SEED_NEIGHBOURS, may be NULL otherwise
+ *   seeds     [n_points*3] starting (u,v,w) for DVC_SEED_GIVEN, else NULL
+ * outputs, indexed by point (entries of points never processed are set to
+ * DVC_NOT_SEARCH / 0):
+ *   status    [n_points]   DVC_POINT_GOOD / DVC_RANGE_FAIL
+ *   objmin    [n_points]   objective at the optimum (0 when not good)
+ *   params    [n_points*12] u v w phi the psi exx eyy ezz exy eyz exz (first
+ *             num_srch_dof valid, rest 0; zeros when not good)
+ *   gn_iters  [n_points] Gauss-Newton iterations taken (may be NULL)
+ *   stats     may be NULL */
+int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_process,
+                    const int *order, int n_neigh, const int *neigh, int seed_mode,
+                    const double *seeds, int *status, double *objmin, double *params,
+                    int *gn_iters, dvc_stats *stats);
+
+/* Same as dvc_gpu_process with every array already in device memory
+   (points, order, neigh, seeds; outputs status, objmin, params, gn_iters).
+   Enqueued on `stream` (cudaStream_t, may be NULL); returns once enqueued;
+   stats are not filled. */
+int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev, int n_process,
+                           const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
+                           const double *seeds_dev, int *status_dev, double *objmin_dev,
+                           double *params_dev, int *gn_iters_dev, void *stream);
+
+/* ---- function-level entry points ----------------------------------------
+ * Interpolate one volume (0 = reference, 1 = correlate) at n points, with the
+ * interpolation box of this engine's search (Search::Search est_box_nom,
+ * Core/Search.cpp:66-80) centred on `center` (Interpolate::center_on,
+ * Core/Interpolate.cpp:569-574). Replaces Interpolate::nearest / tri_lin /
+ * tri_cub_Lek (Core/Interpolate.cpp:404-567). Returns DVC_E_RANGE when the
+ * points' bounding box leaves the active box (the reference's Intrp_Fail,
+ * Core/Interpolate.cpp:474-481); `out` is then untouched. */
+int dvc_gpu_interpolate(dvc_engine *e, int volume, const double center[3], int n,
+                        const double *pts, int interp_type, double *out);
+
+/* Objective of two sample vectors, with optional residual vector. Replaces
+   obj_SAD .. obj_ZNSSD (Core/ObjectiveFunctions.cpp:24-263). */
+int dvc_gpu_objective(int obj_function, int n, const double *ref, const double *tar,
+                      double *obj, double *residual);
+
+/* Strain-window least-squares fit for every point. Replaces the per-point
+ * loop of the `strain` executable (Core/strain.cpp:402-591).
+ *   pts [n*3], status [n], objmin [n], disp [n*3]  (from the .disp file)
+ *   neigh [n*n_neigh]                               (from the .sort.csv file)
+ *   ndp strain window (already clamped by the caller as Core/strain.cpp:204-207)
+ *   objt objmin threshold, refill (-r), planar: bit0 yz_only, bit1 zx_only,
+ *   bit2 xy_only (Core/strain.cpp:340-370)
+ * outputs: u_fit [n*3], pts_in_sw [n], sw_radius [n], e_strain [n*9],
+ *   l_strain [n*9] (exx eyy ezz exy eyz exz p1 p2 p3), dgrad [n*9] row-major */
+int dvc_gpu_strain(int n, const double *pts, const int *status, const double *objmin,
+                   const double *disp, int n_neigh, const int *neigh, int ndp, double objt,
+                   int refill, int planar, double *u_fit, int *pts_in_sw, double *sw_radius,
+                   double *e_strain, double *l_strain, double *dgrad);
+
+/* Synthetic speckle volume for benchmarks and tests (no reference
+   counterpart): Gaussian blobs rendered at the inverse-deformed position of
+   every voxel plus Gaussian noise, clipped and rounded to uint8/uint16.
+   `deform` selects the field: 0 none; 1 affine u(X) = t + E (X - c) with
+   coef = {t0,t1,t2, E00..E22 (9), c0,c1,c2}; 2 sinusoid u_i = A sin(2 pi X_j / L)
+   with coef = {A, L}. vol_dev is a device buffer. */
+int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int bytes_per_voxel,
+                         int n_blobs, const float *blobs_dev /* n_blobs*5: x y z sigma amp */,
+                         int deform, const double *coef, float background, float noise_sigma,
+                         unsigned long long noise_seed, float vmax, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DVC_GPU_H */

@@ -1,0 +1,305 @@
+// dvc_device.cuh — device building blocks of the DVC engine.
+//
+// Interpolation. The reference builds, per touched cell, the 64 Lekien-Marsden
+// tricubic coefficients a = BI * vb from the values and central-difference
+// derivatives (f, fx, fy, fz, fxy, fxz, fyz, fxyz) at the cell's 8 corners
+// (Core/Interpolate.cpp:377-402, Core/Matrix_4d.h:108-133), then evaluates
+// sum a_ijk x^i y^j z^k (Core/Interpolate.cpp:539-561). The corner
+// constraints are the tensor product of the 1D Hermite constraints, and the
+// central differences are the tensor product of 1D differences, so inside the
+// interpolation box that interpolant is exactly the tensor product of 1D cubic
+// Hermite interpolation with central-difference slopes (Catmull-Rom):
+//   val = sum_{a,b,c} wx_a wy_b wz_c V[x-1+a, y-1+b, z-1+c]
+// with per-axis weights of the cell fraction f
+//   w_-1 = (-f^3 + 2f^2 - f)/2, w_0 = (3f^3 - 5f^2 + 2)/2,
+//   w_1  = (-3f^3 + 4f^2 + f)/2, w_2 = (f^3 - f^2)/2.
+// That is 84 FMAs per sample instead of a 64x64 coefficient product.
+//
+// Box faces. The reference computes derivatives only inside its interpolation
+// box and copies them outward on the faces (Core/Interpolate.cpp:293-335): the
+// derivative quantities of a corner on a face equal those of the nearest
+// interior voxel, while the value f stays the corner's own. Per axis this
+// gives three 1D weight sets for a cell of box-local index c (n voxels):
+//   A: values and slopes at the clamped corners (Catmull-Rom inside),
+//   B: values only, at the clamped corners,
+//   C: values only, at the true corners,
+// and the interpolant is  A(x)A(y)A(z) - B(x)B(y)B(z) + C(x)C(y)C(z).
+// Inside the box B == C on every axis and it reduces to the separable form.
+// A cell with c = n-1 (the reference reads past its arrays) is evaluated as
+// the cubic of cell n-2 continued past its end; the FP64 oracle does the same.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dvc {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxDof = 12;
+
+// ------------------------------------------------------------ 1D weights ---
+struct W4 {
+  float w[4];
+};
+
+// Catmull-Rom (interior) weights and their derivative in f.
+__device__ __forceinline__ void cr_weights(float f, float w[4], float dw[4]) {
+  const float f2 = f * f, f3 = f2 * f;
+  w[0] = 0.5f * (-f3 + 2.f * f2 - f);
+  w[1] = 0.5f * (3.f * f3 - 5.f * f2 + 2.f);
+  w[2] = 0.5f * (-3.f * f3 + 4.f * f2 + f);
+  w[3] = 0.5f * (f3 - f2);
+  dw[0] = 0.5f * (-3.f * f2 + 4.f * f - 1.f);
+  dw[1] = 0.5f * (9.f * f2 - 10.f * f);
+  dw[2] = 0.5f * (-9.f * f2 + 8.f * f + 1.f);
+  dw[3] = 0.5f * (3.f * f2 - 2.f * f);
+}
+
+// Face weight sets (A, B, C) for one axis; kind 1 = max face (c == n-2),
+// kind 2 = min face (c == 0). See the file header.
+__device__ __forceinline__ void face_weights(int kind, float f, float A[4], float dA[4], float B[4],
+                                             float dB[4], float Cc[4], float dC[4]) {
+  const float f2 = f * f, f3 = f2 * f;
+  const float h00 = 2.f * f3 - 3.f * f2 + 1.f, dh00 = 6.f * f2 - 6.f * f;
+  const float h01 = 1.f - h00, dh01 = -dh00;
+  const float hs = 2.f * f3 - 3.f * f2 + f, dhs = 6.f * f2 - 6.f * f + 1.f;  // h10 + h11
+  Cc[0] = 0.f; Cc[1] = h00; Cc[2] = h01; Cc[3] = 0.f;
+  dC[0] = 0.f; dC[1] = dh00; dC[2] = dh01; dC[3] = 0.f;
+  if (kind == 1) {
+    A[0] = -0.5f * hs; A[1] = 1.f; A[2] = 0.5f * hs; A[3] = 0.f;
+    dA[0] = -0.5f * dhs; dA[1] = 0.f; dA[2] = 0.5f * dhs; dA[3] = 0.f;
+    B[0] = 0.f; B[1] = 1.f; B[2] = 0.f; B[3] = 0.f;
+  } else {
+    A[0] = 0.f; A[1] = -0.5f * hs; A[2] = 1.f; A[3] = 0.5f * hs;
+    dA[0] = 0.f; dA[1] = -0.5f * dhs; dA[2] = 0.f; dA[3] = 0.5f * dhs;
+    B[0] = 0.f; B[1] = 0.f; B[2] = 1.f; B[3] = 0.f;
+  }
+  dB[0] = dB[1] = dB[2] = dB[3] = 0.f;
+}
+
+// ------------------------------------------------------------- row loads ---
+// Four consecutive voxels along x starting at linear index `idx`, as floats.
+// Volumes are allocated with >= 16 bytes of tail padding, so the aligned
+// over-read past the last row stays inside the allocation.
+__device__ __forceinline__ float u8f(uint32_t b) {  // exact uint8 -> float
+  return __int_as_float(0x4B000000u | b) - 8388608.0f;
+}
+
+__device__ __forceinline__ void load_row4(const uint8_t *__restrict__ vol, long long idx,
+                                          float v[4]) {
+  const uint32_t *p = reinterpret_cast<const uint32_t *>(vol + (idx & ~3LL));
+  const uint32_t w0 = __ldg(p), w1 = __ldg(p + 1);
+  const uint32_t s = (uint32_t)(idx & 3);
+  const uint32_t sel = (s) | ((s + 1) << 4) | ((s + 2) << 8) | ((s + 3) << 12);
+  const uint32_t w = __byte_perm(w0, w1, sel);
+  v[0] = u8f(__byte_perm(w, 0, 0x4440));
+  v[1] = u8f(__byte_perm(w, 0, 0x4441));
+  v[2] = u8f(__byte_perm(w, 0, 0x4442));
+  v[3] = u8f(__byte_perm(w, 0, 0x4443));
+}
+
+__device__ __forceinline__ void load_row4(const uint16_t *__restrict__ vol, long long idx,
+                                          float v[4]) {
+  const char *base = reinterpret_cast<const char *>(vol);
+  const long long a = idx * 2;
+  const uint2 *p = reinterpret_cast<const uint2 *>(base + (a & ~7LL));
+  const uint2 q01 = __ldg(p), q23 = __ldg(p + 1);
+  const uint32_t s = (uint32_t)(a & 7);  // 0, 2, 4 or 6 bytes
+  const bool hi = s >= 4;
+  const uint32_t lo = hi ? q01.y : q01.x, mid = hi ? q23.x : q01.y, top = hi ? q23.y : q23.x;
+  const uint32_t sh = (s & 3) * 8;
+  const uint32_t r0 = __funnelshift_r(lo, mid, sh), r1 = __funnelshift_r(mid, top, sh);
+  v[0] = __int_as_float(0x4B000000u | (r0 & 0xFFFFu)) - 8388608.0f;
+  v[1] = __int_as_float(0x4B000000u | (r0 >> 16)) - 8388608.0f;
+  v[2] = __int_as_float(0x4B000000u | (r1 & 0xFFFFu)) - 8388608.0f;
+  v[3] = __int_as_float(0x4B000000u | (r1 >> 16)) - 8388608.0f;
+}
+
+template <typename VT>
+__device__ __forceinline__ float load_voxel_checked(const VT *__restrict__ vol, int x, int y, int z,
+                                                    int nx, int ny, int nz) {
+  if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return 0.f;
+  return (float)__ldg(vol + ((long long)z * ny + y) * nx + x);
+}
+
+// Volume + interpolation-box description used by the sample evaluators.
+template <typename VT>
+struct VolView {
+  const VT *vol;
+  int nx, ny, nz;      // volume extents
+  int ox, oy, oz;      // global voxel index of box voxel (0,0,0)
+  int bx, by, bz;      // box extents (voxels)
+  bool checked;        // box (+1 voxel margin) not inside the volume: bounds-check loads
+};
+
+// Separable contraction of the 4x4x4 stencil whose low corner is at global
+// voxel (x0, y0, z0), with value weights w* and (when GRAD) slope weights d*.
+// CHECKED: bounds-checked voxel loads (boxes that reach the volume edge).
+template <typename VT, bool GRAD, bool CHECKED>
+__device__ __forceinline__ float contract_impl(const VolView<VT> &V, int x0, int y0, int z0,
+                                               const float wx[4], const float wy[4],
+                                               const float wz[4], const float dx[4],
+                                               const float dy[4], const float dz[4], float g[3]) {
+  float val = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float s = 0.f, sdx = 0.f, sdy = 0.f;
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      float v[4];
+      if (!CHECKED) {
+        load_row4(V.vol, ((long long)(z0 + c) * V.ny + (y0 + b)) * V.nx + x0, v);
+      } else {
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+          v[a] = load_voxel_checked(V.vol, x0 + a, y0 + b, z0 + c, V.nx, V.ny, V.nz);
+      }
+      const float r = wx[0] * v[0] + wx[1] * v[1] + wx[2] * v[2] + wx[3] * v[3];
+      s += wy[b] * r;
+      if (GRAD) {
+        const float rdx = dx[0] * v[0] + dx[1] * v[1] + dx[2] * v[2] + dx[3] * v[3];
+        sdx += wy[b] * rdx;
+        sdy += dy[b] * r;
+      }
+    }
+    val += wz[c] * s;
+    if (GRAD) {
+      gx += wz[c] * sdx;
+      gy += wz[c] * sdy;
+      gz += dz[c] * s;
+    }
+  }
+  if (GRAD) {
+    g[0] = gx;
+    g[1] = gy;
+    g[2] = gz;
+  }
+  return val;
+}
+
+template <typename VT, bool GRAD>
+__device__ __noinline__ float contract_checked(const VolView<VT> &V, int x0, int y0, int z0,
+                                               const float *wx, const float *wy, const float *wz,
+                                               const float *dx, const float *dy, const float *dz,
+                                               float *g) {
+  return contract_impl<VT, GRAD, true>(V, x0, y0, z0, wx, wy, wz, dx, dy, dz, g);
+}
+
+template <typename VT, bool GRAD>
+__device__ __forceinline__ float contract(const VolView<VT> &V, int x0, int y0, int z0,
+                                          const float wx[4], const float wy[4], const float wz[4],
+                                          const float dx[4], const float dy[4], const float dz[4],
+                                          float g[3]) {
+  if (V.checked) return contract_checked<VT, GRAD>(V, x0, y0, z0, wx, wy, wz, dx, dy, dz, g);
+  return contract_impl<VT, GRAD, false>(V, x0, y0, z0, wx, wy, wz, dx, dy, dz, g);
+}
+
+// Face cells (rare): A A A - B B B + C C C, out of line to keep the hot
+// interior path small.
+template <typename VT, bool GRAD>
+__device__ __noinline__ float interp_face(const VolView<VT> &V, int x0, int y0, int z0,
+                                          const int kind[3], const float f[3], float g[3]) {
+  float A[3][4], dA[3][4], B[3][4], dB[3][4], Cc[3][4], dC[3][4];
+  for (int d = 0; d < 3; d++) {
+    if (kind[d] == 0) {
+      cr_weights(f[d], A[d], dA[d]);
+      const float f2 = f[d] * f[d], f3 = f2 * f[d];
+      const float h00 = 2.f * f3 - 3.f * f2 + 1.f, dh00 = 6.f * f2 - 6.f * f[d];
+      B[d][0] = 0.f; B[d][1] = h00; B[d][2] = 1.f - h00; B[d][3] = 0.f;
+      dB[d][0] = 0.f; dB[d][1] = dh00; dB[d][2] = -dh00; dB[d][3] = 0.f;
+      for (int k = 0; k < 4; k++) {
+        Cc[d][k] = B[d][k];
+        dC[d][k] = dB[d][k];
+      }
+    } else {
+      face_weights(kind[d], f[d], A[d], dA[d], B[d], dB[d], Cc[d], dC[d]);
+    }
+  }
+  float g1[3], g2[3], g3[3];
+  float v = contract<VT, GRAD>(V, x0, y0, z0, A[0], A[1], A[2], dA[0], dA[1], dA[2], g1);
+  v -= contract<VT, GRAD>(V, x0, y0, z0, B[0], B[1], B[2], dB[0], dB[1], dB[2], g2);
+  v += contract<VT, GRAD>(V, x0, y0, z0, Cc[0], Cc[1], Cc[2], dC[0], dC[1], dC[2], g3);
+  if (GRAD)
+    for (int d = 0; d < 3; d++) g[d] = g1[d] - g2[d] + g3[d];
+  return v;
+}
+
+// Interpolation of one sample at box-local cell (c[3]) and fraction (f[3]).
+// ITYPE: 0 nearest, 1 trilinear, 2 tricubic. Returns the value; with GRAD
+// also the spatial gradient. `undef` is set when the sample lies in the last
+// plane of the box (reference-undefined cell, see the file header).
+template <typename VT, int ITYPE, bool GRAD>
+__device__ __forceinline__ float interp_sample(const VolView<VT> &V, int c[3], float f[3],
+                                               float g[3], bool &undef) {
+  const int n[3] = {V.bx, V.by, V.bz};
+  undef = false;
+  if (ITYPE == 0) {
+    // Interpolate::nearest: the voxel at the truncated position
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      if (c[d] > n[d] - 1) {
+        undef = true;
+        c[d] = n[d] - 1;
+      }
+    if (GRAD) g[0] = g[1] = g[2] = 0.f;
+    const int x = V.ox + c[0], y = V.oy + c[1], z = V.oz + c[2];
+    if (V.checked) return load_voxel_checked(V.vol, x, y, z, V.nx, V.ny, V.nz);
+    return (float)__ldg(V.vol + ((long long)z * V.ny + y) * V.nx + x);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    if (c[d] > n[d] - 2) {
+      undef = true;
+      f[d] += (float)(c[d] - (n[d] - 2));
+      c[d] = n[d] - 2;
+    }
+  const int x0 = V.ox + c[0] - 1, y0 = V.oy + c[1] - 1, z0 = V.oz + c[2] - 1;
+  if (ITYPE == 1) {
+    // Interpolate::tri_lin: raw corner values only
+    float w[3][4], dw[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      w[d][0] = 0.f; w[d][1] = 1.f - f[d]; w[d][2] = f[d]; w[d][3] = 0.f;
+      dw[d][0] = 0.f; dw[d][1] = -1.f; dw[d][2] = 1.f; dw[d][3] = 0.f;
+    }
+    return contract<VT, GRAD>(V, x0, y0, z0, w[0], w[1], w[2], dw[0], dw[1], dw[2], g);
+  }
+  // tricubic
+  int kind[3];
+  bool face = false;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    kind[d] = (c[d] == n[d] - 2) ? 1 : (c[d] <= 0 ? 2 : 0);
+    face |= kind[d] != 0;
+  }
+  if (!face) {
+    float w[3][4], dw[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++) cr_weights(f[d], w[d], dw[d]);
+    return contract<VT, GRAD>(V, x0, y0, z0, w[0], w[1], w[2], dw[0], dw[1], dw[2], g);
+  }
+  return interp_face<VT, GRAD>(V, x0, y0, z0, kind, f, g);
+}
+
+// ------------------------------------------------------------ reductions ---
+// Compensated (Kahan) FP32 accumulator.
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
+// TwoSum merge of two compensated partials (hi, lo).
+__device__ __forceinline__ void two_sum_merge(float &hi, float &lo, float bhi, float blo) {
+  const float s = hi + bhi;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (bhi - bb);
+  hi = s;
+  lo = lo + blo + err;
+}
+
+}  // namespace dvc

@@ -1,0 +1,216 @@
+// dvc_synth.cu — synthetic speckle volumes on the device (benchmark and test
+// data; no reference counterpart).
+//
+// value(x) = background + sum_b amp_b exp(-|X(x) - c_b|^2 / (2 sigma_b^2)) + noise
+// where X(x) is the reference position of voxel x under the deformation
+// (X + u(X) = x), blobs contribute within 4 sigma, noise ~ N(0, noise_sigma)
+// from a counter-based hash of (seed, voxel index), then the value is rounded
+// and clipped to [0, vmax]. Blobs are binned on the host by their deformed
+// centre so each voxel visits only the blobs of its 27 neighbouring bins.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/dvc_gpu.h"
+#include "dvc_internal.h"
+
+namespace {
+
+constexpr int kBin = 16;
+
+struct SynthArgs {
+  void *vol;
+  int nx, ny, nz, bpv;
+  int gx, gy, gz;             // bin grid
+  const float4 *blobs;        // x y z 1/(2 sigma^2), sorted by bin
+  const float2 *amp_r2;       // amplitude, (4 sigma)^2
+  const int *bin_start;       // gx*gy*gz + 1
+  int deform;
+  float Ainv[9], t[3], c[3];  // affine: X = c + Ainv (x - t - c)
+  float amp, len;             // sinusoid
+  float background, noise_sigma, vmax;
+  unsigned long long seed;
+};
+
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__global__ void synth_kernel(SynthArgs a) {
+  const long long nvox = (long long)a.nx * a.ny * a.nz;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < nvox;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(idx % a.nx);
+    const int y = (int)((idx / a.nx) % a.ny);
+    const int z = (int)(idx / ((long long)a.nx * a.ny));
+    float X[3] = {(float)x, (float)y, (float)z};
+    if (a.deform == 1) {
+      const float r[3] = {X[0] - a.t[0] - a.c[0], X[1] - a.t[1] - a.c[1], X[2] - a.t[2] - a.c[2]};
+      for (int i = 0; i < 3; i++)
+        X[i] = a.c[i] + a.Ainv[i * 3 + 0] * r[0] + a.Ainv[i * 3 + 1] * r[1] + a.Ainv[i * 3 + 2] * r[2];
+    } else if (a.deform == 2) {
+      const float x0[3] = {X[0], X[1], X[2]};
+      const float w = 6.283185307179586f / a.len;
+      for (int it = 0; it < 30; it++) {
+        const float u0 = a.amp * sinf(w * X[1]), u1 = a.amp * sinf(w * X[2]), u2 = a.amp * sinf(w * X[0]);
+        X[0] = x0[0] - u0;
+        X[1] = x0[1] - u1;
+        X[2] = x0[2] - u2;
+      }
+    }
+    float v = a.background;
+    const int bx = x / kBin, by = y / kBin, bz = z / kBin;
+    for (int dz = -1; dz <= 1; dz++) {
+      const int cz = bz + dz;
+      if (cz < 0 || cz >= a.gz) continue;
+      for (int dy = -1; dy <= 1; dy++) {
+        const int cy = by + dy;
+        if (cy < 0 || cy >= a.gy) continue;
+        for (int dx = -1; dx <= 1; dx++) {
+          const int cx = bx + dx;
+          if (cx < 0 || cx >= a.gx) continue;
+          const int b = (cz * a.gy + cy) * a.gx + cx;
+          for (int k = a.bin_start[b]; k < a.bin_start[b + 1]; k++) {
+            const float4 bl = a.blobs[k];
+            const float ex = X[0] - bl.x, ey = X[1] - bl.y, ez = X[2] - bl.z;
+            const float d2 = ex * ex + ey * ey + ez * ez;
+            const float2 ar = a.amp_r2[k];
+            if (d2 <= ar.y) v += ar.x * __expf(-d2 * bl.w);
+          }
+        }
+      }
+    }
+    if (a.noise_sigma > 0.f) {
+      const unsigned long long h = splitmix(a.seed ^ splitmix((unsigned long long)idx));
+      const float u1 = ((h >> 40) + 1.0f) * (1.0f / 16777217.0f);
+      const float u2 = ((h >> 16) & 0xFFFFFF) * (1.0f / 16777216.0f);
+      v += a.noise_sigma * sqrtf(-2.f * logf(u1)) * cosf(6.283185307179586f * u2);
+    }
+    v = fminf(fmaxf(rintf(v), 0.f), a.vmax);
+    if (a.bpv == 1)
+      reinterpret_cast<unsigned char *>(a.vol)[idx] = (unsigned char)v;
+    else
+      reinterpret_cast<unsigned short *>(a.vol)[idx] = (unsigned short)v;
+  }
+}
+
+}  // namespace
+
+extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int bytes_per_voxel,
+                                    int n_blobs, const float *blobs, int deform,
+                                    const double *coef, float background, float noise_sigma,
+                                    unsigned long long noise_seed, float vmax, void *stream) {
+  if (!vol_dev || nx <= 0 || ny <= 0 || nz <= 0 || (bytes_per_voxel != 1 && bytes_per_voxel != 2) ||
+      n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 2 || (deform && !coef))
+    return dvc_internal_set_error(DVC_E_ARG, "bad synth arguments");
+  SynthArgs a{};
+  a.vol = vol_dev;
+  a.nx = nx;
+  a.ny = ny;
+  a.nz = nz;
+  a.bpv = bytes_per_voxel;
+  a.gx = (nx + kBin - 1) / kBin;
+  a.gy = (ny + kBin - 1) / kBin;
+  a.gz = (nz + kBin - 1) / kBin;
+  a.deform = deform;
+  a.background = background;
+  a.noise_sigma = noise_sigma;
+  a.vmax = vmax;
+  a.seed = noise_seed;
+  // deformed blob centres and bins (host)
+  double Ainv[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (deform == 1) {
+    const double *E = coef + 3;
+    const double A[9] = {1 + E[0], E[1], E[2], E[3], 1 + E[4], E[5], E[6], E[7], 1 + E[8]};
+    const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                       A[2] * (A[3] * A[7] - A[4] * A[6]);
+    Ainv[0] = (A[4] * A[8] - A[5] * A[7]) / det;
+    Ainv[1] = (A[2] * A[7] - A[1] * A[8]) / det;
+    Ainv[2] = (A[1] * A[5] - A[2] * A[4]) / det;
+    Ainv[3] = (A[5] * A[6] - A[3] * A[8]) / det;
+    Ainv[4] = (A[0] * A[8] - A[2] * A[6]) / det;
+    Ainv[5] = (A[2] * A[3] - A[0] * A[5]) / det;
+    Ainv[6] = (A[3] * A[7] - A[4] * A[6]) / det;
+    Ainv[7] = (A[1] * A[6] - A[0] * A[7]) / det;
+    Ainv[8] = (A[0] * A[4] - A[1] * A[3]) / det;
+    for (int i = 0; i < 9; i++) a.Ainv[i] = (float)Ainv[i];
+    for (int i = 0; i < 3; i++) {
+      a.t[i] = (float)coef[i];
+      a.c[i] = (float)coef[12 + i];
+    }
+  } else if (deform == 2) {
+    a.amp = (float)coef[0];
+    a.len = (float)coef[1];
+  }
+  const int nbins = a.gx * a.gy * a.gz;
+  std::vector<int> bin_of((size_t)n_blobs), count((size_t)nbins + 1, 0);
+  for (int k = 0; k < n_blobs; k++) {
+    const float *b = blobs + (size_t)k * 5;
+    double X[3] = {b[0], b[1], b[2]}, x[3] = {b[0], b[1], b[2]};
+    if (deform == 1) {
+      const double *E = coef + 3;
+      for (int i = 0; i < 3; i++)
+        x[i] = X[i] + coef[i] + E[i * 3 + 0] * (X[0] - coef[12]) + E[i * 3 + 1] * (X[1] - coef[13]) +
+               E[i * 3 + 2] * (X[2] - coef[14]);
+    } else if (deform == 2) {
+      const double w = 2.0 * M_PI / coef[1];
+      x[0] = X[0] + coef[0] * sin(w * X[1]);
+      x[1] = X[1] + coef[0] * sin(w * X[2]);
+      x[2] = X[2] + coef[0] * sin(w * X[0]);
+    }
+    int bx = std::min(std::max((int)floor(x[0] / kBin), 0), a.gx - 1);
+    int by = std::min(std::max((int)floor(x[1] / kBin), 0), a.gy - 1);
+    int bz = std::min(std::max((int)floor(x[2] / kBin), 0), a.gz - 1);
+    bin_of[(size_t)k] = (bz * a.gy + by) * a.gx + bx;
+    count[(size_t)bin_of[(size_t)k] + 1]++;
+  }
+  for (int b = 0; b < nbins; b++) count[(size_t)b + 1] += count[(size_t)b];
+  std::vector<int> fill(count.begin(), count.end() - 1);
+  std::vector<float> h_blob((size_t)std::max(n_blobs, 1) * 4), h_ar((size_t)std::max(n_blobs, 1) * 2);
+  for (int k = 0; k < n_blobs; k++) {
+    const float *b = blobs + (size_t)k * 5;
+    const int pos = fill[(size_t)bin_of[(size_t)k]]++;
+    h_blob[(size_t)pos * 4 + 0] = b[0];
+    h_blob[(size_t)pos * 4 + 1] = b[1];
+    h_blob[(size_t)pos * 4 + 2] = b[2];
+    h_blob[(size_t)pos * 4 + 3] = 1.0f / (2.0f * b[3] * b[3]);
+    h_ar[(size_t)pos * 2 + 0] = b[4];
+    h_ar[(size_t)pos * 2 + 1] = 16.0f * b[3] * b[3];
+  }
+  // blobs reach 4 sigma; bins are 16 voxels and neighbours one bin away, so
+  // sigma may not exceed 3.5 voxels (plus the deformation's local stretch)
+  for (int k = 0; k < n_blobs; k++)
+    if (blobs[(size_t)k * 5 + 3] > 3.5f) return dvc_internal_set_error(DVC_E_ARG, "blob sigma > 3.5");
+  void *d_blob = nullptr, *d_ar = nullptr, *d_start = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMalloc(&d_blob, h_blob.size() * 4) != cudaSuccess || cudaMalloc(&d_ar, h_ar.size() * 4) != cudaSuccess ||
+      cudaMalloc(&d_start, count.size() * 4) != cudaSuccess) {
+    cudaFree(d_blob);
+    cudaFree(d_ar);
+    cudaFree(d_start);
+    return dvc_internal_set_error(DVC_E_NOMEM, "synth buffers");
+  }
+  cudaMemcpy(d_blob, h_blob.data(), h_blob.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_ar, h_ar.data(), h_ar.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_start, count.data(), count.size() * 4, cudaMemcpyHostToDevice);
+  a.blobs = (const float4 *)d_blob;
+  a.amp_r2 = (const float2 *)d_ar;
+  a.bin_start = (const int *)d_start;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  synth_kernel<<<sms * 8, 256, 0, st>>>(a);
+  cudaError_t err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+  cudaFree(d_blob);
+  cudaFree(d_ar);
+  cudaFree(d_start);
+  if (err != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(err));
+  return DVC_OK;
+}

@@ -1,0 +1,216 @@
+"""Python mirror of the reference's hot-path interface over libdvcgpu.so.
+
+The reference exposes its hot path as C++ classes used by the `dvc` and
+`strain` programs: Search (process_point over the ROI points,
+Core/Search.cpp:95-192), Interpolate (nearest / tri_lin / tri_cub_Lek,
+Core/Interpolate.cpp:404-567), the objective functions
+(Core/ObjectiveFunctions.cpp) and the strain fit (Core/strain.cpp:402-591).
+This module binds the C ABI of include/dvc_gpu.h with ctypes and keeps the
+reference's names and argument meaning. There is no CPU path: every call runs
+on the GPU, and loading fails loudly when the CUDA library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (DvcParams, DvcStats, E_RANGE, OK, SEED_GIVEN, SEED_NEIGHBOURS, SEED_RIGID,
+                  make_params)
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libdvcgpu.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lib = None
+
+
+class DvcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"dvc_gpu error {code}: {msg}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load libdvcgpu.so (built by digitalvolumecorrelation_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"CUDA library {p} is missing: run `python -m "
+                           "digitalvolumecorrelation_gb300.build` (no CPU fallback exists)")
+    L = C.CDLL(p)
+    L.dvc_gpu_version.restype = C.c_char_p
+    L.dvc_gpu_last_error.restype = C.c_char_p
+    L.dvc_gpu_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(DvcParams), C.c_void_p,
+                                 C.c_void_p, C.c_int]
+    L.dvc_gpu_create_device.argtypes = [C.POINTER(C.c_void_p), C.POINTER(DvcParams), C.c_void_p,
+                                        C.c_void_p]
+    L.dvc_gpu_destroy.argtypes = [C.c_void_p]
+    L.dvc_gpu_destroy.restype = None
+    L.dvc_gpu_process.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int,
+                                  _dp, _ip, _dp, _dp, _ip, C.POINTER(DvcStats)]
+    L.dvc_gpu_process_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                         C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.dvc_gpu_interpolate.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
+    L.dvc_gpu_objective.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp]
+    L.dvc_gpu_strain.argtypes = [C.c_int, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double,
+                                 C.c_int, C.c_int, _dp, _ip, _dp, _dp, _dp, _dp]
+    L.dvc_gpu_synth_volume.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.POINTER(C.c_float), C.c_int, _dp, C.c_float, C.c_float,
+                                       C.c_ulonglong, C.c_float, C.c_void_p]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != OK:
+        raise DvcError(rc, _lib.dvc_gpu_last_error().decode())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class Engine:
+    """Both volumes resident on the GPU; Search::Search + Interpolate."""
+
+    def __init__(self, params: DvcParams, ref=None, cor=None, big_endian=False, ref_dev=None,
+                 cor_dev=None):
+        L = load()
+        self.params = params
+        self._h = C.c_void_p()
+        self._keep = []
+        if ref_dev is not None:
+            # device buffers (e.g. torch CUDA tensors): pass their addresses
+            self._keep = [ref_dev, cor_dev]
+            _check(L.dvc_gpu_create_device(C.byref(self._h), C.byref(params),
+                                           C.c_void_p(_dev_ptr(ref_dev)), C.c_void_p(_dev_ptr(cor_dev))))
+        else:
+            ref = np.ascontiguousarray(ref)
+            cor = np.ascontiguousarray(cor)
+            _check(L.dvc_gpu_create(C.byref(self._h), C.byref(params),
+                                    ref.ctypes.data_as(C.c_void_p), cor.ctypes.data_as(C.c_void_p),
+                                    int(big_endian)))
+
+    def close(self):
+        if self._h:
+            _lib.dvc_gpu_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def process(self, points, order=None, neigh=None, n_process=None, seed_mode=SEED_NEIGHBOURS,
+                seeds=None):
+        """Search::process_point over `order` (Core/dvc.cpp:233-303)."""
+        pts = np.ascontiguousarray(points, np.float64)
+        n = len(pts)
+        order = np.arange(n, dtype=np.int32) if order is None else np.ascontiguousarray(order, np.int32)
+        n_process = len(order) if n_process is None else int(n_process)
+        nn = 0
+        neigh_p = None
+        if neigh is not None and seed_mode == SEED_NEIGHBOURS:
+            neigh = np.ascontiguousarray(neigh, np.int32)
+            nn = neigh.shape[1]
+            neigh_p = _p(neigh, _ip)
+        seeds_p = None
+        if seed_mode == SEED_GIVEN:
+            seeds = np.ascontiguousarray(seeds, np.float64)
+            seeds_p = _p(seeds, _dp)
+        status = np.zeros(n, np.int32)
+        objmin = np.zeros(n)
+        par = np.zeros((n, 12))
+        its = np.zeros(n, np.int32)
+        st = DvcStats()
+        _check(_lib.dvc_gpu_process(self._h, n, _p(pts, _dp), n_process, _p(order, _ip), nn,
+                                    neigh_p, int(seed_mode), seeds_p, _p(status, _ip),
+                                    _p(objmin, _dp), _p(par, _dp), _p(its, _ip), C.byref(st)))
+        return dict(status=status, objmin=objmin, params=par, gn_iters=its,
+                    stats={f: getattr(st, f) for f, _ in DvcStats._fields_})
+
+    def process_device(self, n_points, points_dev, order_dev, n_process, neigh_dev, n_neigh,
+                       seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev=None,
+                       stream=0):
+        """Device-resident variant (torch CUDA tensors or raw pointers)."""
+        ptr = lambda t: C.c_void_p(_dev_ptr(t)) if t is not None else None
+        _check(_lib.dvc_gpu_process_device(self._h, int(n_points), ptr(points_dev), int(n_process),
+                                           ptr(order_dev), int(n_neigh), ptr(neigh_dev),
+                                           int(seed_mode), ptr(seeds_dev), ptr(status_dev),
+                                           ptr(objmin_dev), ptr(params_dev), ptr(gn_iters_dev),
+                                           C.c_void_p(stream)))
+
+    def interpolate(self, volume, center, pts, interp_type=2):
+        """Interpolate::center_on + nearest/tri_lin/tri_cub_Lek; None on Intrp_Fail."""
+        pts = np.ascontiguousarray(pts, np.float64)
+        out = np.zeros(len(pts))
+        c = np.ascontiguousarray(center, np.float64)
+        rc = _lib.dvc_gpu_interpolate(self._h, int(volume), _p(c, _dp), len(pts), _p(pts, _dp),
+                                      int(interp_type), _p(out, _dp))
+        if rc == E_RANGE:
+            return None
+        _check(rc)
+        return out
+
+
+def _dev_ptr(t):
+    if isinstance(t, int):
+        return t
+    return int(t.data_ptr())
+
+
+def objective(fcn, ref, tar, residual=False):
+    """obj_SAD .. obj_ZNSSD on the GPU (FP64)."""
+    load()
+    ref = np.ascontiguousarray(ref, np.float64)
+    tar = np.ascontiguousarray(tar, np.float64)
+    o = C.c_double()
+    res = np.zeros(len(ref)) if residual else None
+    _check(_lib.dvc_gpu_objective(int(fcn), len(ref), _p(ref, _dp), _p(tar, _dp), C.byref(o),
+                                  _p(res, _dp) if residual else None))
+    return (o.value, res) if residual else o.value
+
+
+def strain(pts, status, objmin, disp, neigh, ndp=25, objt=1.0, refill=False, planar=0):
+    """Strain-window fit of the `strain` program (Core/strain.cpp:402-591)."""
+    load()
+    n = len(pts)
+    pts = np.ascontiguousarray(pts, np.float64)
+    status = np.ascontiguousarray(status, np.int32)
+    objmin = np.ascontiguousarray(objmin, np.float64)
+    disp = np.ascontiguousarray(disp, np.float64)
+    neigh = np.ascontiguousarray(neigh, np.int32)
+    out = dict(u_fit=np.zeros((n, 3)), pts_in_sw=np.zeros(n, np.int32), sw_radius=np.zeros(n),
+               e_strain=np.zeros((n, 9)), l_strain=np.zeros((n, 9)), dgrad=np.zeros((n, 9)))
+    _check(_lib.dvc_gpu_strain(n, _p(pts, _dp), _p(status, _ip), _p(objmin, _dp), _p(disp, _dp),
+                               neigh.shape[1], _p(neigh, _ip), int(ndp), float(objt), int(refill),
+                               int(planar), _p(out["u_fit"], _dp), _p(out["pts_in_sw"], _ip),
+                               _p(out["sw_radius"], _dp), _p(out["e_strain"], _dp),
+                               _p(out["l_strain"], _dp), _p(out["dgrad"], _dp)))
+    return out
+
+
+def synth_volume_device(vol_dev, shape_xyz, bytes_per_voxel, blobs, deform=None,
+                        background=0.0, noise_sigma=2.0, noise_seed=1, vmax=None, stream=0):
+    """Render a speckle volume into a device buffer (see dvc_gpu_synth_volume)."""
+    load()
+    b = np.ascontiguousarray(blobs, np.float32)
+    kind = 0 if deform is None else deform.kind
+    coef = np.ascontiguousarray(deform.coef() if deform is not None and kind else [0.0], np.float64)
+    vmax = float(255 if bytes_per_voxel == 1 else 65535) if vmax is None else float(vmax)
+    nx, ny, nz = shape_xyz
+    _check(_lib.dvc_gpu_synth_volume(C.c_void_p(_dev_ptr(vol_dev)), nx, ny, nz, bytes_per_voxel,
+                                     len(b), b.ctypes.data_as(C.POINTER(C.c_float)), kind,
+                                     _p(coef, _dp), background, noise_sigma, noise_seed, vmax,
+                                     C.c_void_p(stream)))
+
+
+__all__ = ["Engine", "objective", "strain", "synth_volume_device", "make_params", "load",
+           "DvcError", "SEED_NEIGHBOURS", "SEED_GIVEN", "SEED_RIGID"]

@@ -203,13 +203,17 @@ struct Interp {
         vb[k * 8 + c] = q[vi(xx, yy, zz) * 8 + k];
       }
     const auto &B = bi().m;
-    double *a = &co[vi(x, y, z) * 64];
     // sparse column-major product order of the reference: y(i) += A(i,j) x(j)
-    // for columns j ascending (exact here: integer BI, dyadic vb)
-    for (int r = 0; r < 64; r++) a[r] = 0.0;
+    // for columns j ascending (exact here: integer BI, dyadic vb). Built in a
+    // local array and stored whole, so two threads filling the same cell
+    // store identical values (the reference's lazy fill races the same way).
+    double va[64];
+    for (int r = 0; r < 64; r++) va[r] = 0.0;
     for (int c = 0; c < 64; c++)
       for (int r = 0; r < 64; r++)
-        if (B[r][c] != 0.0) a[r] += B[r][c] * vb[c];
+        if (B[r][c] != 0.0) va[r] += B[r][c] * vb[c];
+    double *a = &co[vi(x, y, z) * 64];
+    for (int r = 0; r < 64; r++) a[r] = va[r];
   }
 
   // cell + remainder of one point relative to est_box (Core/Interpolate.cpp:494-496,517-524)

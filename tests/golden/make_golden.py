@@ -1,0 +1,202 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Run here, where the reference sources exist:
+
+    python tests/golden/make_golden.py
+
+It builds the reference's own Core/*.cpp (oracle/build_ref.sh) and records,
+on small seeded synthetic volumes, what the reference computes:
+  * interpolation values (Interpolate::nearest / tri_lin / tri_cub_Lek),
+  * objective values and residuals (obj_SAD .. obj_ZNSSD),
+  * whole-search results (Search::process_point over a point grid, in the
+    reference's order with its neighbour seeding, sphere test seed 1),
+  * strain-program CSV outputs (the reference `strain` executable),
+  * the 10-nearest-neighbour table of the reference's own DataCloud test
+    (Core/tests/test_DataCloud.cpp:129-139 over Core/tests/grid_input.roi).
+The GPU machine has no reference sources, so its tests read these files.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from digitalvolumecorrelation_gb300 import synth  # noqa: E402
+from digitalvolumecorrelation_gb300.abi import make_params  # noqa: E402
+from oracle.oracle import REF_SO, Oracle, Reference, build_reference  # noqa: E402
+
+REF_DIR = os.environ.get("DVC_REFERENCE_DIR", "/root/reference")
+SHAPE = (40, 40, 40)
+
+# search configurations run by the reference (volume set, params)
+SEARCH_CASES = [
+    ("A", dict(subvol_geom="cube", subvol_size=11, subvol_npts=300, obj_function="znssd",
+               interp_type="tricubic", num_srch_dof=6, disp_max=3, basin_radius=1.5)),
+    ("A", dict(subvol_geom="sphere", subvol_size=11, subvol_npts=300, obj_function="znssd",
+               interp_type="tricubic", num_srch_dof=12, disp_max=3, basin_radius=1.0)),
+    ("A", dict(subvol_geom="cube", subvol_size=9, subvol_npts=200, obj_function="ssd",
+               interp_type="tricubic", num_srch_dof=3, disp_max=2, basin_radius=0.0)),
+    ("A", dict(subvol_geom="cube", subvol_size=9, subvol_npts=125, obj_function="zssd",
+               interp_type="trilinear", num_srch_dof=6, disp_max=2, basin_radius=1.0)),
+    ("A", dict(subvol_geom="sphere", subvol_size=11, subvol_npts=250, obj_function="nssd",
+               interp_type="tricubic", num_srch_dof=6, disp_max=2, basin_radius=2.0)),
+    ("A", dict(subvol_geom="cube", subvol_size=11, subvol_npts=343, obj_function="sad",
+               interp_type="nearest", num_srch_dof=3, disp_max=2, basin_radius=1.0)),
+    ("B", dict(subvol_geom="sphere", subvol_size=13, subvol_npts=400, obj_function="znssd",
+               interp_type="tricubic", num_srch_dof=12, disp_max=3, basin_radius=1.5)),
+    ("B", dict(subvol_geom="cube", subvol_size=11, subvol_npts=343, obj_function="znssd",
+               interp_type="tricubic", num_srch_dof=6, disp_max=3, basin_radius=3.0)),
+]
+
+
+def volumes():
+    bA = synth.blobs(SHAPE, 90, seed=11)
+    affA = synth.Affine(t=(1.3, -0.7, 0.4), E=((0.005, 0, 0), (0, 0.005, 0), (0, 0, 0.005)),
+                        c=(20.0, 20.0, 20.0))
+    A_ref = synth.render(SHAPE, bA, noise_sigma=2.0, noise_seed=12)
+    A_cor = synth.render(SHAPE, bA, deform=affA, noise_sigma=2.0, noise_seed=13)
+    bB = synth.blobs(SHAPE, 110, amp=(2000.0, 60000.0), seed=21)
+    sinB = synth.Sinusoid(A=1.2, L=48.0)
+    B_ref = synth.render(SHAPE, bB, noise_sigma=150.0, noise_seed=22, dtype=np.uint16)
+    B_cor = synth.render(SHAPE, bB, deform=sinB, noise_sigma=150.0, noise_seed=23, dtype=np.uint16)
+    return {"A": (A_ref, A_cor), "B": (B_ref, B_cor)}
+
+
+def datacloud_golden():
+    roi = os.path.join(REF_DIR, "Core", "tests", "grid_input.roi")
+    src = open(os.path.join(REF_DIR, "Core", "tests", "test_DataCloud.cpp")).read()
+    block = re.search(r"std::vector<int> row = \{(.*?)\};", src, re.S).group(1)
+    table = [int(v) for v in re.findall(r"-?\d+", block)]
+    pts = []
+    for line in open(roi):
+        f = line.split()
+        if len(f) >= 4:
+            pts.append([float(f[1]), float(f[2]), float(f[3])])
+    return dict(points=pts, knn10=np.array(table).reshape(10, 10).tolist(),
+                source="Core/tests/test_DataCloud.cpp:129-139, Core/tests/grid_input.roi")
+
+
+def strain_golden(tmp):
+    """Run the reference `strain` program on a synthetic .disp/.sort.csv."""
+    rng = np.random.default_rng(5)
+    g = synth.grid_points((6, 6, 6), 10.0, (60.0, 70.0, 80.0))
+    n = len(g)
+    X = g - np.array([60.0, 70.0, 80.0])
+    disp = (np.array([0.3, -0.2, 0.1]) + X @ np.array([[0.004, 0.001, 0.0], [0.0, -0.003, 0.002],
+                                                          [0.001, 0.0, 0.002]]).T
+            + 1e-4 * X ** 2 + rng.normal(0, 0.01, (n, 3)))
+    status = np.zeros(n, np.int32)
+    status[rng.choice(n, 12, replace=False)] = -1
+    objmin = rng.uniform(0.001, 0.2, n)
+    disp[status != 0] = 0.0
+    objmin[status != 0] = 0.0
+    O = Oracle()
+    order, neigh = O.order_neighbours(g)
+    out = {}
+    for name, pts, args in [("vol", g, ["-sw", "20", "-A"]),
+                            ("vol_t", g, ["-sw", "15", "-t", "0.1", "-r", "-A"]),
+                            ("planar", g * np.array([1, 1, 0]) + np.array([0, 0, 55.0]), ["-sw", "12", "-A"])]:
+        d = os.path.join(tmp, name)
+        os.makedirs(d, exist_ok=True)
+        base = os.path.join(d, "run")
+        with open(base + ".disp", "w") as f:
+            f.write("n\tx\ty\tz\tstatus\tobjmin\tu\tv\tw\n")
+            for i in range(n):
+                f.write(f"{i + 1}\t{pts[i, 0]:.6g}\t{pts[i, 1]:.6g}\t{pts[i, 2]:.6g}\t{status[i]}\t"
+                        f"{objmin[i]:.6g}\t{disp[i, 0]:.6f}\t{disp[i, 1]:.6f}\t{disp[i, 2]:.6f}\n")
+        _, nb = O.order_neighbours(pts)
+        with open(base + ".sort.csv", "w") as f:
+            for row in nb:
+                f.write(",".join(str(v) for v in row) + "\n")
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "strain"), base + ".disp",
+                        base + ".sort.csv"] + args, cwd=d, check=True, capture_output=True)
+        # the values exactly as the reference read them back from the text files
+        rows = [l.split() for l in open(base + ".disp")][1:]
+        pts = np.array([[float(r[1]), float(r[2]), float(r[3])] for r in rows])
+        objmin = np.array([float(r[5]) for r in rows])
+        disp = np.array([[float(r[6]), float(r[7]), float(r[8])] for r in rows])
+        res = {}
+        for kind in ("Lstr", "Estr", "dgrd"):
+            fn = [x for x in os.listdir(d) if x.endswith(f".{kind}.csv")][0]
+            rows = [l.strip().split(",") for l in open(os.path.join(d, fn))][1:]
+            res[kind] = np.array([[float(v) for v in r] for r in rows])
+        out[name] = dict(points=pts, status=status, objmin=objmin, disp=disp, neigh=nb,
+                         args=args, **res)
+    return out
+
+
+def main():
+    if not os.path.exists(REF_SO):
+        if build_reference() is None:
+            raise SystemExit("reference sources not available")
+    R = Reference()
+    vols = volumes()
+    rng = np.random.default_rng(7)
+    out = {}
+    # interpolation
+    for vs, (vref, vcor) in vols.items():
+        bpv = 1 if vref.dtype == np.uint8 else 2
+        p = make_params(SHAPE, bytes_per_voxel=bpv, subvol_size=11, subvol_npts=300, disp_max=3)
+        center = np.array([19.6, 20.3, 20.45])
+        pts = center + rng.uniform(-9.4, 9.4, (400, 3))
+        # the box's last cell plane (index n-1) is undefined in the reference
+        # (it reads past its arrays): stay below it, and put 40 samples in the
+        # face cells n-2 of each axis, where the face rule of the derivatives applies
+        last = np.floor(center - 10.5) + 20.0  # first coordinate of cell n-1 (n = 21)
+        pts = np.minimum(pts, last - 0.01)
+        for d in range(3):
+            pts[40 * d:40 * (d + 1), d] = last[d] - 1.0 + rng.uniform(0.0, 0.99, 40)
+        for it in range(3):
+            out[f"interp_{vs}_{it}_pts"] = pts
+            out[f"interp_{vs}_{it}_val"] = R.interpolate(p, vcor, center, pts, it)
+            out[f"interp_{vs}_{it}_center"] = center
+    # objectives
+    r = rng.uniform(0, 255, 500)
+    t = r + rng.normal(0, 10, 500)
+    out["obj_ref"] = r
+    out["obj_tar"] = t
+    for f in range(5):
+        o, res = R.objective(f, r, t, True)
+        out[f"obj_{f}_val"] = np.array([o])
+        out[f"obj_{f}_res"] = res
+    # searches
+    pts = synth.grid_points((3, 3, 3), 5.0, (20.0, 20.0, 20.0))
+    O = Oracle()
+    order, neigh = R.order_neighbours(pts)
+    for k, (vs, kw) in enumerate(SEARCH_CASES):
+        vref, vcor = vols[vs]
+        bpv = 1 if vref.dtype == np.uint8 else 2
+        p = make_params(SHAPE, bytes_per_voxel=bpv, **kw)
+        res = R.process(p, vref, cor=vcor, points=pts, order=order, neigh=neigh)
+        out[f"search_{k}_status"] = res["status"]
+        out[f"search_{k}_objmin"] = res["objmin"]
+        out[f"search_{k}_params"] = res["params"]
+    out["search_points"] = pts
+    out["search_order"] = order
+    out["search_neigh"] = neigh
+    for vs, (vref, vcor) in vols.items():
+        out[f"vol_{vs}_ref"] = vref
+        out[f"vol_{vs}_cor"] = vcor
+    np.savez_compressed(os.path.join(HERE, "reference_hotpath.npz"), **out)
+    with open(os.path.join(HERE, "search_cases.json"), "w") as f:
+        json.dump([dict(volumes=vs, **kw) for vs, kw in SEARCH_CASES], f, indent=1)
+    with tempfile.TemporaryDirectory() as tmp:
+        st = strain_golden(tmp)
+    np.savez_compressed(os.path.join(HERE, "reference_strain.npz"),
+                        **{f"{c}_{k}": np.asarray(v) for c, d in st.items() for k, v in d.items()})
+    with open(os.path.join(HERE, "datacloud_knn.json"), "w") as f:
+        json.dump(datacloud_golden(), f, indent=1)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

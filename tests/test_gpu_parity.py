@@ -1,0 +1,140 @@
+"""GPU engine parity: the CUDA path through the C ABI against the reference's
+recorded outputs (tests/golden) and the FP64 oracle.
+
+Tolerances (the engine computes per-sample work in FP32, reductions
+compensated, the normal-equation solve in FP64):
+  * interpolated values: |d| <= 2e-6 x full scale (255 or 65535);
+  * objectives (FP64 path): 1e-12 relative;
+  * searches: status identical; u, v, w within 1e-3 voxel; objmin within
+    1e-5 relative (converged points), rotation/strain within 1e-3.
+"""
+import numpy as np
+import pytest
+
+from fixtures import (SHAPE, case_params, hotpath, interp_params, planar_flag, search_cases,
+                      strain_cases, strain_flags)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng(gpu_lib):
+    from digitalvolumecorrelation_gb300 import engine
+    return engine
+
+
+@pytest.mark.parametrize("vs", ["A", "B"])
+@pytest.mark.parametrize("it", [0, 1, 2])
+def test_interpolation_vs_reference(eng, vs, it):
+    d = hotpath()
+    p = interp_params(vs)
+    E = eng.Engine(p, d[f"vol_{vs}_ref"], d[f"vol_{vs}_cor"])
+    got = E.interpolate(1, d[f"interp_{vs}_{it}_center"], d[f"interp_{vs}_{it}_pts"], it)
+    ref = d[f"interp_{vs}_{it}_val"]
+    full = 255.0 if vs == "A" else 65535.0
+    assert np.max(np.abs(got - ref)) <= 2e-6 * full
+    E.close()
+
+
+def test_interpolation_range_fail(eng):
+    d = hotpath()
+    p = interp_params("A")
+    E = eng.Engine(p, d["vol_A_ref"], d["vol_A_cor"])
+    c = np.array([20.0, 20.0, 20.0])
+    assert E.interpolate(1, c, np.array([[c[0] + 9.6, 20.0, 20.0]]), 2) is None
+    assert E.interpolate(1, c, np.array([[c[0] + 9.4, 20.0, 20.0]]), 2) is not None
+
+
+@pytest.mark.parametrize("fcn", range(5))
+def test_objective_vs_reference(eng, fcn):
+    d = hotpath()
+    o, res = eng.objective(fcn, d["obj_ref"], d["obj_tar"], residual=True)
+    np.testing.assert_allclose(o, d[f"obj_{fcn}_val"][0], rtol=1e-12)
+    np.testing.assert_allclose(res, d[f"obj_{fcn}_res"], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("k", range(8))
+def test_search_vs_reference(eng, k):
+    d = hotpath()
+    case = search_cases()[k]
+    p = case_params(case)
+    vs = case["volumes"]
+    E = eng.Engine(p, d[f"vol_{vs}_ref"], d[f"vol_{vs}_cor"])
+    r = E.process(d["search_points"], order=d["search_order"], neigh=d["search_neigh"])
+    st = d[f"search_{k}_status"]
+    np.testing.assert_array_equal(r["status"], st)
+    good = st == 0
+    du = np.abs(r["params"][good, :3] - d[f"search_{k}_params"][good, :3])
+    assert du.max() <= 1e-3, du.max()
+    ndof = case["num_srch_dof"]
+    if ndof > 3:
+        dr = np.abs(r["params"][good, 3:ndof] - d[f"search_{k}_params"][good, 3:ndof])
+        assert dr.max() <= 1e-3, dr.max()
+    ro = d[f"search_{k}_objmin"][good]
+    rel = np.abs(r["objmin"][good] - ro) / np.maximum(np.abs(ro), 1e-300)
+    assert rel.max() <= 1e-5, rel.max()
+    E.close()
+
+
+@pytest.mark.parametrize("name", ["vol", "vol_t", "planar"])
+def test_strain_vs_reference(eng, name):
+    c = strain_cases()[name]
+    ndp, objt, refill = strain_flags(c["args"])
+    pts = c["points"]
+    out = eng.strain(pts, c["status"], c["objmin"], c["disp"], c["neigh"], ndp=ndp, objt=objt,
+                     refill=refill, planar=planar_flag(pts))
+    L, E, D = c["Lstr"], c["Estr"], c["dgrd"]
+    np.testing.assert_array_equal(out["pts_in_sw"], L[:, 7].astype(int))
+    for got, printed in ((out["u_fit"], L[:, 4:7]), (out["sw_radius"], L[:, 8]),
+                         (out["l_strain"], L[:, 9:18]), (out["e_strain"], E[:, 9:18]),
+                         (out["dgrad"], D[:, 9:18])):
+        printed = np.asarray(printed)
+        mag = np.where(printed == 0, 1e-300, np.abs(printed))
+        tol = np.maximum(0.5001 * 10.0 ** (np.floor(np.log10(mag)) - 5), 1e-12)
+        assert np.all(np.abs(got - printed) <= tol)
+
+
+def test_strain_vs_oracle_random(eng, oracle):
+    rng = np.random.default_rng(3)
+    from digitalvolumecorrelation_gb300 import synth
+    pts = synth.grid_points((7, 7, 7), 9.0, (100.0, 90.0, 80.0)) + rng.normal(0, 0.5, (343, 3))
+    disp = 0.01 * (pts - 90.0) + rng.normal(0, 0.01, (343, 3))
+    status = np.where(rng.uniform(size=343) < 0.1, -1, 0).astype(np.int32)
+    objmin = rng.uniform(0, 0.3, 343)
+    _, neigh = oracle.order_neighbours(pts)
+    for ndp, objt, refill in ((25, 1.0, False), (40, 0.2, True), (10, 1.0, True)):
+        a = eng.strain(pts, status, objmin, disp, neigh, ndp, objt, refill)
+        b = oracle.strain(pts, status, objmin, disp, neigh, ndp, objt, refill)
+        np.testing.assert_array_equal(a["pts_in_sw"], b["pts_in_sw"])
+        for k in ("u_fit", "sw_radius", "e_strain", "l_strain", "dgrad"):
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-7, atol=1e-10)
+
+
+def test_given_seed_mode_vs_oracle(eng, oracle):
+    """Independent points with caller seeds (the throughput path) on a larger
+    volume, uint8 cube and uint16 sphere."""
+    from digitalvolumecorrelation_gb300 import synth
+    rng = np.random.default_rng(9)
+    shape = (72, 72, 72)
+    b = synth.blobs(shape, 500, seed=31)
+    aff = synth.Affine(t=(0.8, -1.4, 2.1), E=((0.004, 0.001, 0), (0, -0.003, 0), (0, 0, 0.006)),
+                       c=(36.0, 36.0, 36.0))
+    ref = synth.render(shape, b, noise_sigma=2.0, noise_seed=32)
+    cor = synth.render(shape, b, deform=aff, noise_sigma=2.0, noise_seed=33)
+    pts = synth.grid_points((4, 4, 4), 7.0, (36.0, 36.0, 36.0))
+    seeds = aff.u(pts) + rng.normal(0, 0.7, pts.shape)
+    for kw in (dict(subvol_geom="cube", subvol_size=17, subvol_npts=1000, num_srch_dof=12,
+                    disp_max=4, basin_radius=2.0),
+               dict(subvol_geom="sphere", subvol_size=19, subvol_npts=1500, num_srch_dof=6,
+                    disp_max=4, basin_radius=0.0)):
+        from digitalvolumecorrelation_gb300.abi import make_params
+        p = make_params(shape, **kw)
+        E = eng.Engine(p, ref, cor)
+        g = E.process(pts, seed_mode=1, seeds=seeds)
+        o = oracle.process(p, ref, cor, pts, seed_mode=1, seeds=seeds)
+        np.testing.assert_array_equal(g["status"], o["status"])
+        good = o["status"] == 0
+        assert np.abs(g["params"][good, :3] - o["params"][good, :3]).max() <= 1e-3
+        rel = np.abs(g["objmin"][good] - o["objmin"][good]) / o["objmin"][good]
+        assert rel.max() <= 1e-5
+        E.close()

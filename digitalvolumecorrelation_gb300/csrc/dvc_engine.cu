@@ -1247,6 +1247,7 @@ struct dvc_engine {
   // grow-only per-call workspace
   void *ws = nullptr;
   size_t ws_bytes = 0;
+  size_t counters_off = 0;  // offset of the last call's counters in ws
   int num_sms = 0;
 };
 
@@ -1359,8 +1360,8 @@ int ensure_ws(dvc_engine *e, size_t bytes) {
 template <typename VT, int IT>
 int launch_search(dvc_engine *e, SearchArgs &a, size_t smem_dyn, int grid, cudaStream_t st) {
   auto kern = search_kernel<VT, IT>;
-  if (smem_dyn > 48 * 1024)
-    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dyn));
+  // static + dynamic shared memory may exceed the 48 KB default: opt in
+  CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dyn));
   kern<<<grid, kThreads, smem_dyn, st>>>(a);
   CUDA_TRY(cudaGetLastError());
   return DVC_OK;
@@ -1369,8 +1370,7 @@ int launch_search(dvc_engine *e, SearchArgs &a, size_t smem_dyn, int grid, cudaS
 template <typename VT, int IT>
 int occupancy(size_t smem_dyn, int *blocks) {
   auto kern = search_kernel<VT, IT>;
-  if (smem_dyn > 48 * 1024)
-    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dyn));
+  CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dyn));
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, kThreads, smem_dyn));
   return DVC_OK;
 }
@@ -1519,6 +1519,7 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
   int *ctl = (int *)(ws + off_ctl);
   unsigned long long *counters = (unsigned long long *)(ws + off_ctl + 64);
   CUDA_TRY(cudaMemsetAsync(ws + off_ctl, 0, 256, st));
+  e->counters_off = off_ctl + 64;
   {
     const int T = 256;
     const int G = (n_points + T - 1) / T;
@@ -1674,6 +1675,17 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
     stats->total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
+  return DVC_OK;
+}
+
+int dvc_gpu_last_counters(dvc_engine *e, long long out[3]) {
+  if (!e || !out) return set_error(DVC_E_ARG, "null argument");
+  out[0] = out[1] = out[2] = 0;
+  if (!e->ws) return DVC_OK;
+  unsigned long long c[3];
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(c, (char *)e->ws + e->counters_off, sizeof c, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 3; k++) out[k] = (long long)c[k];
   return DVC_OK;
 }
 

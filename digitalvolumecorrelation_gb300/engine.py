@@ -56,6 +56,7 @@ def load(path: str | None = None):
     L.dvc_gpu_process_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                          C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.dvc_gpu_last_counters.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
     L.dvc_gpu_interpolate.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
     L.dvc_gpu_objective.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp]
     L.dvc_gpu_strain.argtypes = [C.c_int, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double,
@@ -146,6 +147,13 @@ class Engine:
                                            int(seed_mode), ptr(seeds_dev), ptr(status_dev),
                                            ptr(objmin_dev), ptr(params_dev), ptr(gn_iters_dev),
                                            C.c_void_p(stream)))
+
+    def last_counters(self):
+        """(evaluations, Gauss-Newton iterations, undefined-cell evaluations)
+        of the most recent search on this engine."""
+        out = (C.c_longlong * 3)()
+        _check(_lib.dvc_gpu_last_counters(self._h, out))
+        return tuple(int(v) for v in out)
 
     def interpolate(self, volume, center, pts, interp_type=2):
         """Interpolate::center_on + nearest/tri_lin/tri_cub_Lek; None on Intrp_Fail."""

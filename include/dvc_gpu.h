@@ -108,7 +108,8 @@ int dvc_gpu_abi_version(void);
 int dvc_gpu_create(dvc_engine **out, const dvc_params *p, const void *ref_vox,
                    const void *cor_vox, int big_endian);
 /* Same, for volumes already in device memory (the engine keeps the pointers;
-   the caller keeps the buffers alive). */
+   the caller keeps the buffers alive). Each buffer must be readable for 64
+   bytes past its last voxel (aligned row loads over-read the end). */
 int dvc_gpu_create_device(dvc_engine **out, const dvc_params *p, const void *ref_vox_dev,
                           const void *cor_vox_dev);
 void dvc_gpu_destroy(dvc_engine *e);
@@ -145,6 +146,15 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
                            const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
                            const double *seeds_dev, int *status_dev, double *objmin_dev,
                            double *params_dev, int *gn_iters_dev, void *stream);
+
+/* Counters of the most recent dvc_gpu_process / dvc_gpu_process_device call
+   on this engine (waits for it to finish): out[0] objective evaluations
+   (reference subvolume, grid offsets, Gauss-Newton evaluations, final
+   objective), out[1] Gauss-Newton iterations, out[2] sample evaluations that
+   fell in the interpolation box's last cell plane, which the reference leaves
+   undefined. The reference reports run counts only as pt/sec and status
+   percentages in its .stat file (Core/dvc.cpp:322-338). */
+int dvc_gpu_last_counters(dvc_engine *e, long long out[3]);
 
 /* ---- function-level entry points ----------------------------------------
  * Interpolate one volume (0 = reference, 1 = correlate) at n points, with the

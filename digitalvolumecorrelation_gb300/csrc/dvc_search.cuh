@@ -1,0 +1,1069 @@
+// dvc_search.cuh — the per-point DVC search kernel.
+//
+// One persistent launch processes every ROI point. A thread-block cluster of
+// C CTAs (C = 1..8, on C SMs) cooperates on one point at a time: the point's
+// subvolume samples are split into C contiguous ranges, each CTA evaluates
+// its range, and every sum the search needs (objective statistics, grid
+// objectives, Gauss-Newton normal equations, bounding boxes) is reduced
+// CTA-locally and then across the cluster through distributed shared memory,
+// in a fixed order, so every CTA of the cluster holds identical totals and
+// takes identical decisions. The cluster's leader CTA takes the next point in
+// processing order from a device work counter, waits (bounded) for the
+// neighbours that precede it when the reference's seeding is used, and
+// publishes the result with a release flag. Points are handed out in order,
+// so every awaited neighbour is owned by a cluster that is already running.
+//
+// Reference map (Core/...):
+//   process_point            Search.cpp:95-192       -> search_kernel (per point)
+//   starting_param           Search.cpp:277-377      -> point_seed
+//   search_pt_setup          Search.cpp:248-275      -> point_seed + set-up phase
+//   trgrid_global            Search.cpp:934-1043     -> grid phase
+//   min_Lev_Mar, LM_prep_at  Search.cpp:194-246,490-525 -> Gauss-Newton phase
+//   obj_val_at               Search.cpp:448-488      -> the evaluation loops
+//   affine_to                FloatingCloud.cpp:236-286 -> sample_pos + warp_matrices
+//   set_param_vect           SearchParams.cpp:53-107  -> warp_matrices
+//   tri_cub_Lek / tri_lin / nearest Interpolate.cpp:404-567 -> interp_sample
+//   obj_SAD .. obj_ZNSSD     ObjectiveFunctions.cpp:24-263 -> objective sums
+#pragma once
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "../../include/dvc_gpu.h"
+#include "dvc_device.cuh"
+
+namespace dvc {
+namespace cg = cooperative_groups;
+
+constexpr int kGridChunk = 128;               // grid offsets reduced together
+constexpr long long kWaitPolls = 1LL << 25;   // bounded dependency wait (~seconds)
+constexpr int kCB = 384;                      // cluster reduction buffer length
+constexpr int kGRows = kMaxDof + 3;           // Gauss-Newton chunk rows: g[12], 1, t', q
+
+struct SearchArgs {
+  const void *ref, *cor;
+  int nx, ny, nz;
+  int geom, ndof, objfcn, itype;
+  int n_sub, cube_n;
+  double subv_rad, aspect[3];
+  double nom_mn[3], nom_mx[3], nom_cen[3];  // nominal interpolation box (Search::Search)
+  int bext[3];                              // its integer extents
+  int do_grid, num_inc;
+  double inc;
+  double rigid[3];
+  const double *sphere_rel;  // n_sub*3 uniform offsets (sphere)
+  int n_points, n_process, n_neigh, seed_mode;
+  const double *pts;
+  const int *order, *rank, *neigh;
+  const double *seeds;
+  int *status;
+  double *objmin, *params;
+  int *gn_iters;
+  int *work_counter, *done, *error_flag;
+  unsigned long long *counters;  // [0] evaluations, [1] GN iterations, [2] undefined evals
+  int local_cap;                 // per-CTA sample capacity of the dynamic arrays
+};
+
+struct DBox {
+  double mn[3], mx[3];
+};
+
+// Point description broadcast by the cluster's leader CTA.
+struct PointHeader {
+  int rank, n, flag;  // flag 0: search, 1: no more work, 2: dependency wait gave up
+  int pad;
+  double pt[3], seed[3];
+  DBox act_cor;
+  int o_ref[3], o_cor[3];
+  int chk_ref, chk_cor;
+};
+
+struct CtaState {
+  PointHeader H;
+  double sref[3], sbmn[3], sbmx[3];
+  int kint[3];        // s_ref + seed - O_cor: integer part
+  float kfrac[3];     //                       fractional part
+  float shift;        // value shift of the objective sums
+  double rsum2;       // sum of squared reference quantities
+  double par[kMaxDof];
+  double upd[3];
+  int iu[3];
+  float fu[3];
+  float M[9], R[9], N[27];  // (I+S)R - I, R, (I+S) dR/dangle
+  int use_rot, fail, stop, best;
+  double best_obj, obj, obj_old;
+  int giu[kGridChunk][3];
+  float gfu[kGridChunk][3];
+  double objv[kGridChunk];
+  float wpart[kWarps][kGridChunk * 3];
+  double cbuf[2][kCB];
+  double red[kCB];
+  float wred[kWarps][2 * 8];
+  double wredd[kWarps][8];
+  double A[kMaxDof * kMaxDof], b[kMaxDof], x[kMaxDof], v[kMaxDof], diag[kMaxDof], vv;
+  double ut[kMaxDof], jte[kMaxDof], scal[4];
+  int perm[kMaxDof];
+};
+
+struct Cl {
+  cg::cluster_group g;
+  unsigned rank, size;
+  int parity;
+};
+
+__device__ __forceinline__ int itrunc_d(double v) { return (int)v; }
+
+__device__ __forceinline__ void split_d(double v, int &i, float &f) {
+  const double fl = floor(v);
+  i = (int)fl;
+  f = (float)(v - fl);
+}
+
+// ------------------------------------------------------------ reductions ---
+// The CTA's values are in S.cbuf[parity][0..K); entries [0, nmin) combine with
+// min, the rest with +, over the cluster's CTAs in rank order. Result: S.red.
+__device__ __forceinline__ void cluster_reduce(Cl &c, CtaState &S, int K, int nmin) {
+  c.g.sync();
+  for (int k = threadIdx.x; k < K; k += kThreads) {
+    double t = k < nmin ? 1e300 : 0.0;
+    for (unsigned r = 0; r < c.size; r++) {
+      const double *rem = c.g.map_shared_rank(&S.cbuf[c.parity][0], r);
+      const double v = rem[k];
+      t = k < nmin ? fmin(t, v) : t + v;
+    }
+    S.red[k] = t;
+  }
+  c.parity ^= 1;
+  __syncthreads();
+}
+
+// CTA-level compensated sum of K (<= 8) Kahan partials into dst[0..K) (FP64).
+template <int K>
+__device__ __forceinline__ void cta_sum_comp(KSum (&v)[K], CtaState &S, double *dst) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float hi[K], lo[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    hi[k] = v[k].s;
+    lo[k] = -v[k].c;
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++)
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const float bh = __shfl_xor_sync(0xffffffffu, hi[k], o);
+      const float bl = __shfl_xor_sync(0xffffffffu, lo[k], o);
+      two_sum_merge(hi[k], lo[k], bh, bl);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      S.wred[warp][2 * k] = hi[k];
+      S.wred[warp][2 * k + 1] = lo[k];
+    }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+    for (int w = 0; w < kWarps; w++) s += (double)S.wred[w][2 * threadIdx.x] + (double)S.wred[w][2 * threadIdx.x + 1];
+    dst[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// CTA-level min of K (<= 8) doubles into dst.
+template <int K>
+__device__ __forceinline__ void cta_min(double (&v)[K], CtaState &S, double *dst) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) S.wredd[warp][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double m = 1e300;
+    for (int w = 0; w < kWarps; w++) m = fmin(m, S.wredd[w][threadIdx.x]);
+    dst[threadIdx.x] = m;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------- sample geometry ---
+// Box-local cell and fraction of local sample i for the translation (iu, fu)
+// relative to the seed, plus the warp M d (d = offset from the stable
+// reference point) when `rot`.
+__device__ __forceinline__ void sample_pos(const int *s_ip, const float *s_fp, int i,
+                                           const CtaState &S, const int iu[3], const float fu[3],
+                                           bool rot, int c[3], float f[3]) {
+  const int packed = s_ip[i];
+  const int ip[3] = {packed & 1023, (packed >> 10) & 1023, (packed >> 20) & 1023};
+  float F[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) F[d] = s_fp[i * 3 + d] + fu[d];
+  if (rot) {
+    float dv[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) dv[d] = (float)(ip[d] - S.kint[d]) + (s_fp[i * 3 + d] - S.kfrac[d]);
+#pragma unroll
+    for (int r = 0; r < 3; r++) F[r] += S.M[r * 3 + 0] * dv[0] + S.M[r * 3 + 1] * dv[1] + S.M[r * 3 + 2] * dv[2];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const float fl = floorf(F[d]);
+    c[d] = ip[d] + iu[d] + (int)fl;
+    f[d] = F[d] - fl;
+  }
+}
+
+__device__ __forceinline__ float dvec(const int *s_ip, const float *s_fp, int i, const CtaState &S,
+                                      int d) {
+  const int ip = (s_ip[i] >> (10 * d)) & 1023;
+  return (float)(ip - S.kint[d]) + (s_fp[i * 3 + d] - S.kfrac[d]);
+}
+
+// keep gathers inside the interpolation box whatever the position (NaN
+// parameters, positions the range check already rejected)
+__device__ __forceinline__ void clamp_cell(int c[3], const int bext[3]) {
+#pragma unroll
+  for (int d = 0; d < 3; d++) c[d] = min(max(c[d], 0), bext[d] - 1);
+}
+
+// Stable sample position (FloatingCloud constructors, Core/FloatingCloud.cpp:40-128)
+__device__ __forceinline__ void stable_pos(const SearchArgs &a, const double pt[3], int i,
+                                           double p[3]) {
+  if (a.geom == DVC_SPHERE) {
+    for (int d = 0; d < 3; d++)
+      p[d] = __dadd_rn(pt[d], __dmul_rn(a.aspect[d], a.sphere_rel[(size_t)i * 3 + d]));
+  } else {
+    const int nn = a.cube_n;
+    const int idx[3] = {i % nn, (i / nn) % nn, i / (nn * nn)};
+    for (int d = 0; d < 3; d++) {
+      const double r = __dmul_rn(a.subv_rad, a.aspect[d]);
+      const double bmin = __dadd_rn(pt[d], -r);
+      const double bmax = __dadd_rn(pt[d], r);
+      const double inc = __ddiv_rn(__dsub_rn(bmax, bmin), (double)(nn - 1));
+      p[d] = __dadd_rn(bmin, __dmul_rn((double)idx[d], inc));
+    }
+  }
+}
+
+// Objective from one-pass sums: S1 = sum t', S2 = sum t'^2, S3 = sum t' q,
+// S4 = sum |t' - q|, t' = t - shift, q the per-sample reference quantity,
+// rs2 = sum q^2, n samples.
+__device__ __forceinline__ double objective_from_sums(int fcn, double S1, double S2, double S3,
+                                                      double S4, double rs2, int n) {
+  switch (fcn) {
+    case DVC_SAD: return S4;
+    case DVC_SSD: return S2 - 2.0 * S3 + rs2;
+    case DVC_ZSSD: {
+      const double m = S1 / n;
+      return (S2 - n * m * m) - 2.0 * S3 + rs2;
+    }
+    case DVC_NSSD: return 1.0 - S3 / sqrt(S2);
+    default: {
+      const double m = S1 / n;
+      const double sig = sqrt(S2 - n * m * m);
+      return 0.5 * (1.0 - S3 / sig);
+    }
+  }
+}
+
+// ---------------------------------------------------- seed and boxes ---
+// Search::starting_param (Core/Search.cpp:277-377) and the boxes of
+// search_pt_setup (Core/Search.cpp:248-275). Leader thread only.
+__device__ bool point_seed(const SearchArgs &a, PointHeader &H) {
+  const int n = H.n;
+  double sd[3];
+  if (a.seed_mode == DVC_SEED_GIVEN) {
+    for (int d = 0; d < 3; d++) sd[d] = a.seeds[(size_t)n * 3 + d];
+  } else {
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    int good = 0;
+    if (a.seed_mode == DVC_SEED_NEIGHBOURS) {
+      for (int j = 0; j < a.n_neigh; j++) {
+        const int m = a.neigh[(size_t)n * a.n_neigh + j];
+        if (m < 0 || m >= a.n_points) continue;
+        if (a.rank[m] >= H.rank) continue;  // not yet processed when the reference reaches n
+        long long polls = 0;
+        volatile int *flag = a.done + m;
+        while (*flag == 0) {
+          if (++polls > kWaitPolls) {
+            atomicExch(a.error_flag, DVC_E_TIMEOUT);
+            return false;
+          }
+          __nanosleep(128);
+        }
+        __threadfence();
+        const volatile int *st = a.status;
+        if (st[m] == DVC_POINT_GOOD) {
+          const volatile double *pm = a.params + (size_t)m * 12;
+          sx += pm[0];
+          sy += pm[1];
+          sz += pm[2];
+          good += 1;
+        }
+      }
+    }
+    if (good != 0) {
+      sd[0] = sx / good;
+      sd[1] = sy / good;
+      sd[2] = sz / good;
+    } else {
+      for (int d = 0; d < 3; d++) sd[d] = a.rigid[d];
+    }
+  }
+  for (int d = 0; d < 3; d++) H.seed[d] = sd[d];
+  // the nominal box centred on the point (reference volume) and on
+  // point + seed (correlate volume); act box one voxel inside
+  for (int d = 0; d < 3; d++) {
+    const double cref = H.pt[d];
+    const double ccor = __dadd_rn(H.pt[d], sd[d]);  // Point::move_by
+    const double ref_mn = __dadd_rn(a.nom_mn[d], __dsub_rn(cref, a.nom_cen[d]));
+    const double cor_mn = __dadd_rn(a.nom_mn[d], __dsub_rn(ccor, a.nom_cen[d]));
+    const double amn = __dadd_rn(a.nom_mn[d], 1.0), amx = __dadd_rn(a.nom_mx[d], -1.0);
+    const double acen = __ddiv_rn(__dadd_rn(amn, amx), 2.0);
+    const double dact = __dsub_rn(ccor, acen);
+    H.act_cor.mn[d] = __dadd_rn(amn, dact);
+    H.act_cor.mx[d] = __dadd_rn(amx, dact);
+    H.o_ref[d] = itrunc_d(ref_mn);
+    H.o_cor[d] = itrunc_d(cor_mn);
+  }
+  const int vol[3] = {a.nx, a.ny, a.nz};
+  H.chk_ref = 0;
+  H.chk_cor = 0;
+  for (int d = 0; d < 3; d++) {
+    if (H.o_ref[d] - 1 < 0 || H.o_ref[d] + a.bext[d] > vol[d] - 1) H.chk_ref = 1;
+    if (H.o_cor[d] - 1 < 0 || H.o_cor[d] + a.bext[d] > vol[d] - 1) H.chk_cor = 1;
+  }
+  return true;
+}
+
+// SearchParams::set_param_vect (Core/SearchParams.cpp:53-107) and the
+// derivatives used by the analytic Jacobian. One thread.
+__device__ void warp_matrices(const double *x, int ndof, CtaState &S) {
+  if (ndof <= 3) {
+    S.use_rot = 0;
+    return;
+  }
+  S.use_rot = 1;
+  const double phi = x[3], the = x[4], psi = x[5];
+  const double cf = cos(phi), sf = sin(phi), ct = cos(the), st = sin(the), cp = cos(psi), sp = sin(psi);
+  const double R[9] = {ct * cf, ct * sf, -st,
+                       sp * st * cf - cp * sf, sp * st * sf + cp * cf, ct * sp,
+                       cp * st * cf + sp * sf, cp * st * sf - sp * cf, ct * cp};
+  const double dR[3][9] = {
+      {-ct * sf, ct * cf, 0.0, -sp * st * sf - cp * cf, sp * st * cf - cp * sf, 0.0,
+       -cp * st * sf + sp * cf, cp * st * cf + sp * sf, 0.0},
+      {-st * cf, -st * sf, -ct, sp * ct * cf, sp * ct * sf, -st * sp, cp * ct * cf, cp * ct * sf,
+       -st * cp},
+      {0.0, 0.0, 0.0, cp * st * cf + sp * sf, cp * st * sf - sp * cf, ct * cp,
+       -sp * st * cf + cp * sf, -sp * st * sf - cp * cf, -ct * sp}};
+  double IS[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (ndof > 6) {
+    IS[0] += x[6]; IS[1] += x[9]; IS[2] += x[11];
+    IS[3] += x[9]; IS[4] += x[7]; IS[5] += x[10];
+    IS[6] += x[11]; IS[7] += x[10]; IS[8] += x[8];
+  }
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      double m = 0.0;
+      for (int k = 0; k < 3; k++) m += IS[r * 3 + k] * R[k * 3 + c];
+      S.M[r * 3 + c] = (float)(m - (r == c ? 1.0 : 0.0));
+      S.R[r * 3 + c] = (float)R[r * 3 + c];
+      for (int q = 0; q < 3; q++) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += IS[r * 3 + k] * dR[q][k * 3 + c];
+        S.N[q * 9 + r * 3 + c] = (float)s;
+      }
+    }
+}
+
+// Householder QR with column pivoting solving A x = b (n <= 12, FP64) on one
+// warp: the algorithm the reference reaches through
+// colPivHouseholderQr().solve (Core/Search.cpp:234). Unknowns beyond the
+// numerical rank are 0.
+__device__ void warp_qr_solve(CtaState &S, int n) {
+  const int lane = threadIdx.x & 31;
+  double *A = S.A;  // row-major n x n
+  if (lane < n) S.perm[lane] = lane;
+  __syncwarp();
+  for (int k = 0; k < n; k++) {
+    double s = -1.0;
+    if (lane >= k && lane < n) {
+      s = 0.0;
+      for (int i = k; i < n; i++) s += A[i * n + lane] * A[i * n + lane];
+    }
+    int pc = lane;
+    double best = s;
+    for (int o = 16; o; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, pc, o);
+      if (ob > best || (ob == best && oi < pc)) {
+        best = ob;
+        pc = oi;
+      }
+    }
+    if (pc != k) {
+      if (lane < n) {
+        const double t = A[lane * n + k];
+        A[lane * n + k] = A[lane * n + pc];
+        A[lane * n + pc] = t;
+      }
+      if (lane == 0) {
+        const int t = S.perm[k];
+        S.perm[k] = S.perm[pc];
+        S.perm[pc] = t;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double norm = 0.0;
+      for (int i = k; i < n; i++) norm += A[i * n + k] * A[i * n + k];
+      norm = sqrt(norm);
+      S.vv = 0.0;
+      if (norm != 0.0) {
+        const double alpha = A[k * n + k] > 0 ? -norm : norm;
+        double vv = 0.0;
+        for (int i = k; i < n; i++) {
+          S.v[i - k] = A[i * n + k] - (i == k ? alpha : 0.0);
+          vv += S.v[i - k] * S.v[i - k];
+        }
+        S.vv = vv;
+      }
+    }
+    __syncwarp();
+    const double vv = S.vv;
+    if (vv != 0.0 && lane >= k && lane <= n) {  // lane n applies the reflector to b
+      double s2 = 0.0;
+      for (int i = k; i < n; i++) s2 += S.v[i - k] * (lane < n ? A[i * n + lane] : S.b[i]);
+      s2 = 2.0 * s2 / vv;
+      for (int i = k; i < n; i++) {
+        if (lane < n) A[i * n + lane] -= s2 * S.v[i - k];
+        else S.b[i] -= s2 * S.v[i - k];
+      }
+    }
+    __syncwarp();
+    if (lane == 0) S.diag[k] = A[k * n + k];
+    __syncwarp();
+  }
+  if (lane == 0) {
+    int rank = 0;
+    const double thr = 2.220446049250313e-16 * (double)n * fabs(S.diag[0]);
+    for (int k = 0; k < n; k++) {
+      if (fabs(S.diag[k]) > thr) rank = k + 1;
+      else break;
+    }
+    double y[kMaxDof];
+    for (int k = 0; k < n; k++) y[k] = 0.0;
+    for (int k = rank - 1; k >= 0; k--) {
+      double s2 = S.b[k];
+      for (int j = k + 1; j < rank; j++) s2 -= A[k * n + j] * y[j];
+      y[k] = s2 / A[k * n + k];
+    }
+    for (int k = 0; k < n; k++) S.x[S.perm[k]] = y[k];
+  }
+  __syncwarp();
+}
+
+// Range check of the moving sample cloud against the correlate act box
+// (BoundBox::contains in tri_cub_Lek, Core/Interpolate.cpp:474-481).
+// Translation only: the exact FP64 bbox (stable bbox + u, affine_to). With a
+// rotation/strain: min/max of the warped samples over the cluster.
+__device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float *s_fp, int nl,
+                                            CtaState &S, bool rot) {
+  if (!rot) {
+    if (threadIdx.x == 0) {
+      int fail = 0;
+      for (int d = 0; d < 3; d++) {
+        const double bmn = __dadd_rn(S.sbmn[d], S.par[d]);
+        const double bmx = __dadd_rn(S.sbmx[d], S.par[d]);
+        if (!(bmn >= S.H.act_cor.mn[d]) || !(bmx <= S.H.act_cor.mx[d])) fail = 1;
+      }
+      S.fail = fail;
+    }
+    __syncthreads();
+    return;
+  }
+  double m[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};  // mins, then -maxs
+  for (int i = threadIdx.x; i < nl; i += kThreads) {
+    int c[3];
+    float f[3];
+    sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, true, c, f);
+    for (int d = 0; d < 3; d++) {
+      const double x = (double)c[d] + (double)f[d];
+      m[d] = fmin(m[d], x);
+      m[3 + d] = fmin(m[3 + d], -x);
+    }
+  }
+  cta_min<6>(m, S, S.cbuf[cl.parity]);
+  cluster_reduce(cl, S, 6, 6);
+  if (threadIdx.x == 0) {
+    int fail = 0;
+    for (int d = 0; d < 3; d++) {
+      const double bmn = (double)S.H.o_cor[d] + S.red[d];
+      const double bmx = (double)S.H.o_cor[d] - S.red[3 + d];
+      if (!(bmn >= S.H.act_cor.mn[d]) || !(bmx <= S.H.act_cor.mx[d])) fail = 1;
+    }
+    S.fail = fail;
+  }
+  __syncthreads();
+}
+
+// ================================================================ kernel ===
+template <typename VT, int IT>
+__global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ CtaState S;
+  Cl cl{cg::this_cluster(), 0u, 1u, 0};
+  cl.rank = cl.g.block_rank();
+  cl.size = cl.g.num_blocks();
+  const int tid = threadIdx.x;
+  const int nsub = a.n_sub;
+  const int lo = (int)((long long)nsub * cl.rank / cl.size);
+  const int nl = (int)((long long)nsub * (cl.rank + 1) / cl.size) - lo;
+
+  // per-CTA sample state: packed cell base, cell fraction (3), reference
+  // quantity, final values; and the Gauss-Newton chunk rows
+  const int cap = a.local_cap;
+  int *s_ip = reinterpret_cast<int *>(dsm);
+  float *s_fp = reinterpret_cast<float *>(s_ip + cap);
+  float *s_r = s_fp + 3 * cap;
+  float *s_t = s_r + cap;
+  float *s_G = s_t + cap;  // [kGRows][kThreads]
+
+  const VolView<VT> vbase{reinterpret_cast<const VT *>(a.ref), a.nx, a.ny, a.nz, 0, 0, 0,
+                          a.bext[0], a.bext[1], a.bext[2], false};
+  const int ndof = a.ndof;
+  const int fcn = a.objfcn;
+  const bool sad = (fcn == DVC_SAD);
+
+  for (;;) {
+    // --------------------------------------------- take work (leader) ---
+    if (cl.rank == 0 && tid == 0) {
+      PointHeader &H = S.H;
+      H.rank = atomicAdd(a.work_counter, 1);
+      H.flag = 0;
+      if (H.rank >= a.n_process) {
+        H.flag = 1;
+      } else {
+        H.n = a.order[H.rank];
+        for (int d = 0; d < 3; d++) H.pt[d] = a.pts[(size_t)H.n * 3 + d];
+        if (!point_seed(a, H)) H.flag = 2;
+      }
+    }
+    cl.g.sync();
+    if (cl.rank != 0) {
+      const int *src = reinterpret_cast<const int *>(cl.g.map_shared_rank(&S.H, 0));
+      int *dst = reinterpret_cast<int *>(&S.H);
+      for (int k = tid; k < (int)(sizeof(PointHeader) / 4); k += kThreads) dst[k] = src[k];
+    }
+    __syncthreads();
+    if (S.H.flag == 1) break;
+    if (S.H.flag == 2) {
+      if (cl.rank == 0 && tid == 0) {
+        a.status[S.H.n] = DVC_NOT_SEARCH;
+        __threadfence();
+        atomicExch(a.done + S.H.n, 1);
+      }
+      cl.g.sync();
+      continue;
+    }
+    VolView<VT> Vref = vbase, Vcor = vbase;
+    Vcor.vol = reinterpret_cast<const VT *>(a.cor);
+    Vref.ox = S.H.o_ref[0]; Vref.oy = S.H.o_ref[1]; Vref.oz = S.H.o_ref[2]; Vref.checked = S.H.chk_ref;
+    Vcor.ox = S.H.o_cor[0]; Vcor.oy = S.H.o_cor[1]; Vcor.oz = S.H.o_cor[2]; Vcor.checked = S.H.chk_cor;
+    unsigned long long n_eval = 0, n_undef = 0;
+    if (tid == 0) S.fail = 0;
+
+    // ------------------------------- reference subvolume and samples ---
+    // (search_pt_setup: the stable cloud interpolated in the reference box)
+    {
+      double m[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
+      KSum rk[1];
+      for (int i = tid; i < nl; i += kThreads) {
+        double p[3];
+        stable_pos(a, S.H.pt, lo + i, p);
+        int c[3], ip[3];
+        float f[3], fp[3];
+        for (int d = 0; d < 3; d++) {
+          m[d] = fmin(m[d], p[d]);
+          m[3 + d] = fmin(m[3 + d], -p[d]);
+          split_d(__dsub_rn(p[d], (double)S.H.o_ref[d]), c[d], f[d]);
+          split_d(__dsub_rn(__dadd_rn(p[d], S.H.seed[d]), (double)S.H.o_cor[d]), ip[d], fp[d]);
+          ip[d] = min(max(ip[d], 0), 1023);
+        }
+        clamp_cell(c, a.bext);
+        bool und;
+        float g[3];
+        const float r = interp_sample<VT, IT, false>(Vref, c, f, g, und);
+        n_undef += und;
+        s_r[i] = r;
+        s_ip[i] = ip[0] | (ip[1] << 10) | (ip[2] << 20);
+        s_fp[i * 3 + 0] = fp[0];
+        s_fp[i * 3 + 1] = fp[1];
+        s_fp[i * 3 + 2] = fp[2];
+        rk[0].add(r);
+      }
+      cta_min<6>(m, S, S.cbuf[cl.parity]);
+      cta_sum_comp<1>(rk, S, S.cbuf[cl.parity] + 6);
+      cluster_reduce(cl, S, 7, 6);
+    }
+    if (tid == 0) {
+      for (int d = 0; d < 3; d++) {
+        S.sbmn[d] = S.red[d];
+        S.sbmx[d] = -S.red[3 + d];
+        // stable reference point (FloatingCloud: centre, or middle of the cube box)
+        if (a.geom == DVC_SPHERE) {
+          S.sref[d] = S.H.pt[d];
+        } else {
+          const double r = __dmul_rn(a.subv_rad, a.aspect[d]);
+          S.sref[d] = __ddiv_rn(__dadd_rn(__dadd_rn(S.H.pt[d], r), __dadd_rn(S.H.pt[d], -r)), 2.0);
+        }
+        int ki;
+        float kf;
+        split_d(__dsub_rn(__dadd_rn(S.sref[d], S.H.seed[d]), (double)S.H.o_cor[d]), ki, kf);
+        S.kint[d] = ki;
+        S.kfrac[d] = kf;
+      }
+      S.scal[0] = S.red[6] / nsub;  // reference mean
+    }
+    __syncthreads();
+    const double rmean = S.scal[0];
+    {
+      KSum v[2];
+      const float m = (float)rmean;
+      for (int i = tid; i < nl; i += kThreads) {
+        const float dv = s_r[i] - m;
+        v[0].add(dv * dv);
+        v[1].add(s_r[i] * s_r[i]);
+      }
+      cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
+      cluster_reduce(cl, S, 2, 0);
+    }
+    const double rc2 = S.red[0], rraw2 = S.red[1];
+    // per-sample reference quantity q and the value shift:
+    //   SAD/SSD q = r - mean (shift = mean), ZSSD q = r - mean,
+    //   NSSD q = r / |r| (no shift), ZNSSD q = (r - mean) / |r - mean|
+    const float shift = (fcn == DVC_NSSD) ? 0.f : (float)rmean;
+    const float qs = (float)(fcn == DVC_NSSD ? 1.0 / sqrt(rraw2) : (fcn == DVC_ZNSSD ? 1.0 / sqrt(rc2) : 1.0));
+    for (int i = tid; i < nl; i += kThreads) s_r[i] = (s_r[i] - shift) * qs;
+    if (tid == 0) {
+      S.shift = shift;
+      S.rsum2 = (fcn == DVC_NSSD || fcn == DVC_ZNSSD) ? 1.0 : rc2;
+      for (int d = 0; d < 3; d++) S.par[d] = S.H.seed[d];
+      for (int d = 3; d < kMaxDof; d++) S.par[d] = 0.0;
+      S.best = -1;
+      S.best_obj = 1.7976931348623157e308;
+    }
+    n_eval += 1;
+    __syncthreads();
+
+    // ---------------------------------------------------- grid search ---
+    // trgrid_global (Core/Search.cpp:934-1043): (2k+1)^3 translations; the
+    // first strictly smaller objective in z, y, x loop order wins. Any
+    // translation whose sample box leaves the active box fails the point.
+    if (a.do_grid) {
+      const int k = a.num_inc;
+      const int side = 2 * k + 1;
+      const int total = side * side * side;
+      const double inc = a.inc;
+      for (int o0 = 0; o0 < total; o0 += kGridChunk) {
+        const int nch = min(kGridChunk, total - o0);
+        int bad = 0;
+        if (tid < nch) {
+          const int o = o0 + tid;
+          const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
+          for (int d = 0; d < 3; d++) {
+            const double pc = __dadd_rn(S.par[d], __dmul_rn((double)off[d], inc));
+            if (!(__dadd_rn(S.sbmn[d], pc) >= S.H.act_cor.mn[d]) ||
+                !(__dadd_rn(S.sbmx[d], pc) <= S.H.act_cor.mx[d]))
+              bad = 1;
+            split_d(__dsub_rn(pc, S.H.seed[d]), S.giu[tid][d], S.gfu[tid][d]);
+          }
+        }
+        if (__syncthreads_or(bad)) {
+          if (tid == 0) S.fail = 1;
+          __syncthreads();
+          break;
+        }
+        const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll 1
+        for (int j = 0; j < nch; j++) {
+          const int iu[3] = {S.giu[j][0], S.giu[j][1], S.giu[j][2]};
+          const float fu[3] = {S.gfu[j][0], S.gfu[j][1], S.gfu[j][2]};
+          float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+          for (int i = tid; i < nl; i += kThreads) {
+            int c[3];
+            float f[3], g[3];
+            sample_pos(s_ip, s_fp, i, S, iu, fu, false, c, f);
+            clamp_cell(c, a.bext);
+            bool und;
+            const float t = interp_sample<VT, IT, false>(Vcor, c, f, g, und) - S.shift;
+            n_undef += und;
+            const float q = s_r[i];
+            if (sad) {
+              p0 += fabsf(t - q);
+            } else {
+              p0 += t;
+              p1 += t * t;
+              p2 += t * q;
+            }
+          }
+#pragma unroll
+          for (int o = 16; o; o >>= 1) {
+            p0 += __shfl_xor_sync(0xffffffffu, p0, o);
+            p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+          }
+          if (lane == 0) {
+            S.wpart[warp][3 * j + 0] = p0;
+            S.wpart[warp][3 * j + 1] = p1;
+            S.wpart[warp][3 * j + 2] = p2;
+          }
+        }
+        __syncthreads();
+        for (int q = tid; q < 3 * nch; q += kThreads) {
+          double s = 0.0;
+          for (int w = 0; w < kWarps; w++) s += (double)S.wpart[w][q];
+          S.cbuf[cl.parity][q] = s;
+        }
+        cluster_reduce(cl, S, 3 * nch, 0);
+        if (tid < nch)
+          S.objv[tid] = sad ? S.red[3 * tid]
+                            : objective_from_sums(fcn, S.red[3 * tid], S.red[3 * tid + 1],
+                                                  S.red[3 * tid + 2], 0.0, S.rsum2, nsub);
+        __syncthreads();
+        if (tid == 0)
+          for (int j = 0; j < nch; j++)
+            if (S.objv[j] < S.best_obj) {  // first strictly smaller value wins
+              S.best_obj = S.objv[j];
+              S.best = o0 + j;
+            }
+        __syncthreads();
+        n_eval += nch;
+      }
+      if (S.fail) goto point_done;
+      if (tid == 0 && S.best >= 0) {
+        const int o = S.best;
+        const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
+        for (int d = 0; d < 3; d++) S.par[d] += (double)off[d] * inc;
+      }
+      __syncthreads();
+    }
+
+    // ------------------------------------------------- Gauss-Newton ---
+    // min_Lev_Mar(start, 1e-6, 0.01) (Core/Search.cpp:194-246): undamped
+    // Gauss-Newton on the residual vector of the objective, at most 20
+    // iterations, stop when |obj - obj_old| < 1e-6 or |du| < 0.01. The
+    // reference differentiates the residuals by forward differences
+    // (h = 1e-10, LM_prep_at); here J is the analytic gradient of the
+    // interpolant chained through the warp and the objective's normalisation:
+    //   g_i = dt_i/dp (per sample), G = [g_i], t' = t - shift, q_i reference
+    //   SSD/SAD: e = t - r,            J = G
+    //   ZSSD:    e = t - tbar - q,     J = (I - 11'/n) G
+    //   NSSD:    e = t/T - q,          J = (I - tt'/T^2) G / T
+    //   ZNSSD:   e = (t-tbar)/sig - q, J = (I - 11'/n - that that') G / sig
+    // so J'J and J'e follow from G'G, G'1, G't' and G'q: chunks of kThreads
+    // samples pass through shared memory, one thread per matrix entry.
+    {
+      int it_done = 20;
+      const int ntri = ndof * (ndof + 1) / 2;
+      const int nent = ntri + 3 * ndof;
+      const int nparts = kThreads / nent;
+      const int my_e = tid % nent, my_part = tid / nent;
+      int ea = 0, eb = 0;
+      if (my_e < ntri) {
+        int e = my_e, r = 0;
+        while (e >= ndof - r) {
+          e -= ndof - r;
+          r++;
+        }
+        ea = r;
+        eb = r + e;
+      } else {
+        ea = (my_e - ntri) % ndof;
+        eb = kMaxDof + (my_e - ntri) / ndof;
+      }
+      for (int it = 0; it < 20; it++) {
+        if (tid == 0) {
+          warp_matrices(S.par, ndof, S);
+          for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), S.iu[d], S.fu[d]);
+        }
+        __syncthreads();
+        const bool rot = S.use_rot;
+        range_check(cl, s_ip, s_fp, nl, S, rot);
+        if (S.fail) goto point_done;
+
+        KSum v[4];
+        float gg = 0.f;
+        for (int base = 0; base < nl; base += kThreads) {
+          const int i = base + tid;
+          float g[kMaxDof];
+#pragma unroll
+          for (int p = 0; p < kMaxDof; p++) g[p] = 0.f;
+          float t = 0.f, q = 0.f, one = 0.f;
+          if (i < nl) {
+            int c[3];
+            float f[3], gv[3];
+            sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
+            clamp_cell(c, a.bext);
+            bool und;
+            t = interp_sample<VT, IT, true>(Vcor, c, f, gv, und) - S.shift;
+            n_undef += und;
+            q = s_r[i];
+            one = 1.f;
+            v[0].add(t);
+            v[1].add(t * t);
+            v[2].add(t * q);
+            v[3].add(fabsf(t - q));
+            g[0] = gv[0];
+            g[1] = gv[1];
+            g[2] = gv[2];
+            if (ndof > 3) {
+              float dv[3];
+              for (int d = 0; d < 3; d++) dv[d] = dvec(s_ip, s_fp, i, S, d);
+#pragma unroll
+              for (int an = 0; an < 3; an++) {
+                float acc = 0.f;
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+                  acc += gv[r] * (S.N[an * 9 + r * 3 + 0] * dv[0] + S.N[an * 9 + r * 3 + 1] * dv[1] +
+                                  S.N[an * 9 + r * 3 + 2] * dv[2]);
+                g[3 + an] = acc;
+              }
+              if (ndof > 6) {
+                float Rd[3];
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+                  Rd[r] = S.R[r * 3 + 0] * dv[0] + S.R[r * 3 + 1] * dv[1] + S.R[r * 3 + 2] * dv[2];
+                g[6] = gv[0] * Rd[0];
+                g[7] = gv[1] * Rd[1];
+                g[8] = gv[2] * Rd[2];
+                g[9] = gv[0] * Rd[1] + gv[1] * Rd[0];
+                g[10] = gv[1] * Rd[2] + gv[2] * Rd[1];
+                g[11] = gv[0] * Rd[2] + gv[2] * Rd[0];
+              }
+            }
+          }
+#pragma unroll
+          for (int p = 0; p < kMaxDof; p++) s_G[p * kThreads + tid] = g[p];
+          s_G[(kMaxDof + 0) * kThreads + tid] = one;
+          s_G[(kMaxDof + 1) * kThreads + tid] = t;
+          s_G[(kMaxDof + 2) * kThreads + tid] = q;
+          __syncthreads();
+          if (my_part < nparts) {
+            const int l0 = (my_part * kThreads) / nparts, l1 = ((my_part + 1) * kThreads) / nparts;
+            const float *ga = s_G + ea * kThreads, *gb = s_G + eb * kThreads;
+            for (int s2 = l0; s2 < l1; s2++) gg += ga[s2] * gb[s2];
+          }
+          __syncthreads();
+        }
+        n_eval += 1;
+        cta_sum_comp<4>(v, S, S.cbuf[cl.parity]);
+        // entry parts -> entries (FP64) after the 4 value sums
+        {
+          double *parts = S.red;  // scratch: parts of each entry
+          parts[tid] = (my_part < nparts) ? (double)gg : 0.0;
+          __syncthreads();
+          if (tid < nent) {
+            double s = 0.0;
+            for (int pp = 0; pp < nparts; pp++) s += parts[pp * nent + tid];
+            S.cbuf[cl.parity][4 + tid] = s;
+          }
+        }
+        cluster_reduce(cl, S, 4 + nent, 0);
+        // assemble J'J and -J'e (FP64)
+        if (tid == 0) {
+          const double S1 = S.red[0], S2 = S.red[1], S3 = S.red[2], S4 = S.red[3];
+          const double n = nsub, mean = S1 / n;
+          double obj, sc = 1.0, rho = 0.0, T = 0.0, sig = 0.0;
+          switch (fcn) {
+            case DVC_SAD:
+            case DVC_SSD:
+            case DVC_ZSSD: obj = objective_from_sums(fcn, S1, S2, S3, S4, S.rsum2, nsub); break;
+            case DVC_NSSD:
+              T = sqrt(S2);
+              obj = 1.0 - S3 / T;
+              sc = 1.0 / (T * T);
+              break;
+            default:
+              sig = sqrt(S2 - n * mean * mean);
+              rho = S3 / sig;
+              obj = 0.5 * (1.0 - rho);
+              sc = 1.0 / (sig * sig);
+              break;
+          }
+          S.scal[0] = mean;
+          S.scal[1] = sc;
+          S.scal[2] = (fcn == DVC_NSSD) ? T : sig;
+          S.scal[3] = (fcn == DVC_NSSD) ? S3 / T : rho;
+          S.obj = obj;
+          int stop = 0;
+          if (it > 0) {
+            const double del_obj = fabs(obj - S.obj_old);
+            const double del_mag = sqrt(S.upd[0] * S.upd[0] + S.upd[1] * S.upd[1] + S.upd[2] * S.upd[2]);
+            if ((del_obj < 0.000001) || (del_mag < 0.01)) stop = 1;
+          }
+          S.stop = stop;
+        }
+        __syncthreads();
+        if (S.stop) {
+          it_done = it;
+          break;
+        }
+        {
+          const double *GG = &S.red[4];
+          const double *Gs = GG + ntri, *Gt = GG + ntri + ndof, *Gq = GG + ntri + 2 * ndof;
+          const double mean = S.scal[0], sc = S.scal[1], den = S.scal[2], rr = S.scal[3];
+          const bool sub_mean = (fcn == DVC_ZSSD || fcn == DVC_ZNSSD);
+          const bool sub_t = (fcn == DVC_NSSD || fcn == DVC_ZNSSD);
+          if (tid < ndof) {
+            const int p = tid;
+            double ut = 0.0, jte;
+            if (fcn == DVC_SAD || fcn == DVC_SSD) {
+              jte = Gt[p] - Gq[p];
+            } else if (fcn == DVC_ZSSD) {
+              jte = Gt[p] - mean * Gs[p] - Gq[p];
+            } else if (fcn == DVC_NSSD) {
+              ut = Gt[p] / den;
+              jte = (rr * ut - Gq[p]) / den;
+            } else {
+              ut = (Gt[p] - mean * Gs[p]) / den;
+              jte = (rr * ut - Gq[p]) / den;
+            }
+            S.ut[p] = ut;
+            S.b[p] = -jte;
+          }
+          __syncthreads();
+          if (tid < ntri) {
+            int e = tid, r = 0;
+            while (e >= ndof - r) {
+              e -= ndof - r;
+              r++;
+            }
+            const int c2 = r + e;
+            double v2 = GG[tid];
+            if (sub_mean) v2 -= Gs[r] * Gs[c2] / (double)nsub;
+            if (sub_t) v2 -= S.ut[r] * S.ut[c2];
+            v2 *= sc;
+            S.A[r * ndof + c2] = v2;
+            S.A[c2 * ndof + r] = v2;
+          }
+          __syncthreads();
+        }
+        if (tid < 32) {
+          warp_qr_solve(S, ndof);
+          if (tid == 0) {
+            for (int p = 0; p < ndof; p++) S.par[p] += S.x[p];
+            for (int d = 0; d < 3; d++) S.upd[d] = S.x[d];
+            S.obj_old = S.obj;
+          }
+        }
+        __syncthreads();
+      }
+      if (cl.rank == 0 && tid == 0) {
+        if (a.gn_iters) a.gn_iters[S.H.n] = it_done;
+        atomicAdd(a.counters + 1, (unsigned long long)it_done);
+      }
+    }
+
+    // ------------------------------------------------ final objective ---
+    // obj_val_at(par_min) (Core/Search.cpp:187): explicit residuals over the
+    // stored values, the reference's own two-pass formulation
+    {
+      if (tid == 0) {
+        warp_matrices(S.par, ndof, S);
+        for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), S.iu[d], S.fu[d]);
+      }
+      __syncthreads();
+      const bool rot = S.use_rot;
+      range_check(cl, s_ip, s_fp, nl, S, rot);
+      n_eval += 1;
+      if (S.fail) goto point_done;
+      {
+        KSum v[1];
+        for (int i = tid; i < nl; i += kThreads) {
+          int c[3];
+          float f[3], g[3];
+          sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
+          clamp_cell(c, a.bext);
+          bool und;
+          const float t = interp_sample<VT, IT, false>(Vcor, c, f, g, und) - S.shift;
+          n_undef += und;
+          s_t[i] = t;
+          v[0].add(t);
+        }
+        cta_sum_comp<1>(v, S, S.cbuf[cl.parity]);
+        cluster_reduce(cl, S, 1, 0);
+      }
+      const float tm = (float)(S.red[0] / nsub);
+      {
+        KSum v[2];
+        for (int i = tid; i < nl; i += kThreads) {
+          const float t = s_t[i];
+          v[0].add((t - tm) * (t - tm));
+          v[1].add(t * t);
+        }
+        cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
+        cluster_reduce(cl, S, 2, 0);
+      }
+      const float inv_sig = (float)(1.0 / sqrt(S.red[0]));
+      const float inv_T = (float)(1.0 / sqrt(S.red[1]));
+      {
+        KSum v[2];
+        for (int i = tid; i < nl; i += kThreads) {
+          const float t = s_t[i], q = s_r[i];
+          float e;
+          switch (fcn) {
+            case DVC_SAD:
+            case DVC_SSD: e = t - q; break;
+            case DVC_ZSSD: e = (t - tm) - q; break;
+            case DVC_NSSD: e = t * inv_T - q; break;
+            default: e = (t - tm) * inv_sig - q; break;
+          }
+          v[0].add(e * e);
+          v[1].add(fabsf(e));
+        }
+        cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
+        cluster_reduce(cl, S, 2, 0);
+      }
+      if (tid == 0) {
+        double obj = S.red[0];
+        if (fcn == DVC_SAD) obj = S.red[1];
+        if (fcn == DVC_NSSD) obj /= 2.0;
+        if (fcn == DVC_ZNSSD) obj /= 4.0;
+        S.obj = obj;
+      }
+      __syncthreads();
+    }
+
+  point_done:
+    if (cl.rank == 0 && tid == 0) {
+      const int n = S.H.n;
+      if (S.fail) {
+        a.status[n] = DVC_RANGE_FAIL;
+        a.objmin[n] = 0.0;
+        for (int p = 0; p < 12; p++) a.params[(size_t)n * 12 + p] = 0.0;
+      } else {
+        a.status[n] = DVC_POINT_GOOD;
+        a.objmin[n] = S.obj;
+        for (int p = 0; p < 12; p++) a.params[(size_t)n * 12 + p] = p < ndof ? S.par[p] : 0.0;
+      }
+      __threadfence();
+      atomicExch(a.done + n, 1);
+      atomicAdd(a.counters + 0, n_eval);
+    }
+    {
+      unsigned long long u = n_undef;
+      for (int o = 16; o; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+      if ((tid & 31) == 0 && u) atomicAdd(a.counters + 2, u);
+    }
+    // the leader may overwrite its header only after every CTA copied it
+    cl.g.sync();
+  }
+  // no CTA leaves while another may still read its shared memory
+  cl.g.sync();
+}
+
+}  // namespace dvc

@@ -122,24 +122,99 @@ __device__ __forceinline__ float load_voxel_checked(const VT *__restrict__ vol, 
   return (float)__ldg(vol + ((long long)z * ny + y) * nx + x);
 }
 
-// Volume + interpolation-box description used by the sample evaluators.
+// Voxel sources. A source returns rows of four consecutive voxels along x
+// (and single voxels) at global voxel coordinates.
+//   GSrc: the volume in global memory (read-only path), optionally with
+//         bounds checks (boxes reaching the volume edge read 0 outside);
+//   SSrc: a box-shaped region of the volume staged in shared memory by TMA.
 template <typename VT>
-struct VolView {
+struct GSrc {
   const VT *vol;
-  int nx, ny, nz;      // volume extents
-  int ox, oy, oz;      // global voxel index of box voxel (0,0,0)
-  int bx, by, bz;      // box extents (voxels)
-  bool checked;        // box (+1 voxel margin) not inside the volume: bounds-check loads
+  int nx, ny, nz;
+  bool checked;
+  __device__ __forceinline__ void row4(int x, int y, int z, float v[4]) const {
+    if (!checked) {
+      load_row4(vol, ((long long)z * ny + y) * nx + x, v);
+    } else {
+#pragma unroll
+      for (int a = 0; a < 4; a++) v[a] = load_voxel_checked(vol, x + a, y, z, nx, ny, nz);
+    }
+  }
+  __device__ __forceinline__ float voxel(int x, int y, int z) const {
+    if (checked) return load_voxel_checked(vol, x, y, z, nx, ny, nz);
+    return (float)__ldg(vol + ((long long)z * ny + y) * nx + x);
+  }
+};
+
+__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ uint2 lds64(uint32_t addr) {
+  uint2 v;
+  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(addr));
+  return v;
+}
+
+template <typename VT>
+struct SSrc {
+  uint32_t base;       // shared-memory address of the staged box
+  int r0x, r0y, r0z;   // global voxel coordinates of the box's first element
+  int bx, by;          // box pitch (elements per row, rows per slice)
+  __device__ __forceinline__ uint32_t elem(int x, int y, int z) const {
+    return (uint32_t)(((z - r0z) * by + (y - r0y)) * bx + (x - r0x));
+  }
+  __device__ __forceinline__ void row4(int x, int y, int z, float v[4]) const {
+    const uint32_t e = elem(x, y, z);
+    if (sizeof(VT) == 1) {
+      const uint32_t a = base + e;
+      const uint32_t w0 = lds32(a & ~3u), w1 = lds32((a & ~3u) + 4);
+      const uint32_t sh = a & 3u;
+      const uint32_t w = __byte_perm(w0, w1, sh | ((sh + 1) << 4) | ((sh + 2) << 8) | ((sh + 3) << 12));
+      v[0] = u8f(__byte_perm(w, 0, 0x4440));
+      v[1] = u8f(__byte_perm(w, 0, 0x4441));
+      v[2] = u8f(__byte_perm(w, 0, 0x4442));
+      v[3] = u8f(__byte_perm(w, 0, 0x4443));
+    } else {
+      const uint32_t a = base + 2 * e;
+      const uint2 q01 = lds64(a & ~7u), q23 = lds64((a & ~7u) + 8);
+      const uint32_t s = a & 7u;
+      const bool hi = s >= 4;
+      const uint32_t lo = hi ? q01.y : q01.x, mid = hi ? q23.x : q01.y, top = hi ? q23.y : q23.x;
+      const uint32_t sh = (s & 3u) * 8;
+      const uint32_t r0 = __funnelshift_r(lo, mid, sh), r1 = __funnelshift_r(mid, top, sh);
+      v[0] = __int_as_float(0x4B000000u | (r0 & 0xFFFFu)) - 8388608.0f;
+      v[1] = __int_as_float(0x4B000000u | (r0 >> 16)) - 8388608.0f;
+      v[2] = __int_as_float(0x4B000000u | (r1 & 0xFFFFu)) - 8388608.0f;
+      v[3] = __int_as_float(0x4B000000u | (r1 >> 16)) - 8388608.0f;
+    }
+  }
+  __device__ __forceinline__ float voxel(int x, int y, int z) const {
+    const uint32_t e = elem(x, y, z);
+    if (sizeof(VT) == 1) {
+      const uint32_t a = base + e;
+      return u8f(__byte_perm(lds32(a & ~3u), 0, 0x4440 | (a & 3u)));
+    }
+    const uint32_t a = base + 2 * e;
+    const uint32_t w = lds32(a & ~3u);
+    return __int_as_float(0x4B000000u | ((a & 2u) ? (w >> 16) : (w & 0xFFFFu))) - 8388608.0f;
+  }
+};
+
+// Interpolation box of the current point: global voxel origin and extents.
+struct BoxGeom {
+  int ox, oy, oz;  // global voxel index of box voxel (0,0,0)
+  int bx, by, bz;  // box extents (voxels)
 };
 
 // Separable contraction of the 4x4x4 stencil whose low corner is at global
 // voxel (x0, y0, z0), with value weights w* and (when GRAD) slope weights d*.
-// CHECKED: bounds-checked voxel loads (boxes that reach the volume edge).
-template <typename VT, bool GRAD, bool CHECKED>
-__device__ __forceinline__ float contract_impl(const VolView<VT> &V, int x0, int y0, int z0,
-                                               const float wx[4], const float wy[4],
-                                               const float wz[4], const float dx[4],
-                                               const float dy[4], const float dz[4], float g[3]) {
+template <typename Src, bool GRAD>
+__device__ __forceinline__ float contract(const Src &src, int x0, int y0, int z0,
+                                          const float wx[4], const float wy[4], const float wz[4],
+                                          const float dx[4], const float dy[4], const float dz[4],
+                                          float g[3]) {
   float val = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
   for (int c = 0; c < 4; c++) {
@@ -147,13 +222,7 @@ __device__ __forceinline__ float contract_impl(const VolView<VT> &V, int x0, int
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       float v[4];
-      if (!CHECKED) {
-        load_row4(V.vol, ((long long)(z0 + c) * V.ny + (y0 + b)) * V.nx + x0, v);
-      } else {
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-          v[a] = load_voxel_checked(V.vol, x0 + a, y0 + b, z0 + c, V.nx, V.ny, V.nz);
-      }
+      src.row4(x0, y0 + b, z0 + c, v);
       const float r = wx[0] * v[0] + wx[1] * v[1] + wx[2] * v[2] + wx[3] * v[3];
       s += wy[b] * r;
       if (GRAD) {
@@ -177,28 +246,13 @@ __device__ __forceinline__ float contract_impl(const VolView<VT> &V, int x0, int
   return val;
 }
 
-template <typename VT, bool GRAD>
-__device__ __noinline__ float contract_checked(const VolView<VT> &V, int x0, int y0, int z0,
-                                               const float *wx, const float *wy, const float *wz,
-                                               const float *dx, const float *dy, const float *dz,
-                                               float *g) {
-  return contract_impl<VT, GRAD, true>(V, x0, y0, z0, wx, wy, wz, dx, dy, dz, g);
-}
-
-template <typename VT, bool GRAD>
-__device__ __forceinline__ float contract(const VolView<VT> &V, int x0, int y0, int z0,
-                                          const float wx[4], const float wy[4], const float wz[4],
-                                          const float dx[4], const float dy[4], const float dz[4],
-                                          float g[3]) {
-  if (V.checked) return contract_checked<VT, GRAD>(V, x0, y0, z0, wx, wy, wz, dx, dy, dz, g);
-  return contract_impl<VT, GRAD, false>(V, x0, y0, z0, wx, wy, wz, dx, dy, dz, g);
-}
-
 // Face cells (rare): A A A - B B B + C C C, out of line to keep the hot
 // interior path small.
-template <typename VT, bool GRAD>
-__device__ __noinline__ float interp_face(const VolView<VT> &V, int x0, int y0, int z0,
-                                          const int kind[3], const float f[3], float g[3]) {
+template <typename Src, bool GRAD>
+__device__ __noinline__ float interp_face(const Src src, int x0, int y0, int z0, int k0, int k1,
+                                          int k2, float f0, float f1, float f2, float *gout) {
+  const int kind[3] = {k0, k1, k2};
+  const float f[3] = {f0, f1, f2};
   float A[3][4], dA[3][4], B[3][4], dB[3][4], Cc[3][4], dC[3][4];
   for (int d = 0; d < 3; d++) {
     if (kind[d] == 0) {
@@ -216,69 +270,83 @@ __device__ __noinline__ float interp_face(const VolView<VT> &V, int x0, int y0, 
     }
   }
   float g1[3], g2[3], g3[3];
-  float v = contract<VT, GRAD>(V, x0, y0, z0, A[0], A[1], A[2], dA[0], dA[1], dA[2], g1);
-  v -= contract<VT, GRAD>(V, x0, y0, z0, B[0], B[1], B[2], dB[0], dB[1], dB[2], g2);
-  v += contract<VT, GRAD>(V, x0, y0, z0, Cc[0], Cc[1], Cc[2], dC[0], dC[1], dC[2], g3);
+  float v = contract<Src, GRAD>(src, x0, y0, z0, A[0], A[1], A[2], dA[0], dA[1], dA[2], g1);
+  v -= contract<Src, GRAD>(src, x0, y0, z0, B[0], B[1], B[2], dB[0], dB[1], dB[2], g2);
+  v += contract<Src, GRAD>(src, x0, y0, z0, Cc[0], Cc[1], Cc[2], dC[0], dC[1], dC[2], g3);
   if (GRAD)
-    for (int d = 0; d < 3; d++) g[d] = g1[d] - g2[d] + g3[d];
+    for (int d = 0; d < 3; d++) gout[d] = g1[d] - g2[d] + g3[d];
   return v;
 }
 
-// Interpolation of one sample at box-local cell (c[3]) and fraction (f[3]).
-// ITYPE: 0 nearest, 1 trilinear, 2 tricubic. Returns the value; with GRAD
-// also the spatial gradient. `undef` is set when the sample lies in the last
-// plane of the box (reference-undefined cell, see the file header).
-template <typename VT, int ITYPE, bool GRAD>
-__device__ __forceinline__ float interp_sample(const VolView<VT> &V, int c[3], float f[3],
-                                               float g[3], bool &undef) {
-  const int n[3] = {V.bx, V.by, V.bz};
-  undef = false;
-  if (ITYPE == 0) {
-    // Interpolate::nearest: the voxel at the truncated position
+// Cell adjustment shared by all sources: the reference-undefined last plane
+// (c = n-1) is evaluated as cell n-2 continued past its end. Returns the
+// stencil's low corner (global) and the per-axis face kinds.
+template <int ITYPE>
+__device__ __forceinline__ bool prep_cell(const BoxGeom &G, int c[3], float f[3], int lo[3],
+                                          int kind[3]) {
+  const int n[3] = {G.bx, G.by, G.bz};
+  const int o[3] = {G.ox, G.oy, G.oz};
+  bool undef = false;
+  bool face = false;
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+  for (int d = 0; d < 3; d++) {
+    if (ITYPE == 0) {
       if (c[d] > n[d] - 1) {
         undef = true;
         c[d] = n[d] - 1;
       }
-    if (GRAD) g[0] = g[1] = g[2] = 0.f;
-    const int x = V.ox + c[0], y = V.oy + c[1], z = V.oz + c[2];
-    if (V.checked) return load_voxel_checked(V.vol, x, y, z, V.nx, V.ny, V.nz);
-    return (float)__ldg(V.vol + ((long long)z * V.ny + y) * V.nx + x);
-  }
-#pragma unroll
-  for (int d = 0; d < 3; d++)
-    if (c[d] > n[d] - 2) {
-      undef = true;
-      f[d] += (float)(c[d] - (n[d] - 2));
-      c[d] = n[d] - 2;
+      lo[d] = o[d] + c[d];
+      kind[d] = 0;
+    } else {
+      if (c[d] > n[d] - 2) {
+        undef = true;
+        f[d] += (float)(c[d] - (n[d] - 2));
+        c[d] = n[d] - 2;
+      }
+      lo[d] = o[d] + c[d] - 1;
+      kind[d] = ITYPE == 2 ? ((c[d] == n[d] - 2) ? 1 : (c[d] <= 0 ? 2 : 0)) : 0;
+      face |= kind[d] != 0;
     }
-  const int x0 = V.ox + c[0] - 1, y0 = V.oy + c[1] - 1, z0 = V.oz + c[2] - 1;
+  }
+  (void)face;
+  return undef;
+}
+
+// Interpolation of one sample at box-local cell c and fraction f from source
+// `src`; the stencil's global low corner `lo` and face kinds come from
+// prep_cell. ITYPE: 0 nearest, 1 trilinear, 2 tricubic.
+template <typename Src, int ITYPE, bool GRAD>
+__device__ __forceinline__ float interp_at(const Src &src, const int lo[3], const int kind[3],
+                                           const float f[3], float g[3]) {
+  if (ITYPE == 0) {
+    if (GRAD) g[0] = g[1] = g[2] = 0.f;
+    return src.voxel(lo[0], lo[1], lo[2]);
+  }
+  float w[3][4], dw[3][4];
   if (ITYPE == 1) {
-    // Interpolate::tri_lin: raw corner values only
-    float w[3][4], dw[3][4];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       w[d][0] = 0.f; w[d][1] = 1.f - f[d]; w[d][2] = f[d]; w[d][3] = 0.f;
       dw[d][0] = 0.f; dw[d][1] = -1.f; dw[d][2] = 1.f; dw[d][3] = 0.f;
     }
-    return contract<VT, GRAD>(V, x0, y0, z0, w[0], w[1], w[2], dw[0], dw[1], dw[2], g);
+    return contract<Src, GRAD>(src, lo[0], lo[1], lo[2], w[0], w[1], w[2], dw[0], dw[1], dw[2], g);
   }
-  // tricubic
-  int kind[3];
-  bool face = false;
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    kind[d] = (c[d] == n[d] - 2) ? 1 : (c[d] <= 0 ? 2 : 0);
-    face |= kind[d] != 0;
-  }
-  if (!face) {
-    float w[3][4], dw[3][4];
+  if ((kind[0] | kind[1] | kind[2]) == 0) {
 #pragma unroll
     for (int d = 0; d < 3; d++) cr_weights(f[d], w[d], dw[d]);
-    return contract<VT, GRAD>(V, x0, y0, z0, w[0], w[1], w[2], dw[0], dw[1], dw[2], g);
+    return contract<Src, GRAD>(src, lo[0], lo[1], lo[2], w[0], w[1], w[2], dw[0], dw[1], dw[2], g);
   }
-  return interp_face<VT, GRAD>(V, x0, y0, z0, kind, f, g);
+  return interp_face<Src, GRAD>(src, lo[0], lo[1], lo[2], kind[0], kind[1], kind[2], f[0], f[1],
+                                f[2], g);
+}
+
+// Global-memory interpolation in the point's box (cell clamping included).
+template <typename VT, int ITYPE, bool GRAD>
+__device__ __forceinline__ float interp_global(const GSrc<VT> &src, const BoxGeom &G, int c[3],
+                                               float f[3], float g[3], bool &undef) {
+  int lo[3], kind[3];
+  undef = prep_cell<ITYPE>(G, c, f, lo, kind);
+  return interp_at<GSrc<VT>, ITYPE, GRAD>(src, lo, kind, f, g);
 }
 
 // ------------------------------------------------------------ reductions ---

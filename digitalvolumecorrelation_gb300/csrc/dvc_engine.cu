@@ -22,6 +22,7 @@
 //   set_param_vect           SearchParams.cpp:53-107 -> warp_matrices
 //   tri_cub_Lek etc.         Interpolate.cpp:404-567 -> interp_sample (dvc_device.cuh)
 //   obj_*                    ObjectiveFunctions.cpp:24-263 -> objective sums
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -80,22 +81,22 @@ __global__ void rank_kernel(int n_process, const int *order, int *rank, int n_po
 
 // ------------------------------------------------- interpolation entry ---
 template <typename VT>
-__global__ void interp_points_kernel(VolView<VT> V, int n, const double *pts, int itype,
+__global__ void interp_points_kernel(GSrc<VT> V, BoxGeom G, int n, const double *pts, int itype,
                                      double *out, unsigned long long *undef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int c[3];
   float f[3];
-  const int o[3] = {V.ox, V.oy, V.oz};
-  const int bext[3] = {V.bx, V.by, V.bz};
+  const int o[3] = {G.ox, G.oy, G.oz};
+  const int bext[3] = {G.bx, G.by, G.bz};
   for (int d = 0; d < 3; d++) split_d(__dsub_rn(pts[(size_t)i * 3 + d], (double)o[d]), c[d], f[d]);
   clamp_cell(c, bext);
   bool und;
   float g[3];
   float v;
-  if (itype == 2) v = interp_sample<VT, 2, false>(V, c, f, g, und);
-  else if (itype == 1) v = interp_sample<VT, 1, false>(V, c, f, g, und);
-  else v = interp_sample<VT, 0, false>(V, c, f, g, und);
+  if (itype == 2) v = interp_global<VT, 2, false>(V, G, c, f, g, und);
+  else if (itype == 1) v = interp_global<VT, 1, false>(V, G, c, f, g, und);
+  else v = interp_global<VT, 0, false>(V, G, c, f, g, und);
   out[i] = (double)v;
   if (und) atomicAdd(undef, 1ULL);
 }
@@ -175,13 +176,16 @@ struct dvc_engine {
   double nom_mn[3], nom_mx[3], nom_cen[3];
   int bext[3];
   double *d_sphere = nullptr;
+  double morton_rad = 0.0;
+  int *d_cube_order = nullptr;
+  std::vector<double> h_offsets;  // stable sample offsets from the point (sample order)
   // grow-only per-call workspace
   void *ws = nullptr;
   size_t ws_bytes = 0;
   size_t counters_off = 0;  // offset of the last call's counters in ws
   int num_sms = 0;
   int cluster = 0;          // CTAs per point (0 = choose per call)
-  int last_cluster = 0, last_grid = 0;
+  int last_cluster = 0, last_grid = 0, last_staged = 0;
 };
 
 namespace {
@@ -264,7 +268,7 @@ std::vector<double> sphere_offsets(double rad, int num, unsigned seed) {
 // The samples' order only changes the order of the sums; a space-filling
 // (Morton) order keeps each warp's gathers, and each cluster CTA's share of
 // the subvolume, spatially compact.
-std::vector<double> morton_order(const std::vector<double> &rel, double rad) {
+std::vector<size_t> morton_perm(const std::vector<double> &rel, double rad) {
   const size_t n = rel.size() / 3;
   std::vector<std::pair<uint64_t, size_t>> key(n);
   for (size_t i = 0; i < n; i++) {
@@ -282,9 +286,41 @@ std::vector<double> morton_order(const std::vector<double> &rel, double rad) {
                    [](const std::pair<uint64_t, size_t> &x, const std::pair<uint64_t, size_t> &y) {
                      return x.first < y.first;
                    });
+  std::vector<size_t> perm(n);
+  for (size_t i = 0; i < n; i++) perm[i] = key[i].second;
+  return perm;
+}
+
+// Cluster rank ranges: with samples in Morton order, the first 1, 2 or 3
+// code bits select the half, quarter slab or octant of the subvolume, so each
+// CTA of a 2-, 4- or 8-wide cluster gets one compact piece.
+void rank_ranges(const std::vector<double> &off, double rad, int C, int out[9]) {
+  const size_t n = off.size() / 3;
+  int bits = 0;
+  while ((1 << bits) < C) bits++;
+  std::vector<int> cnt(C + 1, 0);
+  for (size_t i = 0; i < n; i++) {
+    uint32_t top = 0;
+    // same quantisation as morton_perm; top bits interleave z, y, x
+    uint32_t q[3];
+    for (int d = 0; d < 3; d++) {
+      double u = (off[i * 3 + d] + rad) / (2.0 * rad + 1e-9);
+      q[d] = (uint32_t)std::min(1023.0, std::max(0.0, u * 1024.0));
+    }
+    const uint32_t code3 = ((q[2] >> 9) << 2) | ((q[1] >> 9) << 1) | (q[0] >> 9);
+    top = code3 >> (3 - bits);
+    cnt[top + 1]++;
+  }
+  for (int r = 0; r < C; r++) cnt[r + 1] += cnt[r];
+  for (int r = 0; r <= C; r++) out[r] = cnt[r];
+  for (int r = C + 1; r < 9; r++) out[r] = out[C];
+}
+
+std::vector<double> morton_order(const std::vector<double> &rel, double rad) {
+  const std::vector<size_t> perm = morton_perm(rel, rad);
   std::vector<double> out(rel.size());
-  for (size_t i = 0; i < n; i++)
-    for (int d = 0; d < 3; d++) out[i * 3 + d] = rel[key[i].second * 3 + d];
+  for (size_t i = 0; i < perm.size(); i++)
+    for (int d = 0; d < 3; d++) out[i * 3 + d] = rel[perm[i] * 3 + d];
   return out;
 }
 
@@ -292,11 +328,40 @@ int engine_finish(dvc_engine *e) {
   engine_geometry(e);
   if (e->bext[0] > 1023 || e->bext[1] > 1023 || e->bext[2] > 1023)
     return set_error(DVC_E_ARG, "interpolation box larger than 1023 voxels per axis");
+  const double rmax = e->subv_rad * std::max(e->p.subvol_aspect[0],
+                                             std::max(e->p.subvol_aspect[1], e->p.subvol_aspect[2]));
+  e->morton_rad = rmax;
   if (e->p.subvol_geom == DVC_SPHERE) {
-    std::vector<double> rel = morton_order(sphere_offsets(e->subv_rad, e->n_sub, e->p.sphere_seed),
-                                           e->subv_rad);
+    std::vector<double> rel0 = sphere_offsets(e->subv_rad, e->n_sub, e->p.sphere_seed);
+    std::vector<double> sc(rel0.size());
+    for (size_t i = 0; i < rel0.size(); i++) sc[i] = e->p.subvol_aspect[i % 3] * rel0[i];
+    const std::vector<size_t> pm = morton_perm(sc, rmax);
+    std::vector<double> rel(rel0.size());
+    for (size_t i = 0; i < pm.size(); i++)
+      for (int d = 0; d < 3; d++) rel[i * 3 + d] = rel0[pm[i] * 3 + d];
     CUDA_TRY(cudaMalloc(&e->d_sphere, rel.size() * sizeof(double)));
     CUDA_TRY(cudaMemcpy(e->d_sphere, rel.data(), rel.size() * sizeof(double), cudaMemcpyHostToDevice));
+    e->h_offsets.resize(rel.size());
+    for (size_t i = 0; i < rel.size(); i++) e->h_offsets[i] = e->p.subvol_aspect[i % 3] * rel[i];
+  } else {
+    // cube samples on the n^3 grid (FloatingCloud, Core/FloatingCloud.cpp:84-128),
+    // taken in a space-filling order
+    const int nn = e->cube_n;
+    std::vector<double> off((size_t)e->n_sub * 3);
+    for (int i = 0; i < e->n_sub; i++) {
+      const int idx[3] = {i % nn, (i / nn) % nn, i / (nn * nn)};
+      for (int d = 0; d < 3; d++) {
+        const double r = e->subv_rad * e->p.subvol_aspect[d];
+        off[(size_t)i * 3 + d] = -r + idx[d] * (2.0 * r / std::max(1, nn - 1));
+      }
+    }
+    const std::vector<size_t> perm = morton_perm(off, rmax);
+    std::vector<int> order(perm.begin(), perm.end());
+    CUDA_TRY(cudaMalloc(&e->d_cube_order, order.size() * sizeof(int)));
+    CUDA_TRY(cudaMemcpy(e->d_cube_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice));
+    e->h_offsets.resize(off.size());
+    for (size_t i = 0; i < perm.size(); i++)
+      for (int d = 0; d < 3; d++) e->h_offsets[i * 3 + d] = off[perm[i] * 3 + d];
   }
   CUDA_TRY(cudaGetDevice(&e->device));
   CUDA_TRY(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device));
@@ -324,8 +389,8 @@ int ensure_ws(dvc_engine *e, size_t bytes) {
 }
 
 template <typename VT, int IT>
-int launch_search(SearchArgs &a, size_t smem_dyn, int grid, int cluster, cudaStream_t st,
-                  int *max_clusters) {
+int launch_search(SearchArgs &a, const CUtensorMap &tmap, size_t smem_dyn, int grid, int cluster,
+                  cudaStream_t st, int *max_clusters) {
   auto kern = search_kernel<VT, IT>;
   CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dyn));
   cudaLaunchConfig_t cfg = {};
@@ -345,20 +410,62 @@ int launch_search(SearchArgs &a, size_t smem_dyn, int grid, int cluster, cudaStr
     return DVC_OK;
   }
   cfg.gridDim = dim3(grid, 1, 1);
-  CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a));
+  CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a, tmap));
   return DVC_OK;
 }
 
-int dispatch_launch(int bpv, int it, SearchArgs &a, size_t smem, int grid, int cluster,
-                    cudaStream_t st, int *max_clusters) {
-  if (bpv == 1) {
-    if (it == 2) return launch_search<uint8_t, 2>(a, smem, grid, cluster, st, max_clusters);
-    if (it == 1) return launch_search<uint8_t, 1>(a, smem, grid, cluster, st, max_clusters);
-    return launch_search<uint8_t, 0>(a, smem, grid, cluster, st, max_clusters);
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
   }
-  if (it == 2) return launch_search<uint16_t, 2>(a, smem, grid, cluster, st, max_clusters);
-  if (it == 1) return launch_search<uint16_t, 1>(a, smem, grid, cluster, st, max_clusters);
-  return launch_search<uint16_t, 0>(a, smem, grid, cluster, st, max_clusters);
+  return fn;
+}
+
+// Staging box for a cluster of C CTAs: per CTA rank, the extent of its share
+// of the stable sample offsets, plus stencil, rounding and warp margins; x
+// rounded so every copy starts and spans whole 16-byte units.
+void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int rs[9], int out[3]) {
+  double emax[3] = {0.0, 0.0, 0.0};
+  for (int r = 0; r < C; r++) {
+    const int lo = rs[r], hi = rs[r + 1];
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int i = lo; i < hi; i++)
+      for (int d = 0; d < 3; d++) {
+        mn[d] = std::min(mn[d], e->h_offsets[(size_t)i * 3 + d]);
+        mx[d] = std::max(mx[d], e->h_offsets[(size_t)i * 3 + d]);
+      }
+    for (int d = 0; d < 3; d++) emax[d] = std::max(emax[d], mx[d] - mn[d]);
+  }
+  const int al = 16 / esize;
+  for (int d = 0; d < 3; d++) out[d] = (int)ceil(emax[d] + 2.0 * reach) + 6;
+  out[0] = ((out[0] + al - 1 + al - 1) / al) * al;
+}
+
+int dispatch_launch(int bpv, int it, SearchArgs &a, const CUtensorMap &tm, size_t smem, int grid,
+                    int cluster, cudaStream_t st, int *max_clusters) {
+  if (bpv == 1) {
+    if (it == 2) return launch_search<uint8_t, 2>(a, tm, smem, grid, cluster, st, max_clusters);
+    if (it == 1) return launch_search<uint8_t, 1>(a, tm, smem, grid, cluster, st, max_clusters);
+    return launch_search<uint8_t, 0>(a, tm, smem, grid, cluster, st, max_clusters);
+  }
+  if (it == 2) return launch_search<uint16_t, 2>(a, tm, smem, grid, cluster, st, max_clusters);
+  if (it == 1) return launch_search<uint16_t, 1>(a, tm, smem, grid, cluster, st, max_clusters);
+  return launch_search<uint16_t, 0>(a, tm, smem, grid, cluster, st, max_clusters);
 }
 
 }  // namespace
@@ -439,6 +546,7 @@ void dvc_gpu_destroy(dvc_engine *e) {
     if (e->cor) cudaFree(e->cor);
   }
   if (e->d_sphere) cudaFree(e->d_sphere);
+  if (e->d_cube_order) cudaFree(e->d_cube_order);
   if (e->ws) cudaFree(e->ws);
   delete e;
 }
@@ -461,23 +569,71 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
   // launch shape: one cluster of C CTAs per point in flight, persistent grid
   // of as many clusters as fit. Points waiting on neighbours (the reference's
   // seeding) favour wide clusters (short per-point latency); independent
-  // points favour narrow ones (fewer cluster barriers).
+  // points favour narrow ones (fewer cluster barriers). Each CTA stages the
+  // correlate region of its samples in shared memory (TMA) when the volume's
+  // layout allows it and the box fits.
+  const int esize = p.bytes_per_voxel;
+  const size_t kDynBudget = 190 * 1024;
+  const bool tma_layout = encode_tiled_fn() != nullptr &&
+                          ((size_t)p.vol_wide * esize) % 16 == 0 &&
+                          ((size_t)p.vol_wide * p.vol_high * esize) % 16 == 0 &&
+                          ((uintptr_t)e->cor % 16) == 0 && !getenv("DVC_NO_STAGE");
   int C = e->cluster;
   if (C <= 0) {
     const int per = (seed_mode == DVC_SEED_NEIGHBOURS) ? 256 : 1024;
     C = 1;
     while (C < 8 && e->n_sub / (2 * C) >= per) C *= 2;
   }
-  int cap = (e->n_sub + C - 1) / C;
-  while (state_bytes(cap) > 160 * 1024 && C < 8) {
-    C *= 2;
-    cap = (e->n_sub + C - 1) / C;
+  int cap = 0, stage[3] = {0, 0, 0}, rs[9];
+  size_t stage_bytes = 0;
+  bool staged = false;
+  for (;;) {
+    rank_ranges(e->h_offsets, e->morton_rad, C, rs);
+    cap = 0;
+    for (int r = 0; r < C; r++) cap = std::max(cap, rs[r + 1] - rs[r]);
+    staged = tma_layout;
+    if (staged) {
+      // one region per point covers every grid translation (reach k * inc)
+      double reach = 0.0;
+      if (p.basin_radius != 0.0) {
+        const int k = (int)((double)p.disp_max / p.basin_radius);
+        reach = k * ((double)p.disp_max / k);
+      }
+      stage_dims(e, C, esize, reach, rs, stage);
+      if (stage[0] > 256 || stage[1] > 256 || stage[2] > 256) staged = false;
+      stage_bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;
+      if (staged && stage_bytes + state_bytes(cap) > kDynBudget) staged = false;
+    }
+    const size_t need = (staged ? stage_bytes : 0) + state_bytes(cap);
+    if ((tma_layout && !staged) || need > kDynBudget) {
+      if (C < 8) {
+        C *= 2;
+        continue;
+      }
+    }
+    if (need > kDynBudget && !staged && state_bytes(cap) > kDynBudget)
+      return set_error(DVC_E_ARG, "subvolume too large for the search kernel");
+    break;
   }
-  if (state_bytes(cap) > 160 * 1024) return set_error(DVC_E_ARG, "subvolume too large for the search kernel");
-  const size_t smem_dyn = state_bytes(cap);
+  const size_t smem_dyn = (staged ? stage_bytes : 0) + state_bytes(cap);
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof tmap);
+  if (staged) {
+    const cuuint64_t gdim[3] = {(cuuint64_t)p.vol_wide, (cuuint64_t)p.vol_high, (cuuint64_t)p.vol_tall};
+    const cuuint64_t gstride[2] = {(cuuint64_t)p.vol_wide * esize,
+                                   (cuuint64_t)p.vol_wide * p.vol_high * esize};
+    const cuuint32_t box[3] = {(cuuint32_t)stage[0], (cuuint32_t)stage[1], (cuuint32_t)stage[2]};
+    const cuuint32_t estride[3] = {1, 1, 1};
+    const CUresult r = encode_tiled_fn()(
+        &tmap, esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, e->cor,
+        gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) staged = false;
+  }
   int max_clusters = 0;
   SearchArgs probe{};
-  int rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, smem_dyn, 0, C, st, &max_clusters);
+  int rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tmap, smem_dyn, 0, C, st,
+                           &max_clusters);
   if (rc) return rc;
   if (max_clusters < 1) return set_error(DVC_E_ARG, "search kernel cluster does not fit");
   const int grid = C * std::max(1, std::min(max_clusters, n_process));
@@ -551,9 +707,15 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
   a.done = done;
   a.counters = counters;
   a.local_cap = cap;
+  a.cube_order = e->d_cube_order;
+  a.stage_on = staged ? 1 : 0;
+  for (int d = 0; d < 3; d++) a.stage[d] = stage[d];
+  a.stage_bytes = (int)stage_bytes;
+  for (int r = 0; r < 9; r++) a.rank_start[r] = rs[r];
   e->last_cluster = C;
   e->last_grid = grid;
-  return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, smem_dyn, grid, C, st, nullptr);
+  e->last_staged = staged;
+  return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, tmap, smem_dyn, grid, C, st, nullptr);
 }
 
 int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_process,
@@ -701,15 +863,14 @@ int dvc_gpu_interpolate(dvc_engine *e, int volume, const double center[3], int n
   CUDA_TRY(cudaMemset(d_und, 0, sizeof(unsigned long long)));
   CUDA_TRY(cudaMemcpy(d_pts, pts, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
   const void *vp = volume == 0 ? e->ref : e->cor;
+  const BoxGeom Gm{o[0], o[1], o[2], e->bext[0], e->bext[1], e->bext[2]};
   const int T = 256, G = (n + T - 1) / T;
   if (e->p.bytes_per_voxel == 1) {
-    VolView<uint8_t> V{(const uint8_t *)vp, vol[0], vol[1], vol[2], o[0], o[1], o[2],
-                       e->bext[0], e->bext[1], e->bext[2], checked};
-    interp_points_kernel<uint8_t><<<G, T>>>(V, n, d_pts, interp_type, d_out, d_und);
+    GSrc<uint8_t> V{(const uint8_t *)vp, vol[0], vol[1], vol[2], checked};
+    interp_points_kernel<uint8_t><<<G, T>>>(V, Gm, n, d_pts, interp_type, d_out, d_und);
   } else {
-    VolView<uint16_t> V{(const uint16_t *)vp, vol[0], vol[1], vol[2], o[0], o[1], o[2],
-                        e->bext[0], e->bext[1], e->bext[2], checked};
-    interp_points_kernel<uint16_t><<<G, T>>>(V, n, d_pts, interp_type, d_out, d_und);
+    GSrc<uint16_t> V{(const uint16_t *)vp, vol[0], vol[1], vol[2], checked};
+    interp_points_kernel<uint16_t><<<G, T>>>(V, Gm, n, d_pts, interp_type, d_out, d_und);
   }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpy(out, d_out, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));

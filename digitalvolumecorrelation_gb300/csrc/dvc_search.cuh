@@ -26,7 +26,10 @@
 //   obj_SAD .. obj_ZNSSD     ObjectiveFunctions.cpp:24-263 -> objective sums
 #pragma once
 #include <cooperative_groups.h>
+#include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "../../include/dvc_gpu.h"
 #include "dvc_device.cuh"
@@ -61,6 +64,13 @@ struct SearchArgs {
   int *work_counter, *done, *error_flag;
   unsigned long long *counters;  // [0] evaluations, [1] GN iterations, [2] undefined evals
   int local_cap;                 // per-CTA sample capacity of the dynamic arrays
+  const int *cube_order;         // cube samples in space-filling order (natural index)
+  // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
+  // voxels per evaluation, TMA-loaded into one of two shared buffers
+  int stage_on;
+  int stage[3];
+  int stage_bytes;               // one buffer, padded
+  int rank_start[9];             // sample range of each cluster rank
 };
 
 struct DBox {
@@ -77,9 +87,17 @@ struct PointHeader {
   int chk_ref, chk_cor;
 };
 
+struct Region {
+  int r0[3];  // global voxel coordinates of the staged box's first element (x aligned)
+  int ok;     // the staged box covers this CTA's samples for the evaluation
+};
+
 struct CtaState {
   PointHeader H;
   double sref[3], sbmn[3], sbmx[3];
+  double lbmn[3], lbmx[3];  // this CTA's share of the stable cloud: bbox
+  Region reg[2];
+  unsigned long long bar[2];
   int kint[3];        // s_ref + seed - O_cor: integer part
   float kfrac[3];     //                       fractional part
   float shift;        // value shift of the objective sums
@@ -237,7 +255,8 @@ __device__ __forceinline__ void stable_pos(const SearchArgs &a, const double pt[
       p[d] = __dadd_rn(pt[d], __dmul_rn(a.aspect[d], a.sphere_rel[(size_t)i * 3 + d]));
   } else {
     const int nn = a.cube_n;
-    const int idx[3] = {i % nn, (i / nn) % nn, i / (nn * nn)};
+    const int j = a.cube_order ? a.cube_order[i] : i;
+    const int idx[3] = {j % nn, (j / nn) % nn, j / (nn * nn)};
     for (int d = 0; d < 3; d++) {
       const double r = __dmul_rn(a.subv_rad, a.aspect[d]);
       const double bmin = __dadd_rn(pt[d], -r);
@@ -466,12 +485,137 @@ __device__ void warp_qr_solve(CtaState &S, int n) {
   __syncwarp();
 }
 
+// ----------------------------------------------------------- TMA staging ---
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+// One elected thread: order earlier generic-proxy reads of the buffer before
+// the asynchronous write, arm the barrier with the byte count, start the
+// 3D tiled copy (coordinates x, y, z in voxels; out-of-volume parts read 0).
+__device__ __forceinline__ void tma_load_3d(const CUtensorMap *tm, uint32_t dst, uint32_t bar,
+                                            int x, int y, int z, uint32_t bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+// Bounded wait for the barrier's phase; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  for (long long i = 0; i < (1LL << 24); i++) {
+    uint32_t ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (ok) return true;
+    if (i > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+// Staged region covering positions [pmin, pmax] (global voxel coordinates)
+// with the stencil margin; ok = 0 when it does not fit the staging box.
+__device__ __forceinline__ Region make_region(const SearchArgs &a, const double pmin[3],
+                                              const double pmax[3], int esize) {
+  Region r;
+  r.ok = a.stage_on;
+  const int al = 16 / esize;
+  for (int d = 0; d < 3; d++) {
+    const double lo = floor(pmin[d]) - 2.0, hi = floor(pmax[d]) + 3.0;
+    if (!(lo > -1e9 && hi < 1e9)) {  // NaN or absurd positions: do not stage
+      r.ok = 0;
+      r.r0[d] = 0;
+      continue;
+    }
+    int l = (int)lo;
+    if (d == 0) l = (l >= 0) ? (l / al) * al : -(((-l) + al - 1) / al) * al;
+    r.r0[d] = l;
+    if ((int)hi - l + 1 > a.stage[d]) r.ok = 0;
+  }
+  return r;
+}
+
+template <typename VT, int IT, bool GRAD>
+__device__ __noinline__ float interp_gsrc(const GSrc<VT> src, int l0, int l1, int l2, int k0, int k1,
+                                          int k2, float f0, float f1, float f2, float *g) {
+  const int lo[3] = {l0, l1, l2}, kind[3] = {k0, k1, k2};
+  const float f[3] = {f0, f1, f2};
+  float gg[3];
+  const float v = interp_at<GSrc<VT>, IT, GRAD>(src, lo, kind, f, gg);
+  if (GRAD)
+    for (int d = 0; d < 3; d++) g[d] = gg[d];
+  return v;
+}
+
+// One sample of the correlate volume: from the staged box when its stencil
+// lies inside, otherwise from global memory.
+template <typename VT, int IT, bool GRAD>
+__device__ __forceinline__ float eval_sample(bool staged, const SSrc<VT> &ss, const int r0[3],
+                                             const int B[3], const GSrc<VT> &gs, const BoxGeom &G,
+                                             int c[3], float f[3], float g[3], bool &undef) {
+  int lo[3], kind[3];
+  undef = prep_cell<IT>(G, c, f, lo, kind);
+  const int w = IT == 0 ? 1 : 4;
+  const bool in = staged && lo[0] >= r0[0] && lo[0] + w <= r0[0] + B[0] && lo[1] >= r0[1] &&
+                  lo[1] + w <= r0[1] + B[1] && lo[2] >= r0[2] && lo[2] + w <= r0[2] + B[2];
+  if (in) return interp_at<SSrc<VT>, IT, GRAD>(ss, lo, kind, f, g);
+  return interp_gsrc<VT, IT, GRAD>(gs, lo[0], lo[1], lo[2], kind[0], kind[1], kind[2], f[0], f[1],
+                                   f[2], g);
+}
+
+// The same with a compile-time choice: STAGED uses the staged box (and the
+// out-of-line global path for the rare samples outside it); otherwise the
+// global path is inlined.
+template <typename VT, int IT, bool GRAD, bool STAGED>
+__device__ __forceinline__ float eval_sample_t(const SSrc<VT> &ss, const int r0[3], const int B[3],
+                                               const GSrc<VT> &gs, const BoxGeom &G, int c[3],
+                                               float f[3], float g[3], bool &undef) {
+  if (STAGED) return eval_sample<VT, IT, GRAD>(true, ss, r0, B, gs, G, c, f, g, undef);
+  int lo[3], kind[3];
+  undef = prep_cell<IT>(G, c, f, lo, kind);
+  return interp_at<GSrc<VT>, IT, GRAD>(gs, lo, kind, f, g);
+}
+
+// Keep the staged region when it covers positions [pmn, pmx] with the stencil
+// margin; otherwise stage a new one into the same buffer. One thread; returns
+// 1 when a copy was started (the block then waits for it).
+__device__ __forceinline__ int restage(const SearchArgs &a, CtaState &S, const double pmn[3],
+                                       const double pmx[3], int esize, const CUtensorMap *tm,
+                                       uint32_t buf, uint32_t bar, uint32_t tx) {
+  const Region cur = S.reg[0];
+  if (cur.ok) {
+    bool in = true;
+    for (int d = 0; d < 3; d++) {
+      const double lo = floor(pmn[d]) - 2.0, hi = floor(pmx[d]) + 3.0;
+      if (!(lo >= cur.r0[d] && hi < cur.r0[d] + a.stage[d])) in = false;
+    }
+    if (in) return 0;
+  }
+  const Region r = make_region(a, pmn, pmx, esize);
+  S.reg[0] = r;
+  if (!r.ok) return 0;
+  tma_load_3d(tm, buf, bar, r.r0[0], r.r0[1], r.r0[2], tx);
+  return 1;
+}
+
 // Range check of the moving sample cloud against the correlate act box
 // (BoundBox::contains in tri_cub_Lek, Core/Interpolate.cpp:474-481).
 // Translation only: the exact FP64 bbox (stable bbox + u, affine_to). With a
-// rotation/strain: min/max of the warped samples over the cluster.
+// rotation/strain: min/max of the warped samples over the cluster. Also
+// leaves this CTA's own position range in pmn/pmx (local voxel frame).
 __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float *s_fp, int nl,
-                                            CtaState &S, bool rot) {
+                                            CtaState &S, bool rot, double pmn[3], double pmx[3]) {
   if (!rot) {
     if (threadIdx.x == 0) {
       int fail = 0;
@@ -481,6 +625,10 @@ __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float
         if (!(bmn >= S.H.act_cor.mn[d]) || !(bmx <= S.H.act_cor.mx[d])) fail = 1;
       }
       S.fail = fail;
+    }
+    for (int d = 0; d < 3; d++) {
+      pmn[d] = S.lbmn[d] + S.par[d];
+      pmx[d] = S.lbmx[d] + S.par[d];
     }
     __syncthreads();
     return;
@@ -497,6 +645,10 @@ __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float
     }
   }
   cta_min<6>(m, S, S.cbuf[cl.parity]);
+  for (int d = 0; d < 3; d++) {
+    pmn[d] = (double)S.H.o_cor[d] + S.cbuf[cl.parity][d];
+    pmx[d] = (double)S.H.o_cor[d] - S.cbuf[cl.parity][3 + d];
+  }
   cluster_reduce(cl, S, 6, 6);
   if (threadIdx.x == 0) {
     int fail = 0;
@@ -512,28 +664,44 @@ __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float
 
 // ================================================================ kernel ===
 template <typename VT, int IT>
-__global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
-  extern __shared__ __align__(16) unsigned char dsm[];
+__global__ void __launch_bounds__(kThreads, 1)
+    search_kernel(const __grid_constant__ SearchArgs a, const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(128) unsigned char dsm[];
   __shared__ CtaState S;
   Cl cl{cg::this_cluster(), 0u, 1u, 0};
   cl.rank = cl.g.block_rank();
   cl.size = cl.g.num_blocks();
   const int tid = threadIdx.x;
   const int nsub = a.n_sub;
-  const int lo = (int)((long long)nsub * cl.rank / cl.size);
-  const int nl = (int)((long long)nsub * (cl.rank + 1) / cl.size) - lo;
+  const int lo = a.rank_start[cl.rank];
+  const int nl = a.rank_start[cl.rank + 1] - lo;
+  constexpr int esize = (int)sizeof(VT);
 
-  // per-CTA sample state: packed cell base, cell fraction (3), reference
-  // quantity, final values; and the Gauss-Newton chunk rows
+  // dynamic shared memory: two staging buffers, then the per-CTA sample
+  // state (packed cell base, fraction x3, reference quantity, final value)
+  // and the Gauss-Newton chunk rows
+  const int sb = a.stage_on ? a.stage_bytes : 0;
+  unsigned char *stage_buf[2] = {dsm, dsm};
   const int cap = a.local_cap;
-  int *s_ip = reinterpret_cast<int *>(dsm);
+  int *s_ip = reinterpret_cast<int *>(dsm + sb);
   float *s_fp = reinterpret_cast<float *>(s_ip + cap);
   float *s_r = s_fp + 3 * cap;
   float *s_t = s_r + cap;
   float *s_G = s_t + cap;  // [kGRows][kThreads]
+  const uint32_t bar_addr[2] = {smem_addr(&S.bar[0]), smem_addr(&S.bar[1])};
+  const uint32_t buf_addr[2] = {smem_addr(stage_buf[0]), smem_addr(stage_buf[1])};
+  uint32_t phase[2] = {0u, 0u};
+  if (tid == 0) {
+    mbar_init(bar_addr[0]);
+    mbar_init(bar_addr[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int B[3] = {a.stage[0], a.stage[1], a.stage[2]};
+  const uint32_t stage_tx = (uint32_t)(B[0] * B[1] * B[2] * esize);
 
-  const VolView<VT> vbase{reinterpret_cast<const VT *>(a.ref), a.nx, a.ny, a.nz, 0, 0, 0,
-                          a.bext[0], a.bext[1], a.bext[2], false};
+  const GSrc<VT> gref{reinterpret_cast<const VT *>(a.ref), a.nx, a.ny, a.nz, false};
+  const GSrc<VT> gcor0{reinterpret_cast<const VT *>(a.cor), a.nx, a.ny, a.nz, false};
   const int ndof = a.ndof;
   const int fcn = a.objfcn;
   const bool sad = (fcn == DVC_SAD);
@@ -569,10 +737,11 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
       cl.g.sync();
       continue;
     }
-    VolView<VT> Vref = vbase, Vcor = vbase;
-    Vcor.vol = reinterpret_cast<const VT *>(a.cor);
-    Vref.ox = S.H.o_ref[0]; Vref.oy = S.H.o_ref[1]; Vref.oz = S.H.o_ref[2]; Vref.checked = S.H.chk_ref;
-    Vcor.ox = S.H.o_cor[0]; Vcor.oy = S.H.o_cor[1]; Vcor.oz = S.H.o_cor[2]; Vcor.checked = S.H.chk_cor;
+    GSrc<VT> gsr = gref, gsc = gcor0;
+    gsr.checked = S.H.chk_ref;
+    gsc.checked = S.H.chk_cor;
+    const BoxGeom Gref{S.H.o_ref[0], S.H.o_ref[1], S.H.o_ref[2], a.bext[0], a.bext[1], a.bext[2]};
+    const BoxGeom Gcor{S.H.o_cor[0], S.H.o_cor[1], S.H.o_cor[2], a.bext[0], a.bext[1], a.bext[2]};
     unsigned long long n_eval = 0, n_undef = 0;
     if (tid == 0) S.fail = 0;
 
@@ -596,7 +765,7 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
         clamp_cell(c, a.bext);
         bool und;
         float g[3];
-        const float r = interp_sample<VT, IT, false>(Vref, c, f, g, und);
+        const float r = interp_global<VT, IT, false>(gsr, Gref, c, f, g, und);
         n_undef += und;
         s_r[i] = r;
         s_ip[i] = ip[0] | (ip[1] << 10) | (ip[2] << 20);
@@ -606,6 +775,11 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
         rk[0].add(r);
       }
       cta_min<6>(m, S, S.cbuf[cl.parity]);
+      if (tid == 0)
+        for (int d = 0; d < 3; d++) {  // this CTA's stable sub-bbox (global frame)
+          S.lbmn[d] = S.cbuf[cl.parity][d];
+          S.lbmx[d] = -S.cbuf[cl.parity][3 + d];
+        }
       cta_sum_comp<1>(rk, S, S.cbuf[cl.parity] + 6);
       cluster_reduce(cl, S, 7, 6);
     }
@@ -663,70 +837,103 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
     // trgrid_global (Core/Search.cpp:934-1043): (2k+1)^3 translations; the
     // first strictly smaller objective in z, y, x loop order wins. Any
     // translation whose sample box leaves the active box fails the point.
+    // The correlate region of each translation is staged by TMA into one of
+    // two buffers while the previous translation is evaluated.
     if (a.do_grid) {
       const int k = a.num_inc;
       const int side = 2 * k + 1;
       const int total = side * side * side;
       const double inc = a.inc;
-      for (int o0 = 0; o0 < total; o0 += kGridChunk) {
-        const int nch = min(kGridChunk, total - o0);
+      // range check of every translation first (exact FP64; one thread each)
+      {
         int bad = 0;
-        if (tid < nch) {
-          const int o = o0 + tid;
+        for (int o = tid; o < total; o += kThreads) {
           const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
           for (int d = 0; d < 3; d++) {
             const double pc = __dadd_rn(S.par[d], __dmul_rn((double)off[d], inc));
             if (!(__dadd_rn(S.sbmn[d], pc) >= S.H.act_cor.mn[d]) ||
                 !(__dadd_rn(S.sbmx[d], pc) <= S.H.act_cor.mx[d]))
               bad = 1;
-            split_d(__dsub_rn(pc, S.H.seed[d]), S.giu[tid][d], S.gfu[tid][d]);
           }
         }
         if (__syncthreads_or(bad)) {
           if (tid == 0) S.fail = 1;
           __syncthreads();
-          break;
         }
-        const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll 1
-        for (int j = 0; j < nch; j++) {
-          const int iu[3] = {S.giu[j][0], S.giu[j][1], S.giu[j][2]};
-          const float fu[3] = {S.gfu[j][0], S.gfu[j][1], S.gfu[j][2]};
-          float p0 = 0.f, p1 = 0.f, p2 = 0.f;
-          for (int i = tid; i < nl; i += kThreads) {
-            int c[3];
-            float f[3], g[3];
-            sample_pos(s_ip, s_fp, i, S, iu, fu, false, c, f);
-            clamp_cell(c, a.bext);
-            bool und;
-            const float t = interp_sample<VT, IT, false>(Vcor, c, f, g, und) - S.shift;
-            n_undef += und;
-            const float q = s_r[i];
-            if (sad) {
-              p0 += fabsf(t - q);
-            } else {
-              p0 += t;
-              p1 += t * t;
-              p2 += t * q;
-            }
-          }
-#pragma unroll
-          for (int o = 16; o; o >>= 1) {
-            p0 += __shfl_xor_sync(0xffffffffu, p0, o);
-            p1 += __shfl_xor_sync(0xffffffffu, p1, o);
-            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
-          }
-          if (lane == 0) {
-            S.wpart[warp][3 * j + 0] = p0;
-            S.wpart[warp][3 * j + 1] = p1;
-            S.wpart[warp][3 * j + 2] = p2;
+      }
+      if (S.fail) goto point_done;
+      // one staged region covering this CTA's samples under every translation
+      if (tid == 0) {
+        double pmn[3], pmx[3];
+        for (int d = 0; d < 3; d++) {
+          pmn[d] = S.lbmn[d] + S.par[d] - k * inc;
+          pmx[d] = S.lbmx[d] + S.par[d] + k * inc;
+        }
+        Region r = make_region(a, pmn, pmx, esize);
+        S.reg[0] = r;
+        if (r.ok) tma_load_3d(&tmap, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
+      }
+      __syncthreads();
+      const Region rg = S.reg[0];
+      if (rg.ok) {
+        if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
+        phase[0] ^= 1u;
+      }
+      const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
+      const int lane = tid & 31, warp = tid >> 5;
+      for (int o0 = 0; o0 < total; o0 += kGridChunk) {
+        const int nch = min(kGridChunk, total - o0);
+        if (tid < nch) {
+          const int o = o0 + tid;
+          const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
+          for (int d = 0; d < 3; d++) {
+            const double pc = __dadd_rn(S.par[d], __dmul_rn((double)off[d], inc));
+            split_d(__dsub_rn(pc, S.H.seed[d]), S.giu[tid][d], S.gfu[tid][d]);
           }
         }
         __syncthreads();
-        for (int q = tid; q < 3 * nch; q += kThreads) {
-          double s = 0.0;
-          for (int w = 0; w < kWarps; w++) s += (double)S.wpart[w][q];
-          S.cbuf[cl.parity][q] = s;
+        // each warp evaluates whole translations: its lanes cover this CTA's
+        // samples, one shuffle reduction per translation, no block barrier
+#pragma unroll 1
+        for (int j = warp; j < nch; j += kWarps) {
+          const int iu[3] = {S.giu[j][0], S.giu[j][1], S.giu[j][2]};
+          const float fu[3] = {S.gfu[j][0], S.gfu[j][1], S.gfu[j][2]};
+          float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+          auto body = [&](auto staged_tag) {
+            constexpr bool ST = decltype(staged_tag)::value;
+            for (int i = lane; i < nl; i += 32) {
+              int c[3];
+              float f[3], g[3];
+              sample_pos(s_ip, s_fp, i, S, iu, fu, false, c, f);
+              clamp_cell(c, a.bext);
+              bool und;
+              const float t = eval_sample_t<VT, IT, false, ST>(ss, rg.r0, B, gsc, Gcor, c, f, g, und) - S.shift;
+              n_undef += und;
+              const float q = s_r[i];
+              if (sad) {
+                p0 += fabsf(t - q);
+              } else {
+                p0 += t;
+                p1 += t * t;
+                p2 += t * q;
+              }
+            }
+          };
+          if (rg.ok) body(std::true_type{});
+          else body(std::false_type{});
+          // compensated warp reduction (TwoSum tree)
+          float l0 = 0.f, l1 = 0.f, l2 = 0.f;
+#pragma unroll
+          for (int sh = 16; sh; sh >>= 1) {
+            two_sum_merge(p0, l0, __shfl_xor_sync(0xffffffffu, p0, sh), __shfl_xor_sync(0xffffffffu, l0, sh));
+            two_sum_merge(p1, l1, __shfl_xor_sync(0xffffffffu, p1, sh), __shfl_xor_sync(0xffffffffu, l1, sh));
+            two_sum_merge(p2, l2, __shfl_xor_sync(0xffffffffu, p2, sh), __shfl_xor_sync(0xffffffffu, l2, sh));
+          }
+          if (lane == 0) {
+            S.cbuf[cl.parity][3 * j + 0] = (double)p0 + (double)l0;
+            S.cbuf[cl.parity][3 * j + 1] = (double)p1 + (double)l1;
+            S.cbuf[cl.parity][3 * j + 2] = (double)p2 + (double)l2;
+          }
         }
         cluster_reduce(cl, S, 3 * nch, 0);
         if (tid < nch)
@@ -743,13 +950,14 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
         __syncthreads();
         n_eval += nch;
       }
-      if (S.fail) goto point_done;
       if (tid == 0 && S.best >= 0) {
         const int o = S.best;
         const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
         for (int d = 0; d < 3; d++) S.par[d] += (double)off[d] * inc;
       }
       __syncthreads();
+    } else if (tid == 0) {
+      S.reg[0].ok = 0;
     }
 
     // ------------------------------------------------- Gauss-Newton ---
@@ -792,8 +1000,17 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
         }
         __syncthreads();
         const bool rot = S.use_rot;
-        range_check(cl, s_ip, s_fp, nl, S, rot);
+        double pmn[3], pmx[3];
+        range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
         if (S.fail) goto point_done;
+        if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, &tmap, buf_addr[0], bar_addr[0], stage_tx);
+        __syncthreads();
+        const Region rg = S.reg[0];
+        if (S.stop) {
+          if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
+          phase[0] ^= 1u;
+        }
+        const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
 
         KSum v[4];
         float gg = 0.f;
@@ -809,7 +1026,9 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
             sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
             clamp_cell(c, a.bext);
             bool und;
-            t = interp_sample<VT, IT, true>(Vcor, c, f, gv, und) - S.shift;
+            t = (rg.ok ? eval_sample_t<VT, IT, true, true>(ss, rg.r0, B, gsc, Gcor, c, f, gv, und)
+                       : eval_sample_t<VT, IT, true, false>(ss, rg.r0, B, gsc, Gcor, c, f, gv, und)) -
+                S.shift;
             n_undef += und;
             q = s_r[i];
             one = 1.f;
@@ -867,9 +1086,9 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
           parts[tid] = (my_part < nparts) ? (double)gg : 0.0;
           __syncthreads();
           if (tid < nent) {
-            double s = 0.0;
-            for (int pp = 0; pp < nparts; pp++) s += parts[pp * nent + tid];
-            S.cbuf[cl.parity][4 + tid] = s;
+            double sum = 0.0;
+            for (int pp = 0; pp < nparts; pp++) sum += parts[pp * nent + tid];
+            S.cbuf[cl.parity][4 + tid] = sum;
           }
         }
         cluster_reduce(cl, S, 4 + nent, 0);
@@ -978,9 +1197,18 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
       }
       __syncthreads();
       const bool rot = S.use_rot;
-      range_check(cl, s_ip, s_fp, nl, S, rot);
+      double pmn[3], pmx[3];
+      range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
       n_eval += 1;
       if (S.fail) goto point_done;
+      if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, &tmap, buf_addr[0], bar_addr[0], stage_tx);
+      __syncthreads();
+      const Region rg = S.reg[0];
+      if (S.stop) {
+        if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
+        phase[0] ^= 1u;
+      }
+      const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
       {
         KSum v[1];
         for (int i = tid; i < nl; i += kThreads) {
@@ -989,7 +1217,9 @@ __global__ void __launch_bounds__(kThreads, 2) search_kernel(SearchArgs a) {
           sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
           clamp_cell(c, a.bext);
           bool und;
-          const float t = interp_sample<VT, IT, false>(Vcor, c, f, g, und) - S.shift;
+          const float t = (rg.ok ? eval_sample_t<VT, IT, false, true>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)
+                                 : eval_sample_t<VT, IT, false, false>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)) -
+                          S.shift;
           n_undef += und;
           s_t[i] = t;
           v[0].add(t);

@@ -298,7 +298,7 @@ void rank_ranges(const std::vector<double> &off, double rad, int C, int out[9]) 
   const size_t n = off.size() / 3;
   int bits = 0;
   while ((1 << bits) < C) bits++;
-  std::vector<int> cnt(C + 1, 0);
+  int cnt[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (size_t i = 0; i < n; i++) {
     uint32_t top = 0;
     // same quantisation as morton_perm; top bits interleave z, y, x
@@ -551,10 +551,12 @@ void dvc_gpu_destroy(dvc_engine *e) {
   delete e;
 }
 
-int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev, int n_process,
-                           const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
-                           const double *seeds_dev, int *status_dev, double *objmin_dev,
-                           double *params_dev, int *gn_iters_dev, void *stream) {
+// The search launch. Scratch (done flags, ranks, work counter, counters) is
+// the engine's grow-only workspace, or `ws_fixed` when the caller supplies it.
+static int process_device_ws(dvc_engine *e, int n_points, const double *points_dev, int n_process,
+                             const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
+                             const double *seeds_dev, int *status_dev, double *objmin_dev,
+                             double *params_dev, int *gn_iters_dev, void *stream, char *ws_fixed) {
   if (!e) return set_error(DVC_E_ARG, "null engine");
   if (n_points < 0 || n_process < 0 || n_process > n_points)
     return set_error(DVC_E_ARG, "n_process must be in 0..n_points");
@@ -642,15 +644,18 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
   const size_t off_done = 0;
   const size_t off_rank = off_done + (size_t)n_points * 4;
   const size_t off_ctl = (off_rank + (size_t)n_points * 4 + 255) & ~(size_t)255;
-  rc = ensure_ws(e, off_ctl + 256);
-  if (rc) return rc;
-  char *ws = (char *)e->ws;
+  char *ws = ws_fixed;
+  if (!ws) {
+    rc = ensure_ws(e, off_ctl + 256);
+    if (rc) return rc;
+    ws = (char *)e->ws;
+    e->counters_off = off_ctl + 64;
+  }
   int *done = (int *)(ws + off_done);
   int *rank = (int *)(ws + off_rank);
   int *ctl = (int *)(ws + off_ctl);
   unsigned long long *counters = (unsigned long long *)(ws + off_ctl + 64);
   CUDA_TRY(cudaMemsetAsync(ws + off_ctl, 0, 256, st));
-  e->counters_off = off_ctl + 64;
   {
     const int T = 256;
     const int G = (n_points + T - 1) / T;
@@ -716,6 +721,64 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
   e->last_grid = grid;
   e->last_staged = staged;
   return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, tmap, smem_dyn, grid, C, st, nullptr);
+}
+
+int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev, int n_process,
+                           const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
+                           const double *seeds_dev, int *status_dev, double *objmin_dev,
+                           double *params_dev, int *gn_iters_dev, void *stream) {
+  return process_device_ws(e, n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev,
+                           seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev,
+                           stream, nullptr);
+}
+
+// ---- allocation-free search -------------------------------------------------
+// Some callers cannot allocate device memory at the moment they search: a host
+// program that owns the device memory budget through its own pool, or one
+// that records its work while device allocation is off limits. For them the
+// search's scratch (per-point done flags and ranks, the work counter, the
+// evaluation counters) lives in this fixed module array instead of the
+// engine's workspace. It holds DVC_NOALLOC_MAX_POINTS points, belongs to every
+// GPU that loads the library until the process exits, and is shared by all
+// calls: each call clears the parts that must start at zero, and calls whose
+// work overlaps on the GPU race on it.
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[(size_t)DVC_NOALLOC_MAX_POINTS * 8 + 512];
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (the host symbol is only a stand-in, never a device address).
+static int noalloc_scratch(char **out) {
+  static void *addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return set_error(DVC_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(err));
+  if (dev < 0 || dev >= 64) return set_error(DVC_E_ARG, "device index above 63");
+  if (!addr[dev]) {
+    void *p = nullptr;
+    err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (err != cudaSuccess || !p)
+      return set_error(DVC_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(err));
+    addr[dev] = p;
+  }
+  *out = (char *)addr[dev];
+  return DVC_OK;
+}
+
+int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *points_dev,
+                                   int n_process, const int *order_dev, int n_neigh,
+                                   const int *neigh_dev, int seed_mode, const double *seeds_dev,
+                                   int *status_dev, double *objmin_dev, double *params_dev,
+                                   int *gn_iters_dev, void *stream) {
+  if (n_points > DVC_NOALLOC_MAX_POINTS)
+    return set_error(DVC_E_ARG, "dvc_gpu_process_device_noalloc: n_points exceeds "
+                                "DVC_NOALLOC_MAX_POINTS (" + std::to_string(DVC_NOALLOC_MAX_POINTS) +
+                                    "); use dvc_gpu_process_device");
+  char *ws = nullptr;
+  const int rc = noalloc_scratch(&ws);
+  if (rc) return rc;
+  return process_device_ws(e, n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev,
+                           seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev,
+                           stream, ws);
 }
 
 int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_process,

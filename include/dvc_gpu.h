@@ -147,6 +147,28 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
                            const double *seeds_dev, int *status_dev, double *objmin_dev,
                            double *params_dev, int *gn_iters_dev, void *stream);
 
+/* ---- allocation-free search ---------------------------------------------
+ * No counterpart in the reference. Same as dvc_gpu_process_device, but the
+ * call allocates no device memory and calls no allocating routine: its scratch
+ * (per-point done flags and ranks, work counter, evaluation counters) is a
+ * fixed array inside the library, sized for DVC_NOALLOC_MAX_POINTS points,
+ * that every GPU using the library keeps until the process exits. For callers
+ * that must not allocate while they search (a host program that hands out all
+ * device memory from its own pool, or one recording its work where device
+ * allocation is not allowed). More points than DVC_NOALLOC_MAX_POINTS are
+ * rejected with DVC_E_ARG. The first call on a device looks up the array's
+ * device address (and may load the library's device code): make that first
+ * call before any stream capture. All calls share the one array; calls whose
+ * work overlaps on the GPU race on it, so serialise them. The engine must
+ * already exist (dvc_gpu_create / dvc_gpu_create_device allocate).
+ * dvc_gpu_last_counters does not report these calls. */
+#define DVC_NOALLOC_MAX_POINTS 65536
+int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *points_dev,
+                                   int n_process, const int *order_dev, int n_neigh,
+                                   const int *neigh_dev, int seed_mode, const double *seeds_dev,
+                                   int *status_dev, double *objmin_dev, double *params_dev,
+                                   int *gn_iters_dev, void *stream);
+
 /* Counters of the most recent dvc_gpu_process / dvc_gpu_process_device call
    on this engine (waits for it to finish): out[0] objective evaluations
    (reference subvolume, grid offsets, Gauss-Newton evaluations, final

@@ -144,6 +144,15 @@ struct GSrc {
     if (checked) return load_voxel_checked(vol, x, y, z, nx, ny, nz);
     return (float)__ldg(vol + ((long long)z * ny + y) * nx + x);
   }
+  // rows of the 4x4x4 stencil with low corner (x0, y0, z0): row (b, c) is at
+  // y0 + b, z0 + c
+  struct Stencil {
+    int x0, y0, z0;
+  };
+  __device__ __forceinline__ Stencil stencil(int x0, int y0, int z0) const { return {x0, y0, z0}; }
+  __device__ __forceinline__ void srow(const Stencil &h, int b, int c, float v[4]) const {
+    row4(h.x0, h.y0 + b, h.z0 + c, v);
+  }
 };
 
 __device__ __forceinline__ uint32_t lds32(uint32_t addr) {
@@ -161,44 +170,56 @@ template <typename VT>
 struct SSrc {
   uint32_t base;       // shared-memory address of the staged box
   int r0x, r0y, r0z;   // global voxel coordinates of the box's first element
-  int bx, by;          // box pitch (elements per row, rows per slice)
-  __device__ __forceinline__ uint32_t elem(int x, int y, int z) const {
-    return (uint32_t)(((z - r0z) * by + (y - r0y)) * bx + (x - r0x));
+  int bx, by;          // box pitch (elements per row, rows per slice); a row is
+                       // a whole number of 16-byte units
+  __device__ __forceinline__ uint32_t boff(int x, int y, int z) const {
+    return (uint32_t)(((z - r0z) * by + (y - r0y)) * bx + (x - r0x)) * (uint32_t)sizeof(VT);
+  }
+  // A stencil's rows all start at the same position inside their 4-byte
+  // word (row pitches are multiples of 16 bytes): keep the word address of
+  // the first row and the byte shift, each row is then one address add.
+  struct Stencil {
+    uint32_t al;  // shared-memory address of the 4-byte word holding the first voxel
+    uint32_t sh;  // byte position of the first voxel in that word
+  };
+  __device__ __forceinline__ Stencil stencil_at(uint32_t off) const { return {base + (off & ~3u), off & 3u}; }
+  __device__ __forceinline__ Stencil stencil(int x0, int y0, int z0) const {
+    return stencil_at(boff(x0, y0, z0));
+  }
+  // four voxels from word address `al`, byte shift `sh`; the byte permutes
+  // build 2^23 + voxel directly as a float (exact), one subtraction each
+  __device__ __forceinline__ void row_al(uint32_t al, uint32_t sh, float v[4]) const {
+    if (sizeof(VT) == 1) {
+      const uint32_t w = __byte_perm(lds32(al), lds32(al + 4), 0x3210u + sh * 0x1111u);
+      v[0] = __int_as_float(__byte_perm(w, 0x4B00u, 0x5440u)) - 8388608.0f;
+      v[1] = __int_as_float(__byte_perm(w, 0x4B00u, 0x5441u)) - 8388608.0f;
+      v[2] = __int_as_float(__byte_perm(w, 0x4B00u, 0x5442u)) - 8388608.0f;
+      v[3] = __int_as_float(__byte_perm(w, 0x4B00u, 0x5443u)) - 8388608.0f;
+    } else {
+      const uint32_t w0 = lds32(al), w1 = lds32(al + 4), w2 = lds32(al + 8);
+      const uint32_t r0 = __funnelshift_r(w0, w1, sh * 8), r1 = __funnelshift_r(w1, w2, sh * 8);
+      v[0] = __int_as_float(__byte_perm(r0, 0x4B00u, 0x5410u)) - 8388608.0f;
+      v[1] = __int_as_float(__byte_perm(r0, 0x4B00u, 0x5432u)) - 8388608.0f;
+      v[2] = __int_as_float(__byte_perm(r1, 0x4B00u, 0x5410u)) - 8388608.0f;
+      v[3] = __int_as_float(__byte_perm(r1, 0x4B00u, 0x5432u)) - 8388608.0f;
+    }
   }
   __device__ __forceinline__ void row4(int x, int y, int z, float v[4]) const {
-    const uint32_t e = elem(x, y, z);
-    if (sizeof(VT) == 1) {
-      const uint32_t a = base + e;
-      const uint32_t w0 = lds32(a & ~3u), w1 = lds32((a & ~3u) + 4);
-      const uint32_t sh = a & 3u;
-      const uint32_t w = __byte_perm(w0, w1, sh | ((sh + 1) << 4) | ((sh + 2) << 8) | ((sh + 3) << 12));
-      v[0] = u8f(__byte_perm(w, 0, 0x4440));
-      v[1] = u8f(__byte_perm(w, 0, 0x4441));
-      v[2] = u8f(__byte_perm(w, 0, 0x4442));
-      v[3] = u8f(__byte_perm(w, 0, 0x4443));
-    } else {
-      const uint32_t a = base + 2 * e;
-      const uint2 q01 = lds64(a & ~7u), q23 = lds64((a & ~7u) + 8);
-      const uint32_t s = a & 7u;
-      const bool hi = s >= 4;
-      const uint32_t lo = hi ? q01.y : q01.x, mid = hi ? q23.x : q01.y, top = hi ? q23.y : q23.x;
-      const uint32_t sh = (s & 3u) * 8;
-      const uint32_t r0 = __funnelshift_r(lo, mid, sh), r1 = __funnelshift_r(mid, top, sh);
-      v[0] = __int_as_float(0x4B000000u | (r0 & 0xFFFFu)) - 8388608.0f;
-      v[1] = __int_as_float(0x4B000000u | (r0 >> 16)) - 8388608.0f;
-      v[2] = __int_as_float(0x4B000000u | (r1 & 0xFFFFu)) - 8388608.0f;
-      v[3] = __int_as_float(0x4B000000u | (r1 >> 16)) - 8388608.0f;
-    }
+    const Stencil h = stencil(x, y, z);
+    row_al(h.al, h.sh, v);
   }
   __device__ __forceinline__ float voxel(int x, int y, int z) const {
-    const uint32_t e = elem(x, y, z);
-    if (sizeof(VT) == 1) {
-      const uint32_t a = base + e;
-      return u8f(__byte_perm(lds32(a & ~3u), 0, 0x4440 | (a & 3u)));
-    }
-    const uint32_t a = base + 2 * e;
-    const uint32_t w = lds32(a & ~3u);
-    return __int_as_float(0x4B000000u | ((a & 2u) ? (w >> 16) : (w & 0xFFFFu))) - 8388608.0f;
+    const uint32_t off = boff(x, y, z);
+    const uint32_t w = lds32(base + (off & ~3u));
+    if (sizeof(VT) == 1) return __int_as_float(__byte_perm(w, 0x4B00u, 0x5440u | (off & 3u))) - 8388608.0f;
+    return __int_as_float(__byte_perm(w, 0x4B00u, (off & 2u) ? 0x5432u : 0x5410u)) - 8388608.0f;
+  }
+  // byte distance between stencil rows (b, c) and (0, 0)
+  __device__ __forceinline__ uint32_t row_step(int b, int c) const {
+    return (uint32_t)((c * by + b) * bx) * (uint32_t)sizeof(VT);
+  }
+  __device__ __forceinline__ void srow(const Stencil &h, int b, int c, float v[4]) const {
+    row_al(h.al + row_step(b, c), h.sh, v);
   }
 };
 
@@ -211,10 +232,10 @@ struct BoxGeom {
 // Separable contraction of the 4x4x4 stencil whose low corner is at global
 // voxel (x0, y0, z0), with value weights w* and (when GRAD) slope weights d*.
 template <typename Src, bool GRAD>
-__device__ __forceinline__ float contract(const Src &src, int x0, int y0, int z0,
-                                          const float wx[4], const float wy[4], const float wz[4],
-                                          const float dx[4], const float dy[4], const float dz[4],
-                                          float g[3]) {
+__device__ __forceinline__ float contract_h(const Src &src, const typename Src::Stencil &h,
+                                            const float wx[4], const float wy[4], const float wz[4],
+                                            const float dx[4], const float dy[4], const float dz[4],
+                                            float g[3]) {
   float val = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
   for (int c = 0; c < 4; c++) {
@@ -222,7 +243,7 @@ __device__ __forceinline__ float contract(const Src &src, int x0, int y0, int z0
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       float v[4];
-      src.row4(x0, y0 + b, z0 + c, v);
+      src.srow(h, b, c, v);
       const float r = wx[0] * v[0] + wx[1] * v[1] + wx[2] * v[2] + wx[3] * v[3];
       s += wy[b] * r;
       if (GRAD) {
@@ -244,6 +265,14 @@ __device__ __forceinline__ float contract(const Src &src, int x0, int y0, int z0
     g[2] = gz;
   }
   return val;
+}
+
+template <typename Src, bool GRAD>
+__device__ __forceinline__ float contract(const Src &src, int x0, int y0, int z0,
+                                          const float wx[4], const float wy[4], const float wz[4],
+                                          const float dx[4], const float dy[4], const float dz[4],
+                                          float g[3]) {
+  return contract_h<Src, GRAD>(src, src.stencil(x0, y0, z0), wx, wy, wz, dx, dy, dz, g);
 }
 
 // Face cells (rare): A A A - B B B + C C C, out of line to keep the hot

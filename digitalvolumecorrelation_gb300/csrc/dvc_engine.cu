@@ -439,7 +439,8 @@ EncodeTiledFn encode_tiled_fn() {
 // Staging box for a cluster of C CTAs: per CTA rank, the extent of its share
 // of the stable sample offsets, plus stencil, rounding and warp margins; x
 // rounded so every copy starts and spans whole 16-byte units.
-void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int rs[9], int out[3]) {
+void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int rs[9], bool odd,
+                int out[3]) {
   double emax[3] = {0.0, 0.0, 0.0};
   for (int r = 0; r < C; r++) {
     const int lo = rs[r], hi = rs[r + 1];
@@ -453,7 +454,12 @@ void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int r
   }
   const int al = 16 / esize;
   for (int d = 0; d < 3; d++) out[d] = (int)ceil(emax[d] + 2.0 * reach) + 6;
-  out[0] = ((out[0] + al - 1 + al - 1) / al) * al;
+  // rows of an odd number of 16-byte units: consecutive rows then start in
+  // all eight 16-byte bank groups, so the gathers of nearby samples spread
+  // over the 32 shared-memory banks (an even count uses half of them)
+  int units = (out[0] + al - 1 + al - 1) / al;
+  if (odd && units % 2 == 0) units++;
+  out[0] = units * al;
 }
 
 int dispatch_launch(int bpv, int it, SearchArgs &a, const CUtensorMap &tm, size_t smem, int grid,
@@ -575,7 +581,18 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   // correlate region of its samples in shared memory (TMA) when the volume's
   // layout allows it and the box fits.
   const int esize = p.bytes_per_voxel;
-  const size_t kDynBudget = 190 * 1024;
+  // dynamic shared memory: what a block may opt into, less the kernel's
+  // static CtaState and a little slack
+  static int optin[64] = {0};
+  {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(DVC_E_ARG, "device index out of range");
+    if (!optin[dev]) CUDA_TRY(cudaDeviceGetAttribute(&optin[dev], cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  }
+  int dev_now = 0;
+  CUDA_TRY(cudaGetDevice(&dev_now));
+  const size_t kDynBudget = (size_t)optin[dev_now] - sizeof(CtaState) - 1024;
   const bool tma_layout = encode_tiled_fn() != nullptr &&
                           ((size_t)p.vol_wide * esize) % 16 == 0 &&
                           ((size_t)p.vol_wide * p.vol_high * esize) % 16 == 0 &&
@@ -601,9 +618,13 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
         const int k = (int)((double)p.disp_max / p.basin_radius);
         reach = k * ((double)p.disp_max / k);
       }
-      stage_dims(e, C, esize, reach, rs, stage);
+      // odd row pitch (in 16-byte units) when it fits, else the plain one
+      for (int odd = 1; odd >= 0; odd--) {
+        stage_dims(e, C, esize, reach, rs, odd != 0, stage);
+        stage_bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;
+        if (stage_bytes + state_bytes(cap) <= kDynBudget) break;
+      }
       if (stage[0] > 256 || stage[1] > 256 || stage[2] > 256) staged = false;
-      stage_bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;
       if (staged && stage_bytes + state_bytes(cap) > kDynBudget) staged = false;
     }
     const size_t need = (staged ? stage_bytes : 0) + state_bytes(cap);
@@ -692,6 +713,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
     const double displ_max = p.disp_max;
     a.num_inc = (int)(displ_max / p.basin_radius);
     a.inc = displ_max / a.num_inc;
+    a.inc_int = (a.inc == std::floor(a.inc) && a.inc <= 64.0 && !getenv("DVC_GENERAL_GRID")) ? (int)a.inc : 0;
   }
   a.sphere_rel = e->d_sphere;
   a.n_points = n_points;
@@ -717,6 +739,11 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   for (int d = 0; d < 3; d++) a.stage[d] = stage[d];
   a.stage_bytes = (int)stage_bytes;
   for (int r = 0; r < 9; r++) a.rank_start[r] = rs[r];
+  if (getenv("DVC_VERBOSE"))
+    fprintf(stderr, "dvc search: %d points, cluster %d, grid %d CTAs, staged %d (box %d x %d x %d), "
+            "dynamic smem %zu of %zu, samples/CTA <= %d, grid step %s\n", n_process, C, grid, (int)staged,
+            stage[0], stage[1], stage[2], smem_dyn, kDynBudget, cap,
+            a.inc_int ? "integral" : (a.do_grid ? "general" : "none"));
   e->last_cluster = C;
   e->last_grid = grid;
   e->last_staged = staged;
@@ -886,6 +913,28 @@ int dvc_gpu_last_counters(dvc_engine *e, long long out[3]) {
   CUDA_TRY(cudaDeviceSynchronize());
   CUDA_TRY(cudaMemcpy(c, (char *)e->ws + e->counters_off, sizeof c, cudaMemcpyDeviceToHost));
   for (int k = 0; k < 3; k++) out[k] = (long long)c[k];
+  return DVC_OK;
+}
+
+int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]) {
+  if (!e || !out) return set_error(DVC_E_ARG, "null argument");
+  for (int k = 0; k < DVC_N_PHASES; k++) out[k] = 0;
+  if (!e->ws) return DVC_OK;
+  static_assert(DVC_N_PHASES == kPhases, "phase count");
+  unsigned long long c[DVC_N_PHASES];
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(c, (char *)e->ws + e->counters_off + 4 * sizeof(unsigned long long), sizeof c,
+                      cudaMemcpyDeviceToHost));
+  for (int k = 0; k < DVC_N_PHASES; k++) out[k] = (long long)c[k];
+  if (getenv("DVC_VERBOSE")) {
+    unsigned long long slow = 0, fp64 = 0;
+    CUDA_TRY(cudaMemcpy(&slow, (char *)e->ws + e->counters_off + 3 * sizeof(unsigned long long),
+                        sizeof slow, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(&fp64, (char *)e->ws + e->counters_off + 14 * sizeof(unsigned long long),
+                        sizeof fp64, cudaMemcpyDeviceToHost));
+    fprintf(stderr, "dvc search: %llu integral-grid evaluations took the general path, "
+            "%llu Gauss-Newton systems used the FP64 factorisation\n", slow, fp64);
+  }
   return DVC_OK;
 }
 

@@ -51,6 +51,7 @@ struct SearchArgs {
   double nom_mn[3], nom_mx[3], nom_cen[3];  // nominal interpolation box (Search::Search)
   int bext[3];                              // its integer extents
   int do_grid, num_inc;
+  int inc_int;  // the grid step when it is a whole number of voxels, else 0
   double inc;
   double rigid[3];
   const double *sphere_rel;  // n_sub*3 uniform offsets (sphere)
@@ -62,7 +63,11 @@ struct SearchArgs {
   double *objmin, *params;
   int *gn_iters;
   int *work_counter, *done, *error_flag;
-  unsigned long long *counters;  // [0] evaluations, [1] GN iterations, [2] undefined evals
+  unsigned long long *counters;  // [0] evaluations, [1] GN iterations, [2] undefined evals,
+                                 // [3] sample evaluations of the integral grid that took the
+                                 // general path, [4 + k] SM cycles of phase k summed over
+                                 // CTAs (PhaseClock), [14] Gauss-Newton systems solved by
+                                 // the FP64 factorisation
   int local_cap;                 // per-CTA sample capacity of the dynamic arrays
   const int *cube_order;         // cube samples in space-filling order (natural index)
   // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
@@ -118,7 +123,7 @@ struct CtaState {
   float wred[kWarps][2 * 8];
   double wredd[kWarps][8];
   double A[kMaxDof * kMaxDof], b[kMaxDof], x[kMaxDof], v[kMaxDof], diag[kMaxDof], vv;
-  double ut[kMaxDof], jte[kMaxDof], scal[4];
+  double ut[kMaxDof], jte[kMaxDof], scal[6];
   int perm[kMaxDof];
 };
 
@@ -366,34 +371,47 @@ __device__ void warp_matrices(const double *x, int ndof, CtaState &S) {
     return;
   }
   S.use_rot = 1;
-  const double phi = x[3], the = x[4], psi = x[5];
-  const double cf = cos(phi), sf = sin(phi), ct = cos(the), st = sin(the), cp = cos(psi), sp = sin(psi);
-  const double R[9] = {ct * cf, ct * sf, -st,
-                       sp * st * cf - cp * sf, sp * st * sf + cp * cf, ct * sp,
-                       cp * st * cf + sp * sf, cp * st * sf - sp * cf, ct * cp};
-  const double dR[3][9] = {
-      {-ct * sf, ct * cf, 0.0, -sp * st * sf - cp * cf, sp * st * cf - cp * sf, 0.0,
-       -cp * st * sf + sp * cf, cp * st * cf + sp * sf, 0.0},
+  // FP32: the matrices are consumed in FP32 by the sample positions. Cosines
+  // enter M = (I+S)R - I through cos(a) - 1 = -2 sin^2(a/2), so M keeps its
+  // full relative accuracy for small angles.
+  float sf, cf, st, ct, sp, cp;
+  sincosf((float)x[3], &sf, &cf);
+  sincosf((float)x[4], &st, &ct);
+  sincosf((float)x[5], &sp, &cp);
+  const float s2 = sinf(0.5f * (float)x[3]), t2 = sinf(0.5f * (float)x[4]),
+              p2 = sinf(0.5f * (float)x[5]);
+  const float hf = -2.f * s2 * s2, ht = -2.f * t2 * t2, hp = -2.f * p2 * p2;  // cos - 1
+  const float R[9] = {ct * cf, ct * sf, -st,
+                      sp * st * cf - cp * sf, sp * st * sf + cp * cf, ct * sp,
+                      cp * st * cf + sp * sf, cp * st * sf - sp * cf, ct * cp};
+  // R - I with the diagonal formed from the cos - 1 terms
+  float Rm[9] = {ht * cf + hf, R[1], R[2],
+                 R[3], sp * st * sf + hp * cf + hf, R[5],
+                 R[6], R[7], ht * cp + hp};
+  const float dR[3][9] = {
+      {-ct * sf, ct * cf, 0.f, -sp * st * sf - cp * cf, sp * st * cf - cp * sf, 0.f,
+       -cp * st * sf + sp * cf, cp * st * cf + sp * sf, 0.f},
       {-st * cf, -st * sf, -ct, sp * ct * cf, sp * ct * sf, -st * sp, cp * ct * cf, cp * ct * sf,
        -st * cp},
-      {0.0, 0.0, 0.0, cp * st * cf + sp * sf, cp * st * sf - sp * cf, ct * cp,
+      {0.f, 0.f, 0.f, cp * st * cf + sp * sf, cp * st * sf - sp * cf, ct * cp,
        -sp * st * cf + cp * sf, -sp * st * sf - cp * cf, -ct * sp}};
-  double IS[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  float Sm[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if (ndof > 6) {
-    IS[0] += x[6]; IS[1] += x[9]; IS[2] += x[11];
-    IS[3] += x[9]; IS[4] += x[7]; IS[5] += x[10];
-    IS[6] += x[11]; IS[7] += x[10]; IS[8] += x[8];
+    Sm[0] = (float)x[6]; Sm[1] = (float)x[9]; Sm[2] = (float)x[11];
+    Sm[3] = (float)x[9]; Sm[4] = (float)x[7]; Sm[5] = (float)x[10];
+    Sm[6] = (float)x[11]; Sm[7] = (float)x[10]; Sm[8] = (float)x[8];
   }
   for (int r = 0; r < 3; r++)
     for (int c = 0; c < 3; c++) {
-      double m = 0.0;
-      for (int k = 0; k < 3; k++) m += IS[r * 3 + k] * R[k * 3 + c];
-      S.M[r * 3 + c] = (float)(m - (r == c ? 1.0 : 0.0));
-      S.R[r * 3 + c] = (float)R[r * 3 + c];
+      // M = (R - I) + S R ; N_q = (I + S) dR_q
+      float m = Rm[r * 3 + c];
+      for (int k = 0; k < 3; k++) m += Sm[r * 3 + k] * R[k * 3 + c];
+      S.M[r * 3 + c] = m;
+      S.R[r * 3 + c] = R[r * 3 + c];
       for (int q = 0; q < 3; q++) {
-        double s = 0.0;
-        for (int k = 0; k < 3; k++) s += IS[r * 3 + k] * dR[q][k * 3 + c];
-        S.N[q * 9 + r * 3 + c] = (float)s;
+        float s = dR[q][r * 3 + c];
+        for (int k = 0; k < 3; k++) s += Sm[r * 3 + k] * dR[q][k * 3 + c];
+        S.N[q * 9 + r * 3 + c] = s;
       }
     }
 }
@@ -483,6 +501,172 @@ __device__ void warp_qr_solve(CtaState &S, int n) {
     for (int k = 0; k < n; k++) S.x[S.perm[k]] = y[k];
   }
   __syncwarp();
+}
+
+// The same solve with little FP64 work: each FP64 instruction occupies the
+// SM's narrow FP64 pipe for a whole warp, so the serial FP64 factorisation
+// costs tens of thousands of cycles per Gauss-Newton iteration. Here the
+// Jacobi-scaled system D A D y = D b (D = diag(A)^-1/2) is factored by
+// pivoted Householder QR in FP32 on one warp (lane j holds column j), and
+// three solves with FP64 residuals r = b - A x (iterative refinement) bring
+// x to FP64 accuracy. A factor with |R_kk| < 1e-3 |R_00| (an ill-conditioned
+// or rank-deficient system) returns false and the caller uses the FP64
+// factorisation above, which also decides the numerical rank. Scratch: S.red,
+// free once A and b are assembled.
+__device__ bool warp_solve_mixed(CtaState &S, int n) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int M = kMaxDof;
+  const int lane = threadIdx.x & 31;
+  float *sR = reinterpret_cast<float *>(S.red);  // [M][M] upper triangle of R
+  float *sV = sR + M * M;                         // [M][M] reflector of step k in row k
+  float *sBeta = sV + M * M;                      // [16]
+  float *sRinv = sBeta + 16;                      // [16] 1 / R_kk
+  float *sD = sRinv + 16;                         // [16] scaling
+  float *sZ = sD + 16;                            // [16] scaled residual
+  float *sXi = sZ + 16;                           // [16] correction, original order
+  float *sAf = sXi + 16;                          // [M * M] A in FP32
+  double *sX = reinterpret_cast<double *>(sAf + M * M);  // [M] current x
+  for (int e = lane; e < n * n; e += 32) sAf[e] = (float)S.A[e];
+  __syncwarp();
+  if (lane < n) {
+    const float ajj = sAf[lane * n + lane];
+    sD[lane] = ajj > 0.f ? rsqrtf(ajj) : 1.f;
+  }
+  __syncwarp();
+  float a[M];
+  const float dj = lane < n ? sD[lane] : 0.f;
+#pragma unroll
+  for (int i = 0; i < M; i++) a[i] = (lane < n && i < n) ? sAf[i * n + lane] * sD[i] * dj : 0.f;
+  int col = lane;
+  float r00 = 0.f;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < M; k++) {
+    if (k >= n) break;
+    float s = -1.f;
+    if (lane >= k && lane < n) {
+      s = 0.f;
+#pragma unroll
+      for (int i = k; i < M; i++)
+        if (i < n) s = fmaf(a[i], a[i], s);
+    }
+    float best = s;
+    int pc = lane;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const float ob = __shfl_xor_sync(FULL, best, o);
+      const int oi = __shfl_xor_sync(FULL, pc, o);
+      if (ob > best || (ob == best && oi < pc)) {
+        best = ob;
+        pc = oi;
+      }
+    }
+    if (pc != k) {
+      const int src = lane == k ? pc : (lane == pc ? k : lane);
+#pragma unroll
+      for (int i = 0; i < M; i++) a[i] = __shfl_sync(FULL, a[i], src);
+      col = __shfl_sync(FULL, col, src);
+    }
+    const float nrm = sqrtf(best);
+    if (k == 0) r00 = nrm;
+    if (!(nrm > 1e-3f * r00)) {  // also NaN
+      ok = false;
+      break;
+    }
+    float v[M];
+#pragma unroll
+    for (int i = 0; i < M; i++) v[i] = i >= k ? __shfl_sync(FULL, a[i], k) : 0.f;
+    const float xk = v[k];
+    const float alpha = xk > 0.f ? -nrm : nrm;
+    const float beta = 1.f / (nrm * (nrm + fabsf(xk)));  // 2 / v'v
+    v[k] = xk - alpha;
+    if (lane > k && lane < n) {
+      float t = 0.f;
+#pragma unroll
+      for (int i = k; i < M; i++)
+        if (i < n) t = fmaf(v[i], a[i], t);
+      t *= beta;
+#pragma unroll
+      for (int i = k; i < M; i++)
+        if (i < n) a[i] = fmaf(-t, v[i], a[i]);
+    }
+    if (lane == k) {
+      a[k] = alpha;
+#pragma unroll
+      for (int i = k + 1; i < M; i++) a[i] = 0.f;
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int i = k; i < M; i++)
+        if (i < n) sV[k * M + i] = v[i];
+      sBeta[k] = beta;
+    }
+  }
+  if (!__all_sync(FULL, ok)) return false;
+  if (lane < n) {
+#pragma unroll
+    for (int i = 0; i < M; i++)
+      if (i <= lane) sR[i * M + lane] = a[i];
+    S.perm[lane] = col;
+  }
+  __syncwarp();
+  if (lane < n) sRinv[lane] = 1.f / sR[lane * M + lane];
+  __syncwarp();
+  double xi = 0.0;  // lane i: x_i
+  for (int pass = 0; pass < 3; pass++) {
+    if (lane < n) {
+      double r = S.b[lane];
+      if (pass > 0)
+        for (int j = 0; j < n; j++) r = fma(-S.A[lane * n + j], sX[j], r);
+      sZ[lane] = (float)r * sD[lane];
+    }
+    __syncwarp();
+    // every lane forms the same solution: z <- Q'z, then R y = z
+    float z[M], y[M];
+#pragma unroll
+    for (int i = 0; i < M; i++) z[i] = i < n ? sZ[i] : 0.f;
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      if (k < n) {
+        float t = 0.f;
+#pragma unroll
+        for (int i = k; i < M; i++)
+          if (i < n) t = fmaf(sV[k * M + i], z[i], t);
+        t *= sBeta[k];
+#pragma unroll
+        for (int i = k; i < M; i++)
+          if (i < n) z[i] = fmaf(-t, sV[k * M + i], z[i]);
+      }
+    }
+#pragma unroll
+    for (int k = M - 1; k >= 0; k--) {
+      y[k] = 0.f;
+      if (k < n) {
+        float t = z[k];
+#pragma unroll
+        for (int j = k + 1; j < M; j++)
+          if (j < n) t = fmaf(-sR[k * M + j], y[j], t);
+        y[k] = t * sRinv[k];
+      }
+    }
+    float yl = 0.f;
+#pragma unroll
+    for (int k = 0; k < M; k++)
+      if (k == lane) yl = y[k];
+    if (lane < n) {
+      const int c = S.perm[lane];
+      sXi[c] = yl * sD[c];
+    }
+    __syncwarp();
+    if (lane < n) {
+      xi += (double)sXi[lane];
+      sX[lane] = xi;
+    }
+    __syncwarp();
+  }
+  if (lane < n) S.x[lane] = xi;
+  __syncwarp();
+  return true;
 }
 
 // ----------------------------------------------------------- TMA staging ---
@@ -587,6 +771,130 @@ __device__ __forceinline__ float eval_sample_t(const SSrc<VT> &ss, const int r0[
   return interp_at<GSrc<VT>, IT, GRAD>(gs, lo, kind, f, g);
 }
 
+// ---------------------------------------------------- integral-step grid ---
+// When the grid step inc is a whole number of voxels, every translation of
+// the coarse grid (trgrid_global, Core/Search.cpp:934-1043) moves a sample by
+// whole voxels: its cell fraction, and so its interpolation weights, are those
+// of the centre translation. The CTA's threads are split into groups of
+// `span` lanes; lane j of a group evaluates translation j of the chunk for the
+// group's share of the samples. A warp thus gathers the stencils of ONE
+// sample under 32 translations: addresses a fixed lattice apart, spread over
+// the shared-memory banks (lanes that read the same word share it), where
+// 32 different samples would hit the banks at random. Sample data reaches
+// the lanes by shuffles, 32 samples per round. A (sample, translation) whose
+// stencil leaves the staged box, or lies on a face cell or the undefined last
+// plane, takes the general evaluation in its lane. Sums: FP32 over a round,
+// compensated across rounds, then over the groups.
+template <typename VT, int IT>
+__device__ __forceinline__ void grid_chunk_lanes(
+    const SearchArgs &a, CtaState &S, const int *s_ip, const float *s_fp, const float *s_r, int nl,
+    float *s_scr, const SSrc<VT> &ss, const int r0[3], const int B[3], const GSrc<VT> &gsc,
+    const BoxGeom &G, int o0, int nch, int side, int k, int parity, bool sad,
+    unsigned long long &n_undef, unsigned long long &n_slow) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int esize = (int)sizeof(VT);
+  const int tid = threadIdx.x, lane = tid & 31;
+  int span = 32;
+  while (span < nch) span *= 2;  // nch <= kGridChunk = 128
+  const int groups = kThreads / span;
+  const int j = tid % span, grp = tid / span;
+  const bool live = j < nch;
+  // this lane's translation
+  const int step = a.inc_int;
+  const int o = o0 + min(j, nch - 1);
+  const int dc[3] = {(o % side - k) * step, ((o / side) % side - k) * step, (o / (side * side) - k) * step};
+  const int dbytes = ((dc[2] * B[1] + dc[1]) * B[0] + dc[0]) * esize;
+  const int n3[3] = {G.bx, G.by, G.bz};
+  const int o3[3] = {G.ox, G.oy, G.oz};
+  int lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    lo[d] = max(IT == 2 ? 1 : 0, r0[d] + 1 - o3[d]) - dc[d];
+    hi[d] = min(min(n3[d] - (IT == 2 ? 3 : 2), a.bext[d] - 1), r0[d] + B[d] - 3 - o3[d]) - dc[d];
+  }
+  int iu0[3];
+  float fu0[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), iu0[d], fu0[d]);
+  // this group's samples
+  const int s_lo = (int)(((long long)nl * grp) / groups), s_hi = (int)(((long long)nl * (grp + 1)) / groups);
+  KSum k0, k1, k2;
+  for (int ib = s_lo; ib < s_hi; ib += 32) {
+    const int nb = min(32, s_hi - ib);
+    // lane l prepares sample ib + l
+    int c[3] = {0, 0, 0};
+    float f[3] = {0.f, 0.f, 0.f}, qv = 0.f;
+    uint32_t off0 = 0;
+    if (lane < nb) {
+      sample_pos(s_ip, s_fp, ib + lane, S, iu0, fu0, false, c, f);
+      qv = s_r[ib + lane];
+      off0 = ss.boff(o3[0] + c[0] - 1, o3[1] + c[1] - 1, o3[2] + c[2] - 1);
+    }
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+    for (int m = 0; m < nb; m++) {
+      const int cx = __shfl_sync(FULL, c[0], m), cy = __shfl_sync(FULL, c[1], m),
+                cz = __shfl_sync(FULL, c[2], m);
+      float fm[3] = {__shfl_sync(FULL, f[0], m), __shfl_sync(FULL, f[1], m), __shfl_sync(FULL, f[2], m)};
+      const float q = __shfl_sync(FULL, qv, m);
+      const uint32_t ob = __shfl_sync(FULL, off0, m);
+      if (!live) continue;
+      float t;
+      if (cx >= lo[0] && cx <= hi[0] && cy >= lo[1] && cy <= hi[1] && cz >= lo[2] && cz <= hi[2]) {
+        float w[3][4], dw[4];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          if (IT == 2) {
+            cr_weights(fm[d], w[d], dw);
+          } else {
+            w[d][0] = 0.f; w[d][1] = 1.f - fm[d]; w[d][2] = fm[d]; w[d][3] = 0.f;
+          }
+        }
+        float g[3];
+        t = contract_h<SSrc<VT>, false>(ss, ss.stencil_at(ob + (uint32_t)dbytes), w[0], w[1], w[2],
+                                        w[0], w[1], w[2], g);
+      } else {
+        int cc[3] = {cx + dc[0], cy + dc[1], cz + dc[2]};
+        clamp_cell(cc, a.bext);
+        float g[3];
+        bool und;
+        t = eval_sample_t<VT, IT, false, true>(ss, r0, B, gsc, G, cc, fm, g, und);
+        n_undef += und;
+        n_slow++;
+      }
+      t -= S.shift;
+      if (sad) {
+        p0 += fabsf(t - q);
+      } else {
+        p0 += t;
+        p1 += t * t;
+        p2 += t * q;
+      }
+    }
+    k0.add(p0);
+    k1.add(p1);
+    k2.add(p2);
+  }
+  // groups -> chunk sums (FP32 pairs in scratch, FP64 in cbuf)
+  float *part = s_scr;  // [groups][span][6]
+  {
+    float *my = part + ((size_t)grp * span + j) * 6;
+    my[0] = k0.s; my[1] = -k0.c;
+    my[2] = k1.s; my[3] = -k1.c;
+    my[4] = k2.s; my[5] = -k2.c;
+  }
+  __syncthreads();
+  if (tid < nch) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int g2 = 0; g2 < groups; g2++) {
+      const float *pp = part + ((size_t)g2 * span + tid) * 6;
+#pragma unroll
+      for (int m = 0; m < 3; m++) acc[m] += (double)pp[2 * m] + (double)pp[2 * m + 1];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; m++) S.cbuf[parity][3 * tid + m] = acc[m];
+  }
+}
+
 // Keep the staged region when it covers positions [pmn, pmx] with the stencil
 // margin; otherwise stage a new one into the same buffer. One thread; returns
 // 1 when a copy was started (the block then waits for it).
@@ -612,8 +920,9 @@ __device__ __forceinline__ int restage(const SearchArgs &a, CtaState &S, const d
 // Range check of the moving sample cloud against the correlate act box
 // (BoundBox::contains in tri_cub_Lek, Core/Interpolate.cpp:474-481).
 // Translation only: the exact FP64 bbox (stable bbox + u, affine_to). With a
-// rotation/strain: min/max of the warped samples over the cluster. Also
-// leaves this CTA's own position range in pmn/pmx (local voxel frame).
+// rotation/strain: min/max of the warped samples over the cluster. Thread 0
+// also gets this CTA's own position range in pmn/pmx (global voxel frame),
+// which only it uses (staging).
 __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float *s_fp, int nl,
                                             CtaState &S, bool rot, double pmn[3], double pmx[3]) {
   if (!rot) {
@@ -623,44 +932,107 @@ __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float
         const double bmn = __dadd_rn(S.sbmn[d], S.par[d]);
         const double bmx = __dadd_rn(S.sbmx[d], S.par[d]);
         if (!(bmn >= S.H.act_cor.mn[d]) || !(bmx <= S.H.act_cor.mx[d])) fail = 1;
+        pmn[d] = S.lbmn[d] + S.par[d];
+        pmx[d] = S.lbmx[d] + S.par[d];
       }
       S.fail = fail;
-    }
-    for (int d = 0; d < 3; d++) {
-      pmn[d] = S.lbmn[d] + S.par[d];
-      pmx[d] = S.lbmx[d] + S.par[d];
     }
     __syncthreads();
     return;
   }
-  double m[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};  // mins, then -maxs
+  // Exact min / max of the warped positions c + f without FP64 per sample:
+  // the key (c + 2^20) << 32 | bits(f) orders exactly as c + f does, f being
+  // a non-negative float below 1. Mins of the keys and of their complements
+  // (the maxima) over the CTA, then over the cluster.
+  constexpr unsigned FULL = 0xffffffffu;
+  unsigned long long v[6] = {~0ull, ~0ull, ~0ull, ~0ull, ~0ull, ~0ull};
   for (int i = threadIdx.x; i < nl; i += kThreads) {
     int c[3];
     float f[3];
     sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, true, c, f);
+#pragma unroll
     for (int d = 0; d < 3; d++) {
-      const double x = (double)c[d] + (double)f[d];
-      m[d] = fmin(m[d], x);
-      m[3 + d] = fmin(m[3 + d], -x);
+      const unsigned long long key =
+          ((unsigned long long)(unsigned)(c[d] + (1 << 20)) << 32) | __float_as_uint(f[d]);
+      v[d] = min(v[d], key);
+      v[3 + d] = min(v[3 + d], ~key);
     }
   }
-  cta_min<6>(m, S, S.cbuf[cl.parity]);
-  for (int d = 0; d < 3; d++) {
-    pmn[d] = (double)S.H.o_cor[d] + S.cbuf[cl.parity][d];
-    pmx[d] = (double)S.H.o_cor[d] - S.cbuf[cl.parity][3 + d];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; k++)
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v[k] = min(v[k], __shfl_xor_sync(FULL, v[k], o));
+  unsigned long long *wk = reinterpret_cast<unsigned long long *>(S.red);  // [kWarps][6]
+  unsigned long long *out = wk + 64;                                       // [6]
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 6; k++) wk[warp * 6 + k] = v[k];
+  __syncthreads();
+  unsigned long long *cb = reinterpret_cast<unsigned long long *>(S.cbuf[cl.parity]);
+  if (threadIdx.x < 6) {
+    unsigned long long m = ~0ull;
+    for (int w = 0; w < kWarps; w++) m = min(m, wk[w * 6 + threadIdx.x]);
+    cb[threadIdx.x] = m;
   }
-  cluster_reduce(cl, S, 6, 6);
+  cl.g.sync();
+  if (threadIdx.x < 6) {
+    unsigned long long m = ~0ull;
+    for (unsigned r = 0; r < cl.size; r++) {
+      const unsigned long long *rem = cl.g.map_shared_rank(cb, r);
+      m = min(m, rem[threadIdx.x]);
+    }
+    out[threadIdx.x] = m;
+  }
+  cl.parity ^= 1;
+  __syncthreads();
   if (threadIdx.x == 0) {
+    // this CTA's own range (staging) and the cluster's (range check)
     int fail = 0;
     for (int d = 0; d < 3; d++) {
-      const double bmn = (double)S.H.o_cor[d] + S.red[d];
-      const double bmx = (double)S.H.o_cor[d] - S.red[3 + d];
+      const unsigned long long kl = cb[d], kh = ~cb[3 + d];
+      const unsigned long long gl = out[d], gh = ~out[3 + d];
+      const double o = (double)S.H.o_cor[d];
+      pmn[d] = o + ((double)((int)(kl >> 32) - (1 << 20)) + (double)__uint_as_float((unsigned)kl));
+      pmx[d] = o + ((double)((int)(kh >> 32) - (1 << 20)) + (double)__uint_as_float((unsigned)kh));
+      const double bmn = o + ((double)((int)(gl >> 32) - (1 << 20)) + (double)__uint_as_float((unsigned)gl));
+      const double bmx = o + ((double)((int)(gh >> 32) - (1 << 20)) + (double)__uint_as_float((unsigned)gh));
       if (!(bmn >= S.H.act_cor.mn[d]) || !(bmx <= S.H.act_cor.mx[d])) fail = 1;
     }
     S.fail = fail;
   }
   __syncthreads();
 }
+
+// Time per phase of the point loop, kept by thread 0 of each CTA from the SM
+// clock and added to the call's counters once at exit: 0 take work and seed
+// (dependency waits included), 1 reference subvolume and samples, 2 coarse
+// grid, 3 Gauss-Newton entry and exit, 4 final objective and result; inside
+// each Gauss-Newton iteration 5 warp matrices, 6 range check and staging,
+// 7 sample evaluation and G'G chunks, 8 block and cluster reductions,
+// 9 objective, assembly, solve and update.
+constexpr int kPhases = 10;
+struct PhaseClock {
+  long long acc[kPhases] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  long long prev = 0;
+  int cur = 0;
+  __device__ __forceinline__ void start() {
+    if (threadIdx.x == 0) prev = clock64();
+  }
+  __device__ __forceinline__ void to(int ph) {
+    if (threadIdx.x == 0) {
+      const long long t = clock64();
+      acc[cur] += t - prev;
+      prev = t;
+      cur = ph;
+    }
+  }
+  __device__ __forceinline__ void flush(unsigned long long *counters) {
+    to(0);
+    if (threadIdx.x == 0)
+      for (int k = 0; k < kPhases; k++) atomicAdd(counters + 4 + k, (unsigned long long)acc[k]);
+  }
+};
 
 // ================================================================ kernel ===
 template <typename VT, int IT>
@@ -705,6 +1077,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int ndof = a.ndof;
   const int fcn = a.objfcn;
   const bool sad = (fcn == DVC_SAD);
+  const double inv_nsub = 1.0 / (double)nsub;
+  PhaseClock pc;
+  pc.start();
 
   for (;;) {
     // --------------------------------------------- take work (leader) ---
@@ -742,8 +1117,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     gsc.checked = S.H.chk_cor;
     const BoxGeom Gref{S.H.o_ref[0], S.H.o_ref[1], S.H.o_ref[2], a.bext[0], a.bext[1], a.bext[2]};
     const BoxGeom Gcor{S.H.o_cor[0], S.H.o_cor[1], S.H.o_cor[2], a.bext[0], a.bext[1], a.bext[2]};
-    unsigned long long n_eval = 0, n_undef = 0;
+    unsigned long long n_eval = 0, n_undef = 0, n_slow = 0;
     if (tid == 0) S.fail = 0;
+    pc.to(1);
 
     // ------------------------------- reference subvolume and samples ---
     // (search_pt_setup: the stable cloud interpolated in the reference box)
@@ -833,6 +1209,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     n_eval += 1;
     __syncthreads();
 
+    pc.to(2);
     // ---------------------------------------------------- grid search ---
     // trgrid_global (Core/Search.cpp:934-1043): (2k+1)^3 translations; the
     // first strictly smaller objective in z, y, x loop order wins. Any
@@ -892,6 +1269,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
         __syncthreads();
+        if (IT != 0 && rg.ok && a.inc_int > 0) {
+          grid_chunk_lanes<VT, IT>(a, S, s_ip, s_fp, s_r, nl, s_G, ss, rg.r0, B, gsc, Gcor, o0, nch,
+                                   side, k, cl.parity, sad, n_undef, n_slow);
+        } else {
         // each warp evaluates whole translations: its lanes cover this CTA's
         // samples, one shuffle reduction per translation, no block barrier
 #pragma unroll 1
@@ -935,6 +1316,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             S.cbuf[cl.parity][3 * j + 2] = (double)p2 + (double)l2;
           }
         }
+        }
         cluster_reduce(cl, S, 3 * nch, 0);
         if (tid < nch)
           S.objv[tid] = sad ? S.red[3 * tid]
@@ -960,6 +1342,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       S.reg[0].ok = 0;
     }
 
+    pc.to(3);
     // ------------------------------------------------- Gauss-Newton ---
     // min_Lev_Mar(start, 1e-6, 0.01) (Core/Search.cpp:194-246): undamped
     // Gauss-Newton on the residual vector of the objective, at most 20
@@ -994,6 +1377,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         eb = kMaxDof + (my_e - ntri) / ndof;
       }
       for (int it = 0; it < 20; it++) {
+        pc.to(5);
         if (tid == 0) {
           warp_matrices(S.par, ndof, S);
           for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), S.iu[d], S.fu[d]);
@@ -1001,6 +1385,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncthreads();
         const bool rot = S.use_rot;
         double pmn[3], pmx[3];
+        pc.to(6);
         range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
         if (S.fail) goto point_done;
         if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, &tmap, buf_addr[0], bar_addr[0], stage_tx);
@@ -1011,6 +1396,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           phase[0] ^= 1u;
         }
         const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
+        pc.to(7);
 
         KSum v[4];
         float gg = 0.f;
@@ -1079,6 +1465,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           __syncthreads();
         }
         n_eval += 1;
+        pc.to(8);
         cta_sum_comp<4>(v, S, S.cbuf[cl.parity]);
         // entry parts -> entries (FP64) after the 4 value sums
         {
@@ -1092,6 +1479,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
         cluster_reduce(cl, S, 4 + nent, 0);
+        pc.to(9);
         // assemble J'J and -J'e (FP64)
         if (tid == 0) {
           const double S1 = S.red[0], S2 = S.red[1], S3 = S.red[2], S4 = S.red[3];
@@ -1117,6 +1505,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           S.scal[1] = sc;
           S.scal[2] = (fcn == DVC_NSSD) ? T : sig;
           S.scal[3] = (fcn == DVC_NSSD) ? S3 / T : rho;
+          S.scal[4] = 1.0 / S.scal[2];
           S.obj = obj;
           int stop = 0;
           if (it > 0) {
@@ -1134,7 +1523,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         {
           const double *GG = &S.red[4];
           const double *Gs = GG + ntri, *Gt = GG + ntri + ndof, *Gq = GG + ntri + 2 * ndof;
-          const double mean = S.scal[0], sc = S.scal[1], den = S.scal[2], rr = S.scal[3];
+          const double mean = S.scal[0], sc = S.scal[1], rden = S.scal[4], rr = S.scal[3];
           const bool sub_mean = (fcn == DVC_ZSSD || fcn == DVC_ZNSSD);
           const bool sub_t = (fcn == DVC_NSSD || fcn == DVC_ZNSSD);
           if (tid < ndof) {
@@ -1145,11 +1534,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             } else if (fcn == DVC_ZSSD) {
               jte = Gt[p] - mean * Gs[p] - Gq[p];
             } else if (fcn == DVC_NSSD) {
-              ut = Gt[p] / den;
-              jte = (rr * ut - Gq[p]) / den;
+              ut = Gt[p] * rden;
+              jte = (rr * ut - Gq[p]) * rden;
             } else {
-              ut = (Gt[p] - mean * Gs[p]) / den;
-              jte = (rr * ut - Gq[p]) / den;
+              ut = (Gt[p] - mean * Gs[p]) * rden;
+              jte = (rr * ut - Gq[p]) * rden;
             }
             S.ut[p] = ut;
             S.b[p] = -jte;
@@ -1163,7 +1552,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             const int c2 = r + e;
             double v2 = GG[tid];
-            if (sub_mean) v2 -= Gs[r] * Gs[c2] / (double)nsub;
+            if (sub_mean) v2 -= Gs[r] * Gs[c2] * inv_nsub;
             if (sub_t) v2 -= S.ut[r] * S.ut[c2];
             v2 *= sc;
             S.A[r * ndof + c2] = v2;
@@ -1172,21 +1561,24 @@ __global__ void __launch_bounds__(kThreads, 1)
           __syncthreads();
         }
         if (tid < 32) {
-          warp_qr_solve(S, ndof);
-          if (tid == 0) {
-            for (int p = 0; p < ndof; p++) S.par[p] += S.x[p];
-            for (int d = 0; d < 3; d++) S.upd[d] = S.x[d];
-            S.obj_old = S.obj;
+          if (!warp_solve_mixed(S, ndof)) {
+            warp_qr_solve(S, ndof);
+            if (tid == 0) atomicAdd(a.counters + 14, 1ull);
           }
+          if (tid < ndof) S.par[tid] += S.x[tid];
+          if (tid < 3) S.upd[tid] = S.x[tid];
+          if (tid == 0) S.obj_old = S.obj;
         }
         __syncthreads();
       }
+      pc.to(3);
       if (cl.rank == 0 && tid == 0) {
         if (a.gn_iters) a.gn_iters[S.H.n] = it_done;
         atomicAdd(a.counters + 1, (unsigned long long)it_done);
       }
     }
 
+    pc.to(4);
     // ------------------------------------------------ final objective ---
     // obj_val_at(par_min) (Core/Search.cpp:187): explicit residuals over the
     // stored values, the reference's own two-pass formulation
@@ -1288,10 +1680,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       unsigned long long u = n_undef;
       for (int o = 16; o; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
       if ((tid & 31) == 0 && u) atomicAdd(a.counters + 2, u);
+      unsigned long long w = n_slow;
+      for (int o = 16; o; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+      if ((tid & 31) == 0 && w) atomicAdd(a.counters + 3, w);
     }
     // the leader may overwrite its header only after every CTA copied it
     cl.g.sync();
+    pc.to(0);
   }
+  pc.flush(a.counters);
   // no CTA leaves while another may still read its shared memory
   cl.g.sync();
 }

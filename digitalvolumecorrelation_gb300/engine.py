@@ -57,6 +57,7 @@ def load(path: str | None = None):
                                          C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.dvc_gpu_last_counters.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+    L.dvc_gpu_last_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
     L.dvc_gpu_interpolate.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
     L.dvc_gpu_objective.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp]
     L.dvc_gpu_strain.argtypes = [C.c_int, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double,
@@ -153,6 +154,14 @@ class Engine:
         of the most recent search on this engine."""
         out = (C.c_longlong * 3)()
         _check(_lib.dvc_gpu_last_counters(self._h, out))
+        return tuple(int(v) for v in out)
+
+    def last_phase_cycles(self):
+        """SM cycles of the most recent search per phase, summed over CTAs:
+        (seed, setup, grid, gn_entry_exit, final, gn_warp, gn_range_stage,
+        gn_eval, gn_reduce, gn_solve)."""
+        out = (C.c_longlong * 10)()
+        _check(_lib.dvc_gpu_last_phase_cycles(self._h, out))
         return tuple(int(v) for v in out)
 
     def interpolate(self, volume, center, pts, interp_type=2):

@@ -178,6 +178,18 @@ int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *po
    percentages in its .stat file (Core/dvc.cpp:322-338). */
 int dvc_gpu_last_counters(dvc_engine *e, long long out[3]);
 
+/* Diagnostics of the same call: SM clock cycles spent per phase of the
+   per-point loop, summed over every CTA of the launch: out[0] taking work and
+   forming the start estimate (neighbour waits included), out[1] reference
+   subvolume and sample setup, out[2] coarse translation grid, out[3]
+   Gauss-Newton set-up and exit, out[4] final objective and result; per
+   Gauss-Newton iteration out[5] warp matrices, out[6] range check and
+   staging, out[7] sample evaluation, out[8] reductions, out[9] assembly,
+   solve and update. No counterpart in the reference (it has no per-phase
+   timing). */
+#define DVC_N_PHASES 10
+int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]);
+
 /* ---- function-level entry points ----------------------------------------
  * Interpolate one volume (0 = reference, 1 = correlate) at n points, with the
  * interpolation box of this engine's search (Search::Search est_box_nom,

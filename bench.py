@@ -39,7 +39,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=2, choices=[1, 2])
-    ap.add_argument("--cpu-sample", type=int, default=12, help="points timed on the CPU")
+    ap.add_argument("--cpu-sample", type=int, default=384,
+                    help="points of the workload timed on the CPU (cpu_baseline leg)")
+    ap.add_argument("--ref-sample", type=int, default=64,
+                    help="points per step of the reference arm (--impl reference)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -302,40 +305,45 @@ def run_reference(args, rank, world):
     # a CPU rendering of the same workload definition is out of reach for
     # 1 GiB volumes in a few minutes, so each step processes points of a
     # cropped copy: the sample points' own neighbourhoods rendered on the CPU
-    n_sample = max(1, args.cpu_sample // 2)
+    n_sample = max(1, args.ref_sample)
     idx = np.linspace(0, len(W.points) - 1, n_sample).astype(int)
     crop = 2 * int(np.ceil(p.subvol_size / 2.0 * max(p.subvol_aspect[:]) + p.disp_max + 8))
     from oracle.oracle import Oracle
     O = Oracle()
     threads = os.cpu_count() or 1
+    from digitalvolumecorrelation_gb300.abi import make_params
+    crops = []  # rendered once, outside the timed calls
+    for i in idx:
+        pt = W.points[i]
+        lo = np.floor(pt - crop / 2).astype(int)
+        shape = (crop, crop, crop)
+        b = W.blobs.copy()
+        b[:, :3] -= lo
+        keep = np.all((b[:, :3] > -12) & (b[:, :3] < crop + 12), axis=1)
+        dt_ = np.uint8 if W.bytes_per_voxel == 1 else np.uint16
+        ref = synth.render(shape, b[keep], None, W.noise_sigma, 1000 + i, dtype=dt_)
+
+        class Shift:
+            kind = 0
+
+            def __init__(self, lo):
+                self.lo = lo
+
+            def u(self, X):
+                return W.deform.u(np.asarray(X) + self.lo)
+
+            def inverse(self, x):
+                return W.deform.inverse(np.asarray(x) + self.lo) - self.lo
+
+        cor = synth.render(shape, b[keep], Shift(lo), W.noise_sigma, 2000 + i, dtype=dt_)
+        pc = make_params(shape, bytes_per_voxel=W.bytes_per_voxel, **W.params_kw)
+        crops.append((pc, ref, cor, (pt - lo)[None, :], W.truth(pt[None, :])))
     rates = []
     for s in range(args.warmup + args.steps):
         t_total = 0.0
-        for i in idx:
-            pt = W.points[i]
-            lo = np.floor(pt - crop / 2).astype(int)
-            shape = (crop, crop, crop)
-            b = W.blobs.copy()
-            b[:, :3] -= lo
-            keep = np.all((b[:, :3] > -12) & (b[:, :3] < crop + 12), axis=1)
-            dt_ = np.uint8 if W.bytes_per_voxel == 1 else np.uint16
-            ref = synth.render(shape, b[keep], None, W.noise_sigma, 1000 + i, dtype=dt_)
-
-            class Shift:
-                kind = 0
-
-                def u(self, X):
-                    return W.deform.u(np.asarray(X) + lo)
-
-                def inverse(self, x):
-                    return W.deform.inverse(np.asarray(x) + lo) - lo
-
-            cor = synth.render(shape, b[keep], Shift(), W.noise_sigma, 2000 + i, dtype=dt_)
-            from digitalvolumecorrelation_gb300.abi import make_params
-            pc = make_params(shape, bytes_per_voxel=W.bytes_per_voxel, **W.params_kw)
-            local = (pt - lo)[None, :]
+        for pc, ref, cor, local, seed in crops:
             t0 = time.perf_counter()
-            O.process(pc, ref, cor, local, seed_mode=1, seeds=W.truth(pt[None, :]), n_threads=threads)
+            O.process(pc, ref, cor, local, seed_mode=1, seeds=seed, n_threads=threads)
             t_total += time.perf_counter() - t0
         if s >= args.warmup:
             rates.append(len(idx) / t_total)

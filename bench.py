@@ -43,6 +43,10 @@ def parse():
                     help="points of the workload timed on the CPU (cpu_baseline leg)")
     ap.add_argument("--ref-sample", type=int, default=64,
                     help="points per step of the reference arm (--impl reference)")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one search launch on a small case for profilers: the bench "
+                         "configuration's subvolumes and search on 384^3 uint16 volumes, "
+                         "216 points with given seeds")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -140,11 +144,46 @@ def cpu_leg(W, p, ref_np, cor_np, pts, seeds, gpu_params, sample, threads):
     return len(idx) / dt, dt, err, r
 
 
+def profile_case():
+    """One launch of the search kernel on a case small enough for ncu's
+    replays: the bench configuration's sphere subvolumes (41 voxels, 4000
+    samples), znssd, tricubic, 12 degrees of freedom, disp_max 6 / basin 3, on
+    384^3 uint16 volumes (2 x 113 MB, more than L2), 216 points, seeds within
+    half a voxel of the truth."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine, synth, workloads
+    shape = (384, 384, 384)
+    pts = synth.grid_points((6, 6, 6), 24.0, (192.0, 192.0, 192.0))
+    kw = dict(subvol_geom="sphere", subvol_size=41, subvol_npts=4000, obj_function="znssd",
+              interp_type="tricubic", num_srch_dof=12, disp_max=6, basin_radius=3.0)
+    b = synth.blobs(shape, int(np.prod(shape) // 1000), sigma=(1.5, 3.0), amp=(2000.0, 60000.0), seed=2)
+    W = workloads.Workload("profile_384cube_u16_216pts_sphere41_dof12", shape, 2, kw, pts,
+                           synth.Sinusoid(A=3.0, L=400.0), b, 150.0, 201, 202)
+    p = W.params()
+    n = len(pts)
+    ref_d, cor_d = W.render_device()
+    E = engine.Engine(p, ref_dev=ref_d, cor_dev=cor_d)
+    dev = torch.device("cuda")
+    seeds = W.truth() + np.random.default_rng(0).normal(0, 0.5, (n, 3))
+    t = lambda a, dt=None: torch.as_tensor(a, dtype=dt, device=dev)
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+    ob = torch.empty(n, dtype=torch.float64, device=dev)
+    pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
+    it = torch.empty(n, dtype=torch.int32, device=dev)
+    E.process_device(n, t(W.points), t(np.arange(n), torch.int32), n, None, 0, 1, t(seeds), st, ob,
+                     pa, it, stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": W.name, "good": int((st == 0).sum().item()), "points": n,
+                      "evaluations": E.last_counters()[0], "sample_evals": E.last_counters()[0] * 4000}))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.profile_case:
+        return profile_case()
 
     import torch
     from digitalvolumecorrelation_gb300 import engine, workloads

@@ -83,7 +83,10 @@ def build_host(force=False):
     headers = [os.path.join(HOST, h) for h in os.listdir(HOST) if h.endswith(".h")]
     headers.append(os.path.join(ROOT, "include", "dvc_gpu.h"))
     cxx = os.environ.get("CXX", "g++")
-    flags = ["-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", HOST]
+    # -ffp-contract=off: the neighbour distances are formed as in the
+    # reference, without fused multiply-adds (ties must compare the same)
+    flags = ["-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+             "-I", HOST]
     link = ["-L", LIB_DIR, "-ldvcgpu", "-Wl,-rpath,$ORIGIN/../lib"]
     jobs = []
     for prog in ("dvc", "strain"):

@@ -12,7 +12,10 @@ on small seeded synthetic volumes, what the reference computes:
     reference's order with its neighbour seeding, sphere test seed 1),
   * strain-program CSV outputs (the reference `strain` executable),
   * the 10-nearest-neighbour table of the reference's own DataCloud test
-    (Core/tests/test_DataCloud.cpp:129-139 over Core/tests/grid_input.roi).
+    (Core/tests/test_DataCloud.cpp:129-139 over Core/tests/grid_input.roi),
+  * end-to-end runs of the reference's `dvc` and `strain` programs
+    (input file, point cloud and raw volumes -> .disp, .stat, .sort.csv,
+    strain CSVs); `--dvc-runs` regenerates only these.
 The GPU machine has no reference sources, so its tests read these files.
 """
 from __future__ import annotations
@@ -33,6 +36,9 @@ sys.path.insert(0, ROOT)
 from digitalvolumecorrelation_gb300 import synth  # noqa: E402
 from digitalvolumecorrelation_gb300.abi import make_params  # noqa: E402
 from oracle.oracle import REF_SO, Oracle, Reference, build_reference  # noqa: E402
+
+sys.path.insert(0, HERE)
+from dvc_inputs import write_dvc_inputs  # noqa: E402
 
 REF_DIR = os.environ.get("DVC_REFERENCE_DIR", "/root/reference")
 SHAPE = (40, 40, 40)
@@ -134,7 +140,76 @@ def strain_golden(tmp):
     return out
 
 
+# end-to-end runs of the reference's own `dvc` and `strain` programs
+# (cube subvolumes: the reference's normal runs seed sphere samples from the
+# clock). Inputs are written from the fixture volumes at test time.
+DVC_RUNS = [
+    dict(name="u8_nostart", volumes="A", header=0, endian="little",
+         roi_extra="n\tx\ty\tz\n# comment line\n7.5 1 2 3\n",
+         keys=[("subvol_geom", "cube"), ("subvol_size", "11"), ("subvol_npts", "300"),
+               ("subvol_thresh", "off"), ("disp_max", "3"), ("num_srch_dof", "6"),
+               ("obj_function", "znssd"), ("interp_type", "tricubic"), ("basin_radius", "1.5"),
+               ("num_points_to_process", "0")]),
+    dict(name="u16be_start", volumes="B", header=32, endian="big", roi_extra="",
+         keys=[("subvol_geom", "cube"), ("subvol_size", "11"), ("subvol_npts", "343"),
+               ("subvol_thresh", "off"), ("disp_max", "3"), ("num_srch_dof", "12"),
+               ("obj_function", "zssd"), ("interp_type", "tricubic"), ("basin_radius", "0.0"),
+               ("rigid_trans", "0.5 -0.3 0.2"), ("starting_point", "21.0 19.0 20.0"),
+               ("num_points_to_process", "20")]),
+]
+
+
+def dvc_runs_golden(tmp, vols):
+    rng = np.random.default_rng(9)
+    pts = synth.grid_points((3, 3, 3), 5.0, (20.0, 20.0, 20.0)) + rng.uniform(-0.4, 0.4, (27, 3)).round(2)
+    labels = rng.permutation(np.arange(101, 128))
+    runs = []
+    for case in DVC_RUNS:
+        d = os.path.join(tmp, case["name"])
+        os.makedirs(d, exist_ok=True)
+        write_dvc_inputs(d, case, vols, pts, labels)
+        r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "dvc"), "dvc_in"], cwd=d,
+                           capture_output=True, text=True, env=dict(os.environ, OMP_NUM_THREADS="4"))
+        assert r.returncode == 0, r.stdout + r.stderr
+        out = dict(case=case, points=pts.tolist(), labels=labels.tolist(),
+                   disp=open(os.path.join(d, "result.disp")).read(),
+                   sort_csv=open(os.path.join(d, "points.roi.sort.csv")).read(),
+                   stat=open(os.path.join(d, "result.stat")).read())
+        if case["name"] == "u8_nostart":
+            # the reference `strain` on this run's outputs: with the sort file
+            # and without it (strain then writes its own)
+            st = {}
+            for tag, extra in (("sorted", ["points.roi.sort.csv"]), ("unsorted", [])):
+                sd = os.path.join(d, tag)
+                os.makedirs(sd, exist_ok=True)
+                open(os.path.join(sd, "result.disp"), "w").write(out["disp"])
+                if extra:
+                    open(os.path.join(sd, extra[0]), "w").write(out["sort_csv"])
+                args = ["-sw", "12", "-A"] if tag == "sorted" else ["-t", "0.5", "-r", "-E"]
+                r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "strain"), "result.disp"]
+                                   + extra + args, cwd=sd, capture_output=True, text=True)
+                assert r.returncode == 0, r.stdout + r.stderr
+                st[tag] = dict(args=extra + args,
+                               files={f: open(os.path.join(sd, f)).read() for f in sorted(os.listdir(sd))
+                                      if f.endswith(".csv") and f != "points.roi.sort.csv"})
+            out["strain"] = st
+        runs.append(out)
+    return runs
+
+
 def main():
+    if "--dvc-runs" in sys.argv:  # only the end-to-end program runs
+        if not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "dvc")):
+            if build_reference() is None:
+                raise SystemExit("reference sources not available")
+        z = np.load(os.path.join(HERE, "reference_hotpath.npz"))
+        vols = {k: (z[f"vol_{k}_ref"], z[f"vol_{k}_cor"]) for k in ("A", "B")}
+        with tempfile.TemporaryDirectory() as tmp:
+            runs = dvc_runs_golden(tmp, vols)
+        with open(os.path.join(HERE, "dvc_runs.json"), "w") as f:
+            json.dump(runs, f, indent=1)
+        print("dvc_runs.json written")
+        return
     if not os.path.exists(REF_SO):
         if build_reference() is None:
             raise SystemExit("reference sources not available")
@@ -195,6 +270,10 @@ def main():
                         **{f"{c}_{k}": np.asarray(v) for c, d in st.items() for k, v in d.items()})
     with open(os.path.join(HERE, "datacloud_knn.json"), "w") as f:
         json.dump(datacloud_golden(), f, indent=1)
+    with tempfile.TemporaryDirectory() as tmp:
+        runs = dvc_runs_golden(tmp, vols)
+    with open(os.path.join(HERE, "dvc_runs.json"), "w") as f:
+        json.dump(runs, f, indent=1)
     print("golden fixtures written to", HERE)
 
 

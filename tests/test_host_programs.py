@@ -1,0 +1,195 @@
+"""The drop-in `dvc` and `strain` programs against the reference's own.
+
+tests/golden/dvc_runs.json holds end-to-end runs of the reference's `dvc`
+and `strain` executables (built from its sources by oracle/build_ref.sh and
+run by tests/golden/make_golden.py): the input files, point clouds, volume
+layouts and the .disp / .stat / .sort.csv / strain CSV outputs. The same
+inputs are written here and the drop-in programs run on them.
+
+CPU tests: the input-file checks and their messages, the command line
+modes, and the outputs written before the GPU is used (`<roi>.sort.csv`,
+the .stat input echo, strain's own sort file). GPU tests: whole runs.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, GOLDEN)
+from dvc_inputs import write_dvc_inputs  # noqa: E402
+
+RUNS = json.load(open(os.path.join(GOLDEN, "dvc_runs.json")))
+
+
+@pytest.fixture(scope="session")
+def vols():
+    z = np.load(os.path.join(GOLDEN, "reference_hotpath.npz"))
+    return {k: (z[f"vol_{k}_ref"], z[f"vol_{k}_cor"]) for k in ("A", "B")}
+
+
+@pytest.fixture(scope="session")
+def bins():
+    from digitalvolumecorrelation_gb300 import build
+    build.build_library()
+    build.build_host()
+    return os.path.join(build.BIN_DIR, "dvc"), os.path.join(build.BIN_DIR, "strain")
+
+
+def run(cmd, cwd):
+    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr  # the reference's programs return 0, also on errors
+    return r.stdout
+
+
+def setup_run(tmp_path, run_, vols):
+    d = str(tmp_path)
+    write_dvc_inputs(d, run_["case"], vols, np.array(run_["points"]), run_["labels"])
+    return d
+
+
+def echo_part(stat):
+    """The .stat input echo and point-cloud block (before the version line)."""
+    return stat.split("running under dvc code version:")[0]
+
+
+# ------------------------------------------------------------------ CPU ---
+@pytest.mark.parametrize("k", range(len(RUNS)), ids=[r["case"]["name"] for r in RUNS])
+def test_dvc_sort_file_and_echo(bins, vols, tmp_path, k):
+    """<roi>.sort.csv and the .stat echo equal the reference's byte for byte
+    (std::sort neighbour order with ties; starting_point handling)."""
+    g = RUNS[k]
+    d = setup_run(tmp_path, g, vols)
+    run([bins[0], "dvc_in"], d)
+    assert open(os.path.join(d, "points.roi.sort.csv")).read() == g["sort_csv"]
+    assert echo_part(open(os.path.join(d, "result.stat")).read()) == echo_part(g["stat"])
+
+
+BAD_INPUTS = [
+    # (edit of the valid input file, message expected)
+    (lambda t: t.replace("interp_type\ttricubic", "# interp_type\ttricubic"),
+     "keyword 'interp_type' not found"),
+    (lambda t: t.replace("num_srch_dof\t6", "num_srch_dof\t7"), "num_srch_dof contains an invalid parameter"),
+    (lambda t: t.replace("ref.raw\t", "nope.raw\t"), "cannot find file: nope.raw"),
+    (lambda t: t.replace("vol_wide\t40", "vol_wide\t41"), "does not match the volume description"),
+    (lambda t: t + "subvol_aspect\t0.05 1 1\n", "subvol_aspect contains an invalid parameter"),
+    (lambda t: t.replace("basin_radius\t1.5", "basin_radius\t3.5"), "basin_radius contains an invalid parameter"),
+    (lambda t: t.replace("num_points_to_process\t0", ""), "keyword 'num_points_to_process' not found"),
+    (lambda t: t.replace("subvol_thresh\toff", "subvol_thresh\ton"), "keyword 'gray_thresh_min' not found"),
+    (lambda t: t.replace("vol_bit_depth\t8", "vol_bit_depth\t16"), "keyword 'vol_endian' not found"),
+    (lambda t: t + "rigid_trans\t0 50 0\n", "rigid_trans contains an invalid parameter"),
+]
+
+
+@pytest.mark.parametrize("edit,msg", BAD_INPUTS, ids=[m for _, m in BAD_INPUTS])
+def test_dvc_input_errors(bins, vols, tmp_path, edit, msg):
+    d = setup_run(tmp_path, RUNS[0], vols)
+    p = os.path.join(d, "dvc_in")
+    text = edit(open(p).read())
+    with open(p, "w") as f:
+        f.write(text)
+    out = run([bins[0], "dvc_in"], d)
+    assert msg in out, out
+    assert not os.path.exists(os.path.join(d, "result.disp"))
+
+
+def test_dvc_roi_rules_and_modes(bins, vols, tmp_path):
+    d = setup_run(tmp_path, RUNS[0], vols)
+    # a point cloud with no valid line aborts
+    open(os.path.join(d, "points.roi"), "w").write("n x y z\n1.5 2 3 4\n7 8 9\n")
+    out = run([bins[0], "dvc_in"], d)
+    assert "No points were read" in out
+    assert "Options:" in run([bins[0]], d)
+    run([bins[0], "example"], d)
+    ex = open(os.path.join(d, "dvc_in_example")).read()
+    from digitalvolumecorrelation_gb300 import abi  # noqa: F401  (package importable)
+    for kw in ("reference_filename", "vol_endian", "subvol_aspect", "num_points_to_process",
+               "starting_point", "basin_radius", "min_vol_fract"):
+        assert kw in ex
+    run([bins[0], "manual"], d)
+    assert os.path.getsize(os.path.join(d, "dvc_manual")) > 500
+    assert "version" in run([bins[0], "version"], d)
+    assert "Cannot find input file" in run([bins[0], "missing_file"], d)
+
+
+def test_strain_cli_before_gpu(bins, tmp_path):
+    d = str(tmp_path)
+    assert "strain needs a .disp file" in run([bins[1]], d)
+    assert "cannot find .disp file" in run([bins[1], "none.disp"], d)
+    open(os.path.join(d, "bad.disp"), "w").write("1\t2\t3\t4\t0\t0.1\t0\t0\t0\n")
+    assert "lacks the header" in run([bins[1], "bad.disp"], d)
+    # without a sort file, strain writes its own first (std::sort order with ties)
+    g = RUNS[0]["strain"]["unsorted"]
+    open(os.path.join(d, "result.disp"), "w").write(RUNS[0]["disp"])
+    out = run([bins[1], "result.disp", "-q"] + g["args"], d)
+    assert "unused flag -q found, ignored" in out
+    assert open(os.path.join(d, "result.sort.csv")).read() == g["files"]["result.sort.csv"]
+
+
+# ------------------------------------------------------------------ GPU ---
+def parse_disp(text):
+    rows = [l.split("\t") for l in text.strip().split("\n")[1:]]
+    return rows
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("k", range(len(RUNS)), ids=[r["case"]["name"] for r in RUNS])
+def test_dvc_run_matches_reference(bins, vols, tmp_path, k):
+    """Whole `dvc` run: rows in the reference's processing order, the same
+    labels, coordinates and statuses; u, v, w within 1e-3 voxel; objmin
+    within 2e-5 relative (both printed with six significant digits)."""
+    g = RUNS[k]
+    d = setup_run(tmp_path, g, vols)
+    run([bins[0], "dvc_in"], d)
+    ours = parse_disp(open(os.path.join(d, "result.disp")).read())
+    ref = parse_disp(g["disp"])
+    assert len(ours) == len(ref)
+    for a, b in zip(ours, ref):
+        assert a[:5] == b[:5], (a, b)  # n x y z status, as text
+        oa, ob = float(a[5]), float(b[5])
+        assert abs(oa - ob) <= 2e-5 * max(abs(ob), 1e-12) + 1e-12, (a, b)
+        du = np.abs(np.array(a[6:9], float) - np.array(b[6:9], float))
+        assert du.max() <= 1e-3, (a, b)
+    stat = open(os.path.join(d, "result.stat")).read()
+    for line in g["stat"].splitlines():
+        if line.startswith(("number ", "Point Cloud", "\tbounding")) or " points processed in " in line:
+            key = line.split(" in ")[0] if " points processed in " in line else line
+            assert key in stat, line
+
+
+def close6(a, b, scale):
+    """Two values each printed with six significant digits agree to within
+    one unit of the sixth digit, or 1e-9 of the column's scale."""
+    mag = np.maximum(np.abs(a), np.abs(b))
+    unit = 10.0 ** (np.floor(np.log10(np.where(mag == 0, 1e-300, mag))) - 5)
+    return np.abs(a - b) <= np.maximum(1.01 * unit, 1e-9 * scale)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", ["sorted", "unsorted"])
+def test_strain_run_matches_reference(bins, tmp_path, tag):
+    g = RUNS[0]["strain"][tag]
+    d = str(tmp_path)
+    open(os.path.join(d, "result.disp"), "w").write(RUNS[0]["disp"])
+    if tag == "sorted":
+        open(os.path.join(d, "points.roi.sort.csv"), "w").write(RUNS[0]["sort_csv"])
+    run([bins[1], "result.disp"] + g["args"], d)
+    for name, text in g["files"].items():
+        mine = open(os.path.join(d, name)).read()
+        if name.endswith(".sort.csv"):
+            assert mine == text
+            continue
+        a = np.array([[float(v) for v in l.split(",")] for l in mine.strip().split("\n")[1:]])
+        b = np.array([[float(v) for v in l.split(",")] for l in text.strip().split("\n")[1:]])
+        assert mine.split("\n")[0] == text.split("\n")[0]
+        assert a.shape == b.shape
+        assert np.array_equal(a[:, [0, 7]], b[:, [0, 7]]), name  # labels, points in window
+        scale = np.abs(b).max(axis=0)
+        ok = close6(a, b, scale[None, :])
+        assert ok.all(), (name, np.argwhere(~ok)[:5], a[~ok][:5], b[~ok][:5])

@@ -31,6 +31,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ROI points/s at <=0.01-voxel error vs FP64 oracle (plain GPU method)"
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one search launch, per workload
+# (profiles/search_kernel_config2_bench.md)
+MEASURED_TRAFFIC = {"config2_1024cube_u16_60800pts_sphere41_dof12": 57.36e9 + 56.28e6}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -251,6 +255,9 @@ def main():
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak_tf = peaks.get("bf16_tflops", 1900.0)
     achieved = sample_evals * flop_per_sample / (ms / 1e3) / 1e12
+    # DRAM bytes of one search launch of this workload, from the one-pass ncu
+    # capture summarised in profiles/search_kernel_config2_bench.md
+    traffic = MEASURED_TRAFFIC.get(W.name)
 
     # accuracy: truth and oracle sample
     truth = W.truth()
@@ -274,7 +281,8 @@ def main():
                     "median_abs_err_vs_truth_vox": float(np.median(np.abs(params[good, :3] - truth[good])))
                     if good.any() else None},
         "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak_tf,
-                     "unit": "TFLOP/s", "frac": round(achieved / peak_tf, 4), "traffic": None,
+                     "unit": "TFLOP/s", "frac": round(achieved / peak_tf, 4),
+                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram read+write)",
                      "flop_per_unit": flop_per_sample, "units_per_launch": sample_evals,
                      "note": "algorithmic FLOPs of the fused 64x64 coefficient product per "
                              "sample-evaluation; the kernel evaluates the same interpolant in "

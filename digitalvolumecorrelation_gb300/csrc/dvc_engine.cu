@@ -930,7 +930,7 @@ int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]) {
     unsigned long long slow = 0, fp64 = 0;
     CUDA_TRY(cudaMemcpy(&slow, (char *)e->ws + e->counters_off + 3 * sizeof(unsigned long long),
                         sizeof slow, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(&fp64, (char *)e->ws + e->counters_off + 14 * sizeof(unsigned long long),
+    CUDA_TRY(cudaMemcpy(&fp64, (char *)e->ws + e->counters_off + 16 * sizeof(unsigned long long),
                         sizeof fp64, cudaMemcpyDeviceToHost));
     fprintf(stderr, "dvc search: %llu integral-grid evaluations took the general path, "
             "%llu Gauss-Newton systems used the FP64 factorisation\n", slow, fp64);

@@ -66,7 +66,7 @@ struct SearchArgs {
   unsigned long long *counters;  // [0] evaluations, [1] GN iterations, [2] undefined evals,
                                  // [3] sample evaluations of the integral grid that took the
                                  // general path, [4 + k] SM cycles of phase k summed over
-                                 // CTAs (PhaseClock), [14] Gauss-Newton systems solved by
+                                 // CTAs (PhaseClock), [16] Gauss-Newton systems solved by
                                  // the FP64 factorisation
   int local_cap;                 // per-CTA sample capacity of the dynamic arrays
   const int *cube_order;         // cube samples in space-filling order (natural index)
@@ -1010,10 +1010,10 @@ __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float
 // grid, 3 Gauss-Newton entry and exit, 4 final objective and result; inside
 // each Gauss-Newton iteration 5 warp matrices, 6 range check and staging,
 // 7 sample evaluation and G'G chunks, 8 block and cluster reductions,
-// 9 objective, assembly, solve and update.
-constexpr int kPhases = 10;
+// 9 objective, assembly, solve and update, 10 G'G accumulation (inside 7).
+constexpr int kPhases = 11;
 struct PhaseClock {
-  long long acc[kPhases] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  long long acc[kPhases] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   long long prev = 0;
   int cur = 0;
   __device__ __forceinline__ void start() {
@@ -1361,20 +1361,27 @@ __global__ void __launch_bounds__(kThreads, 1)
       int it_done = 20;
       const int ntri = ndof * (ndof + 1) / 2;
       const int nent = ntri + 3 * ndof;
-      const int nparts = kThreads / nent;
-      const int my_e = tid % nent, my_part = tid / nent;
-      int ea = 0, eb = 0;
-      if (my_e < ntri) {
-        int e = my_e, r = 0;
-        while (e >= ndof - r) {
-          e -= ndof - r;
-          r++;
+      // G'G in 3x3 register tiles: row blocks of the ndof gradient
+      // components, column blocks of the components plus one block of the
+      // (1, t, q) columns; tiles on or above the diagonal. Each tile is summed
+      // by `parts` threads over interleaved samples (consecutive lanes read
+      // consecutive samples: no bank conflicts), the parts are combined at
+      // the end of the iteration.
+      const int R = ndof / 3;
+      const int ntile = R * (R + 1) / 2 + R;
+      const int parts = kThreads / ntile;
+      const int tile = tid / parts, part = tid % parts;
+      const bool gact = tile < ntile;
+      int row0 = 0, col0 = 0;
+      if (gact) {
+        int b = tile, rb = 0;
+        while (b >= R + 1 - rb) {
+          b -= R + 1 - rb;
+          rb++;
         }
-        ea = r;
-        eb = r + e;
-      } else {
-        ea = (my_e - ntri) % ndof;
-        eb = kMaxDof + (my_e - ntri) / ndof;
+        const int cb = rb + b;
+        row0 = 3 * rb;
+        col0 = cb == R ? kMaxDof : 3 * cb;
       }
       for (int it = 0; it < 20; it++) {
         pc.to(5);
@@ -1399,7 +1406,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         pc.to(7);
 
         KSum v[4];
-        float gg = 0.f;
+        float acc[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[q] = 0.f;
         for (int base = 0; base < nl; base += kThreads) {
           const int i = base + tid;
           float g[kMaxDof];
@@ -1457,25 +1466,46 @@ __global__ void __launch_bounds__(kThreads, 1)
           s_G[(kMaxDof + 1) * kThreads + tid] = t;
           s_G[(kMaxDof + 2) * kThreads + tid] = q;
           __syncthreads();
-          if (my_part < nparts) {
-            const int l0 = (my_part * kThreads) / nparts, l1 = ((my_part + 1) * kThreads) / nparts;
-            const float *ga = s_G + ea * kThreads, *gb = s_G + eb * kThreads;
-            for (int s2 = l0; s2 < l1; s2++) gg += ga[s2] * gb[s2];
+          pc.to(10);
+          if (gact) {
+            const int cnt = min(kThreads, nl - base);
+            for (int s2 = part; s2 < cnt; s2 += parts) {
+              float ga[3], gb[3];
+#pragma unroll
+              for (int q = 0; q < 3; q++) {
+                ga[q] = s_G[(row0 + q) * kThreads + s2];
+                gb[q] = s_G[(col0 + q) * kThreads + s2];
+              }
+#pragma unroll
+              for (int q = 0; q < 9; q++) acc[q] = fmaf(ga[q / 3], gb[q % 3], acc[q]);
+            }
           }
           __syncthreads();
+          pc.to(7);
         }
         n_eval += 1;
         pc.to(8);
         cta_sum_comp<4>(v, S, S.cbuf[cl.parity]);
-        // entry parts -> entries (FP64) after the 4 value sums
+        // tile parts -> entries after the 4 value sums: each (part, entry)
+        // is written by exactly one thread (the lower half of diagonal tiles
+        // is left out), then summed over the parts with TwoSum
         {
-          double *parts = S.red;  // scratch: parts of each entry
-          parts[tid] = (my_part < nparts) ? (double)gg : 0.0;
+          float *pe = s_G;  // [parts][nent], free after the last chunk
+          if (gact) {
+#pragma unroll
+            for (int q = 0; q < 9; q++) {
+              const int ra = row0 + q / 3, cb2 = col0 + q % 3;
+              int e = -1;
+              if (cb2 >= kMaxDof) e = ntri + (cb2 - kMaxDof) * ndof + ra;
+              else if (ra <= cb2) e = ra * ndof - ra * (ra - 1) / 2 + (cb2 - ra);
+              if (e >= 0) pe[part * nent + e] = acc[q];
+            }
+          }
           __syncthreads();
           if (tid < nent) {
-            double sum = 0.0;
-            for (int pp = 0; pp < nparts; pp++) sum += parts[pp * nent + tid];
-            S.cbuf[cl.parity][4 + tid] = sum;
+            float hi = 0.f, lo = 0.f;
+            for (int pp = 0; pp < parts; pp++) two_sum_merge(hi, lo, pe[pp * nent + tid], 0.f);
+            S.cbuf[cl.parity][4 + tid] = (double)hi + (double)lo;
           }
         }
         cluster_reduce(cl, S, 4 + nent, 0);
@@ -1563,7 +1593,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (tid < 32) {
           if (!warp_solve_mixed(S, ndof)) {
             warp_qr_solve(S, ndof);
-            if (tid == 0) atomicAdd(a.counters + 14, 1ull);
+            if (tid == 0) atomicAdd(a.counters + 16, 1ull);
           }
           if (tid < ndof) S.par[tid] += S.x[tid];
           if (tid < 3) S.upd[tid] = S.x[tid];

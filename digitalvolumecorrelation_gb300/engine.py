@@ -159,8 +159,8 @@ class Engine:
     def last_phase_cycles(self):
         """SM cycles of the most recent search per phase, summed over CTAs:
         (seed, setup, grid, gn_entry_exit, final, gn_warp, gn_range_stage,
-        gn_eval, gn_reduce, gn_solve)."""
-        out = (C.c_longlong * 10)()
+        gn_eval, gn_reduce, gn_solve, gn_gtg)."""
+        out = (C.c_longlong * 11)()
         _check(_lib.dvc_gpu_last_phase_cycles(self._h, out))
         return tuple(int(v) for v in out)
 

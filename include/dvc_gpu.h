@@ -185,9 +185,9 @@ int dvc_gpu_last_counters(dvc_engine *e, long long out[3]);
    Gauss-Newton set-up and exit, out[4] final objective and result; per
    Gauss-Newton iteration out[5] warp matrices, out[6] range check and
    staging, out[7] sample evaluation, out[8] reductions, out[9] assembly,
-   solve and update. No counterpart in the reference (it has no per-phase
-   timing). */
-#define DVC_N_PHASES 10
+   solve and update, out[10] the G'G accumulation of the evaluations. No
+   counterpart in the reference (it has no per-phase timing). */
+#define DVC_N_PHASES 11
 int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]);
 
 /* ---- function-level entry points ----------------------------------------

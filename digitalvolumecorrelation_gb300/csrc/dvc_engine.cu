@@ -158,6 +158,80 @@ __global__ void objective_kernel(int fcn, int n, const double *r, const double *
   }
 }
 
+// ------------------------------------------- dataflow scheduling set-up ---
+// Edge (i = order[r], m = neigh[i][j]) is a dependency of i when the reference
+// processes m before i (rank[m] < r): Search::starting_param then reads m's
+// result (Core/Search.cpp:297-356).
+__global__ void dep_count_kernel(int n_process, int n_points, int nn, const int *order,
+                                 const int *neigh, const int *rank, int *pend, int *succ_cnt) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (long long)n_process * nn) return;
+  const int r = (int)(k / nn), j = (int)(k % nn);
+  const int i = order[r];
+  if (i < 0 || i >= n_points) return;
+  const int m = neigh[(size_t)i * nn + j];
+  if (m < 0 || m >= n_points || rank[m] >= r) return;
+  atomicAdd(pend + i, 1);
+  atomicAdd(succ_cnt + m, 1);
+}
+
+__global__ void dep_fill_kernel(int n_process, int n_points, int nn, const int *order,
+                                const int *neigh, const int *rank, const int *succ_off, int *cursor,
+                                int *succ) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (long long)n_process * nn) return;
+  const int r = (int)(k / nn), j = (int)(k % nn);
+  const int i = order[r];
+  if (i < 0 || i >= n_points) return;
+  const int m = neigh[(size_t)i * nn + j];
+  if (m < 0 || m >= n_points || rank[m] >= r) return;
+  succ[succ_off[m] + atomicAdd(cursor + m, 1)] = i;
+}
+
+// exclusive prefix sum of in[0..n) into out[0..n], one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) exclusive_scan_kernel(int n, const int *in, int *out) {
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += 1024) {
+    const int v = base + t < n ? in[base + t] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    const int incl = x + (warp > 0 ? wsum[warp - 1] : 0);
+    if (base + t < n) out[base + t] = carry + incl - v;
+    __syncthreads();
+    if (t == 1023) carry += incl;
+    __syncthreads();
+  }
+  if (t == 0) out[n] = carry;
+}
+
+// points without predecessors start the ready queue
+__global__ void ready_kernel(int n_process, int n_points, const int *order, const int *pend,
+                             int *queue, int *tail) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_process) return;
+  const int i = order[r];
+  if (i < 0 || i >= n_points || pend[i] != 0) return;
+  queue[atomicAdd(tail, 1)] = i;
+}
+
 __global__ void byteswap16_kernel(uint16_t *v, size_t n) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) v[i] = (uint16_t)((v[i] >> 8) | (v[i] << 8));
@@ -661,13 +735,22 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   if (max_clusters < 1) return set_error(DVC_E_ARG, "search kernel cluster does not fit");
   const int grid = C * std::max(1, std::min(max_clusters, n_process));
 
-  // workspace: done[n], rank[n], counter/error/counters, per-CTA state
+  // workspace: done[n], rank[n], counter/error/counters; with dataflow
+  // scheduling also the predecessor counts, successor lists and ready queue
   const size_t off_done = 0;
   const size_t off_rank = off_done + (size_t)n_points * 4;
   const size_t off_ctl = (off_rank + (size_t)n_points * 4 + 255) & ~(size_t)255;
+  const bool dataflow = seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !ws_fixed &&
+                        !getenv("DVC_IN_ORDER");
+  const size_t off_pend = off_ctl + 256;
+  const size_t off_soff = off_pend + (size_t)n_points * 4;
+  const size_t off_cursor = off_soff + ((size_t)n_points + 1) * 4;
+  const size_t off_queue = off_cursor + (size_t)n_points * 4;
+  const size_t off_succ = off_queue + (size_t)n_process * 4;
+  const size_t ws_need = dataflow ? off_succ + (size_t)n_process * n_neigh * 4 : off_ctl + 256;
   char *ws = ws_fixed;
   if (!ws) {
-    rc = ensure_ws(e, off_ctl + 256);
+    rc = ensure_ws(e, ws_need);
     if (rc) return rc;
     ws = (char *)e->ws;
     e->counters_off = off_ctl + 64;
@@ -686,6 +769,23 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
     CUDA_TRY(cudaGetLastError());
   }
   if (n_process == 0) return DVC_OK;
+  if (dataflow) {
+    const int T = 256;
+    int *pend = (int *)(ws + off_pend), *soff = (int *)(ws + off_soff);
+    int *cursor = (int *)(ws + off_cursor), *queue = (int *)(ws + off_queue);
+    CUDA_TRY(cudaMemsetAsync(ws + off_pend, 0, off_queue - off_pend, st));  // pend, counts, cursor
+    CUDA_TRY(cudaMemsetAsync(queue, 0xFF, (size_t)n_process * 4, st));       // -1: slot empty
+    const long long edges = (long long)n_process * n_neigh;
+    const unsigned eg = (unsigned)((edges + T - 1) / T);
+    dep_count_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, order_dev, neigh_dev, rank, pend,
+                                       soff);
+    exclusive_scan_kernel<<<1, 1024, 0, st>>>(n_points, soff, soff);
+    dep_fill_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, order_dev, neigh_dev, rank, soff,
+                                      cursor, (int *)(ws + off_succ));
+    ready_kernel<<<(n_process + T - 1) / T, T, 0, st>>>(n_process, n_points, order_dev, pend, queue,
+                                                        (int *)(ws + off_ctl) + 2);
+    CUDA_TRY(cudaGetLastError());
+  }
 
   SearchArgs a{};
   a.ref = e->ref;
@@ -731,6 +831,14 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   a.gn_iters = gn_iters_dev;
   a.work_counter = ctl;
   a.error_flag = ctl + 1;
+  a.dataflow = dataflow ? 1 : 0;
+  if (dataflow) {
+    a.pend = (int *)(ws + off_pend);
+    a.succ_off = (const int *)(ws + off_soff);
+    a.succ = (const int *)(ws + off_succ);
+    a.queue = (int *)(ws + off_queue);
+    a.queue_tail = ctl + 2;
+  }
   a.done = done;
   a.counters = counters;
   a.local_cap = cap;

@@ -63,6 +63,15 @@ struct SearchArgs {
   double *objmin, *params;
   int *gn_iters;
   int *work_counter, *done, *error_flag;
+  // dataflow scheduling of the reference's seeding (Search::starting_param
+  // reads the neighbours processed before a point): pend[i] counts point i's
+  // unfinished predecessors; succ[succ_off[j] .. succ_off[j + 1]) lists the
+  // points that have j as a predecessor; ready points are appended to queue
+  // (queue_tail) as their last predecessor finishes and taken in queue order
+  int dataflow;
+  int *pend;
+  const int *succ_off, *succ;
+  int *queue, *queue_tail;
   unsigned long long *counters;  // [0] evaluations, [1] GN iterations, [2] undefined evals,
                                  // [3] sample evaluations of the integral grid that took the
                                  // general path, [4 + k] SM cycles of phase k summed over
@@ -295,54 +304,66 @@ __device__ __forceinline__ double objective_from_sums(int fcn, double S1, double
 
 // ---------------------------------------------------- seed and boxes ---
 // Search::starting_param (Core/Search.cpp:277-377) and the boxes of
-// search_pt_setup (Core/Search.cpp:248-275). Leader thread only.
+// search_pt_setup (Core/Search.cpp:248-275), on the leader CTA's first warp.
+// The lanes read the neighbour list (entries lane, lane + 32, ...), wait
+// (bounded) for the neighbours the reference processes before this point
+// and sum the displacements of the converged ones: per lane in list order,
+// then a fixed shuffle tree, where the reference keeps one running sum (the
+// two differ only in FP64 rounding). H.n and H.rank are set by lane 0.
 __device__ bool point_seed(const SearchArgs &a, PointHeader &H) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   const int n = H.n;
-  double sd[3];
-  if (a.seed_mode == DVC_SEED_GIVEN) {
-    for (int d = 0; d < 3; d++) sd[d] = a.seeds[(size_t)n * 3 + d];
-  } else {
-    double sx = 0.0, sy = 0.0, sz = 0.0;
-    int good = 0;
-    if (a.seed_mode == DVC_SEED_NEIGHBOURS) {
-      for (int j = 0; j < a.n_neigh; j++) {
-        const int m = a.neigh[(size_t)n * a.n_neigh + j];
-        if (m < 0 || m >= a.n_points) continue;
-        if (a.rank[m] >= H.rank) continue;  // not yet processed when the reference reaches n
-        long long polls = 0;
-        volatile int *flag = a.done + m;
-        while (*flag == 0) {
-          if (++polls > kWaitPolls) {
-            atomicExch(a.error_flag, DVC_E_TIMEOUT);
-            return false;
-          }
-          __nanosleep(128);
+  double sum[3] = {0.0, 0.0, 0.0};
+  int good = 0;
+  if (a.seed_mode == DVC_SEED_NEIGHBOURS) {
+    int fail = 0;
+    for (int j = lane; j < a.n_neigh && !fail; j += 32) {
+      const int m = a.neigh[(size_t)n * a.n_neigh + j];
+      if (m < 0 || m >= a.n_points) continue;
+      if (a.rank[m] >= H.rank) continue;  // not yet processed when the reference reaches n
+      long long polls = 0;
+      volatile int *flag = a.done + m;
+      while (*flag == 0) {
+        if (++polls > kWaitPolls) {
+          fail = 1;
+          break;
         }
-        __threadfence();
-        const volatile int *st = a.status;
-        if (st[m] == DVC_POINT_GOOD) {
-          const volatile double *pm = a.params + (size_t)m * 12;
-          sx += pm[0];
-          sy += pm[1];
-          sz += pm[2];
-          good += 1;
-        }
+        __nanosleep(128);
+      }
+      if (fail) break;
+      __threadfence();
+      const volatile int *st = a.status;
+      if (st[m] == DVC_POINT_GOOD) {
+        const volatile double *pm = a.params + (size_t)m * 12;
+        sum[0] += pm[0];
+        sum[1] += pm[1];
+        sum[2] += pm[2];
+        good += 1;
       }
     }
-    if (good != 0) {
-      sd[0] = sx / good;
-      sd[1] = sy / good;
-      sd[2] = sz / good;
-    } else {
-      for (int d = 0; d < 3; d++) sd[d] = a.rigid[d];
+    if (__any_sync(FULL, fail)) {
+      if (lane == 0) atomicExch(a.error_flag, DVC_E_TIMEOUT);
+      return false;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      for (int d = 0; d < 3; d++) sum[d] += __shfl_xor_sync(FULL, sum[d], o);
+      good += __shfl_xor_sync(FULL, good, o);
     }
   }
-  for (int d = 0; d < 3; d++) H.seed[d] = sd[d];
-  // the nominal box centred on the point (reference volume) and on
-  // point + seed (correlate volume); act box one voxel inside
-  for (int d = 0; d < 3; d++) {
+  // lanes 0..2: the seed and the boxes of one axis each: the nominal box
+  // centred on the point (reference volume) and on point + seed (correlate
+  // volume); act box one voxel inside
+  if (lane < 3) {
+    const int d = lane;
+    double sd;
+    if (a.seed_mode == DVC_SEED_GIVEN) sd = a.seeds[(size_t)n * 3 + d];
+    else if (good != 0) sd = sum[d] / good;
+    else sd = a.rigid[d];
+    H.seed[d] = sd;
     const double cref = H.pt[d];
-    const double ccor = __dadd_rn(H.pt[d], sd[d]);  // Point::move_by
+    const double ccor = __dadd_rn(H.pt[d], sd);  // Point::move_by
     const double ref_mn = __dadd_rn(a.nom_mn[d], __dsub_rn(cref, a.nom_cen[d]));
     const double cor_mn = __dadd_rn(a.nom_mn[d], __dsub_rn(ccor, a.nom_cen[d]));
     const double amn = __dadd_rn(a.nom_mn[d], 1.0), amx = __dadd_rn(a.nom_mx[d], -1.0);
@@ -353,14 +374,31 @@ __device__ bool point_seed(const SearchArgs &a, PointHeader &H) {
     H.o_ref[d] = itrunc_d(ref_mn);
     H.o_cor[d] = itrunc_d(cor_mn);
   }
-  const int vol[3] = {a.nx, a.ny, a.nz};
-  H.chk_ref = 0;
-  H.chk_cor = 0;
-  for (int d = 0; d < 3; d++) {
-    if (H.o_ref[d] - 1 < 0 || H.o_ref[d] + a.bext[d] > vol[d] - 1) H.chk_ref = 1;
-    if (H.o_cor[d] - 1 < 0 || H.o_cor[d] + a.bext[d] > vol[d] - 1) H.chk_cor = 1;
+  __syncwarp();
+  if (lane == 0) {
+    const int vol[3] = {a.nx, a.ny, a.nz};
+    H.chk_ref = 0;
+    H.chk_cor = 0;
+    for (int d = 0; d < 3; d++) {
+      if (H.o_ref[d] - 1 < 0 || H.o_ref[d] + a.bext[d] > vol[d] - 1) H.chk_ref = 1;
+      if (H.o_cor[d] - 1 < 0 || H.o_cor[d] + a.bext[d] > vol[d] - 1) H.chk_cor = 1;
+    }
   }
+  __syncwarp();
   return true;
+}
+
+// The leader CTA's first warp, after point n's result is published: one
+// predecessor fewer for every successor; those left with none become ready.
+__device__ __forceinline__ void release_successors(const SearchArgs &a, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int k = a.succ_off[n] + lane; k < a.succ_off[n + 1]; k += 32) {
+    const int sp = a.succ[k];
+    if (atomicSub(a.pend + sp, 1) == 1) {
+      const int slot = atomicAdd(a.queue_tail, 1);
+      atomicExch(a.queue + slot, sp);
+    }
+  }
 }
 
 // SearchParams::set_param_vect (Core/SearchParams.cpp:53-107) and the
@@ -1083,17 +1121,37 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   for (;;) {
     // --------------------------------------------- take work (leader) ---
-    if (cl.rank == 0 && tid == 0) {
+    // In processing order, or with dataflow scheduling the next point whose
+    // predecessors have all finished (the ready queue's next entry).
+    if (cl.rank == 0 && tid < 32) {
       PointHeader &H = S.H;
-      H.rank = atomicAdd(a.work_counter, 1);
-      H.flag = 0;
-      if (H.rank >= a.n_process) {
-        H.flag = 1;
-      } else {
-        H.n = a.order[H.rank];
-        for (int d = 0; d < 3; d++) H.pt[d] = a.pts[(size_t)H.n * 3 + d];
-        if (!point_seed(a, H)) H.flag = 2;
+      if (tid == 0) {
+        H.flag = 0;
+        const int h = atomicAdd(a.work_counter, 1);
+        if (h >= a.n_process) {
+          H.flag = 1;
+        } else if (a.dataflow) {
+          volatile int *slot = a.queue + h;
+          long long polls = 0;
+          int n;
+          while ((n = *slot) < 0 && ++polls <= kWaitPolls) __nanosleep(256);
+          if (n < 0) {
+            atomicExch(a.error_flag, DVC_E_TIMEOUT);
+            H.flag = 1;
+          } else {
+            __threadfence();
+            H.n = n;
+            H.rank = a.rank[n];
+          }
+        } else {
+          H.rank = h;
+          H.n = a.order[h];
+        }
+        if (H.flag == 0)
+          for (int d = 0; d < 3; d++) H.pt[d] = a.pts[(size_t)H.n * 3 + d];
       }
+      __syncwarp();
+      if (H.flag == 0 && !point_seed(a, H) && tid == 0) H.flag = 2;
     }
     cl.g.sync();
     if (cl.rank != 0) {
@@ -1108,6 +1166,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         a.status[S.H.n] = DVC_NOT_SEARCH;
         __threadfence();
         atomicExch(a.done + S.H.n, 1);
+      }
+      if (a.dataflow && cl.rank == 0 && tid < 32) {
+        __syncwarp();
+        release_successors(a, S.H.n);
       }
       cl.g.sync();
       continue;
@@ -1705,6 +1767,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       __threadfence();
       atomicExch(a.done + n, 1);
       atomicAdd(a.counters + 0, n_eval);
+    }
+    if (a.dataflow && cl.rank == 0 && tid < 32) {
+      __syncwarp();
+      release_successors(a, S.H.n);
     }
     {
       unsigned long long u = n_undef;

@@ -108,6 +108,7 @@ struct Region {
 
 struct CtaState {
   PointHeader H;
+  unsigned long long wkey[kWarps][6];  // per-warp position keys (range checks)
   double sref[3], sbmn[3], sbmx[3];
   double lbmn[3], lbmx[3];  // this CTA's share of the stable cloud: bbox
   Region reg[2];
@@ -122,6 +123,8 @@ struct CtaState {
   float fu[3];
   float M[9], R[9], N[27];  // (I+S)R - I, R, (I+S) dR/dangle
   int use_rot, fail, stop, best;
+  int lrange;                  // lpmn/lpmx hold the last evaluation's positions of this CTA
+  double lpmn[3], lpmx[3];
   double best_obj, obj, obj_old;
   int giu[kGridChunk][3];
   float gfu[kGridChunk][3];
@@ -163,6 +166,61 @@ __device__ __forceinline__ void cluster_reduce(Cl &c, CtaState &S, int K, int nm
       t = k < nmin ? fmin(t, v) : t + v;
     }
     S.red[k] = t;
+  }
+  c.parity ^= 1;
+  __syncthreads();
+}
+
+// Position keys: (c + 2^20) << 32 | bits(f) orders exactly as c + f does for a
+// cell c and a non-negative fraction f < 1. v[0..2] track the minima of the
+// three axes, v[3..5] the minima of the complements (the maxima).
+__device__ __forceinline__ void key_update(unsigned long long v[6], const int c[3], const float f[3]) {
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const unsigned long long key =
+        ((unsigned long long)(unsigned)(c[d] + (1 << 20)) << 32) | __float_as_uint(f[d]);
+    v[d] = min(v[d], key);
+    v[3 + d] = min(v[3 + d], ~key);
+  }
+}
+
+__device__ __forceinline__ double key_pos(unsigned long long k) {
+  return (double)((int)(k >> 32) - (1 << 20)) + (double)__uint_as_float((unsigned)k);
+}
+
+// CTA minima of the six key words into dst[0..6) (one barrier)
+__device__ __forceinline__ void cta_keys(unsigned long long v[6], CtaState &S, unsigned long long *dst) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; k++)
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v[k] = min(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 6; k++) S.wkey[warp][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    unsigned long long m = ~0ull;
+    for (int w = 0; w < kWarps; w++) m = min(m, S.wkey[w][threadIdx.x]);
+    dst[threadIdx.x] = m;
+  }
+}
+
+// cluster_reduce with key words: FP64 sums of entries [0, nsum), minima of the
+// unsigned 64-bit words stored in entries [nsum, nsum + nkey)
+__device__ __forceinline__ void cluster_reduce_keys(Cl &c, CtaState &S, int nsum, int nkey) {
+  c.g.sync();
+  for (int k = threadIdx.x; k < nsum + nkey; k += kThreads) {
+    if (k < nsum) {
+      double t = 0.0;
+      for (unsigned r = 0; r < c.size; r++) t += c.g.map_shared_rank(&S.cbuf[c.parity][0], r)[k];
+      S.red[k] = t;
+    } else {
+      unsigned long long m = ~0ull;
+      for (unsigned r = 0; r < c.size; r++)
+        m = min(m, reinterpret_cast<const unsigned long long *>(c.g.map_shared_rank(&S.cbuf[c.parity][0], r))[k]);
+      reinterpret_cast<unsigned long long *>(S.red)[k] = m;
+    }
   }
   c.parity ^= 1;
   __syncthreads();
@@ -1267,6 +1325,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int d = 3; d < kMaxDof; d++) S.par[d] = 0.0;
       S.best = -1;
       S.best_obj = 1.7976931348623157e308;
+      S.lrange = 0;
     }
     n_eval += 1;
     __syncthreads();
@@ -1455,9 +1514,42 @@ __global__ void __launch_bounds__(kThreads, 1)
         const bool rot = S.use_rot;
         double pmn[3], pmx[3];
         pc.to(6);
-        range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
-        if (S.fail) goto point_done;
-        if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, &tmap, buf_addr[0], bar_addr[0], stage_tx);
+        // Translation only: the exact bbox check before the evaluation. With
+        // rotation/strain the check rides on this iteration's evaluation
+        // (position keys reduced with the sums; a failed check discards the
+        // evaluation); a region is staged here only when none is, otherwise
+        // the previous iteration restaged it if its positions left it.
+        if (!rot || !S.reg[0].ok) {
+          if (!rot) {
+            range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
+            if (S.fail) goto point_done;
+          } else {
+            unsigned long long kv[6] = {~0ull, ~0ull, ~0ull, ~0ull, ~0ull, ~0ull};
+            for (int i = tid; i < nl; i += kThreads) {
+              int c[3];
+              float f[3];
+              sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, true, c, f);
+              key_update(kv, c, f);
+            }
+            cta_keys(kv, S, reinterpret_cast<unsigned long long *>(S.ut));
+            __syncthreads();
+            if (tid == 0) {
+              const unsigned long long *k6 = reinterpret_cast<const unsigned long long *>(S.ut);
+              for (int d = 0; d < 3; d++) {
+                pmn[d] = (double)S.H.o_cor[d] + key_pos(k6[d]);
+                pmx[d] = (double)S.H.o_cor[d] + key_pos(~k6[3 + d]);
+              }
+            }
+          }
+          if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, &tmap, buf_addr[0], bar_addr[0], stage_tx);
+          __syncthreads();
+        } else if (tid == 0) {
+          // restage when the last evaluation's positions left the region
+          S.stop = S.lrange ? restage(a, S, S.lpmn, S.lpmx, esize, &tmap, buf_addr[0], bar_addr[0],
+                                      stage_tx)
+                            : 0;
+          S.lrange = 0;
+        }
         __syncthreads();
         const Region rg = S.reg[0];
         if (S.stop) {
@@ -1471,6 +1563,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         float acc[9];
 #pragma unroll
         for (int q = 0; q < 9; q++) acc[q] = 0.f;
+        unsigned long long kv[6] = {~0ull, ~0ull, ~0ull, ~0ull, ~0ull, ~0ull};
         for (int base = 0; base < nl; base += kThreads) {
           const int i = base + tid;
           float g[kMaxDof];
@@ -1481,6 +1574,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             int c[3];
             float f[3], gv[3];
             sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
+            if (rot) key_update(kv, c, f);
             clamp_cell(c, a.bext);
             bool und;
             t = (rg.ok ? eval_sample_t<VT, IT, true, true>(ss, rg.r0, B, gsc, Gcor, c, f, gv, und)
@@ -1570,7 +1664,32 @@ __global__ void __launch_bounds__(kThreads, 1)
             S.cbuf[cl.parity][4 + tid] = (double)hi + (double)lo;
           }
         }
-        cluster_reduce(cl, S, 4 + nent, 0);
+        if (rot) {
+          cta_keys(kv, S, reinterpret_cast<unsigned long long *>(&S.cbuf[cl.parity][4 + nent]));
+          cluster_reduce_keys(cl, S, 4 + nent, 6);
+          // the range check of this evaluation (BoundBox::contains,
+          // Core/Interpolate.cpp:474-481); this CTA's position range is kept
+          // for the staging decision of the next iteration
+          if (tid == 0) {
+            const unsigned long long *g6 = reinterpret_cast<const unsigned long long *>(&S.red[4 + nent]);
+            const unsigned long long *l6 =
+                reinterpret_cast<const unsigned long long *>(&S.cbuf[cl.parity ^ 1][4 + nent]);
+            int fail = 0;
+            for (int d = 0; d < 3; d++) {
+              const double o = (double)S.H.o_cor[d];
+              if (!(o + key_pos(g6[d]) >= S.H.act_cor.mn[d]) || !(o + key_pos(~g6[3 + d]) <= S.H.act_cor.mx[d]))
+                fail = 1;
+              S.lpmn[d] = o + key_pos(l6[d]);
+              S.lpmx[d] = o + key_pos(~l6[3 + d]);
+            }
+            S.fail = fail;
+            S.lrange = 1;
+          }
+          __syncthreads();
+          if (S.fail) goto point_done;
+        } else {
+          cluster_reduce(cl, S, 4 + nent, 0);
+        }
         pc.to(9);
         // assemble J'J and -J'e (FP64)
         if (tid == 0) {

@@ -249,10 +249,11 @@ struct dvc_engine {
   double subv_rad = 0;
   double nom_mn[3], nom_mx[3], nom_cen[3];
   int bext[3];
-  double *d_sphere = nullptr;
   double morton_rad = 0.0;
-  int *d_cube_order = nullptr;
   std::vector<double> h_offsets;  // stable sample offsets from the point (sample order)
+  // the same split into whole voxels and FP32 fractions in [0, 1)
+  int *d_off_i = nullptr;
+  float *d_off_f = nullptr;
   // grow-only per-call workspace
   void *ws = nullptr;
   size_t ws_bytes = 0;
@@ -413,8 +414,6 @@ int engine_finish(dvc_engine *e) {
     std::vector<double> rel(rel0.size());
     for (size_t i = 0; i < pm.size(); i++)
       for (int d = 0; d < 3; d++) rel[i * 3 + d] = rel0[pm[i] * 3 + d];
-    CUDA_TRY(cudaMalloc(&e->d_sphere, rel.size() * sizeof(double)));
-    CUDA_TRY(cudaMemcpy(e->d_sphere, rel.data(), rel.size() * sizeof(double), cudaMemcpyHostToDevice));
     e->h_offsets.resize(rel.size());
     for (size_t i = 0; i < rel.size(); i++) e->h_offsets[i] = e->p.subvol_aspect[i % 3] * rel[i];
   } else {
@@ -430,12 +429,23 @@ int engine_finish(dvc_engine *e) {
       }
     }
     const std::vector<size_t> perm = morton_perm(off, rmax);
-    std::vector<int> order(perm.begin(), perm.end());
-    CUDA_TRY(cudaMalloc(&e->d_cube_order, order.size() * sizeof(int)));
-    CUDA_TRY(cudaMemcpy(e->d_cube_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice));
     e->h_offsets.resize(off.size());
     for (size_t i = 0; i < perm.size(); i++)
       for (int d = 0; d < 3; d++) e->h_offsets[i * 3 + d] = off[perm[i] * 3 + d];
+  }
+  {
+    const size_t m = e->h_offsets.size();
+    std::vector<int> oi(m);
+    std::vector<float> of(m);
+    for (size_t k = 0; k < m; k++) {
+      const double fl = std::floor(e->h_offsets[k]);
+      oi[k] = (int)fl;
+      of[k] = (float)(e->h_offsets[k] - fl);
+    }
+    CUDA_TRY(cudaMalloc(&e->d_off_i, m * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&e->d_off_f, m * sizeof(float)));
+    CUDA_TRY(cudaMemcpy(e->d_off_i, oi.data(), m * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(e->d_off_f, of.data(), m * sizeof(float), cudaMemcpyHostToDevice));
   }
   CUDA_TRY(cudaGetDevice(&e->device));
   CUDA_TRY(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device));
@@ -625,8 +635,8 @@ void dvc_gpu_destroy(dvc_engine *e) {
     if (e->ref) cudaFree(e->ref);
     if (e->cor) cudaFree(e->cor);
   }
-  if (e->d_sphere) cudaFree(e->d_sphere);
-  if (e->d_cube_order) cudaFree(e->d_cube_order);
+  if (e->d_off_i) cudaFree(e->d_off_i);
+  if (e->d_off_f) cudaFree(e->d_off_f);
   if (e->ws) cudaFree(e->ws);
   delete e;
 }
@@ -815,7 +825,6 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
     a.inc = displ_max / a.num_inc;
     a.inc_int = (a.inc == std::floor(a.inc) && a.inc <= 64.0 && !getenv("DVC_GENERAL_GRID")) ? (int)a.inc : 0;
   }
-  a.sphere_rel = e->d_sphere;
   a.n_points = n_points;
   a.n_process = n_process;
   a.n_neigh = (seed_mode == DVC_SEED_NEIGHBOURS) ? n_neigh : 0;
@@ -842,11 +851,31 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   a.done = done;
   a.counters = counters;
   a.local_cap = cap;
-  a.cube_order = e->d_cube_order;
   a.stage_on = staged ? 1 : 0;
   for (int d = 0; d < 3; d++) a.stage[d] = stage[d];
   a.stage_bytes = (int)stage_bytes;
   for (int r = 0; r < 9; r++) a.rank_start[r] = rs[r];
+  a.off_i = e->d_off_i;
+  a.off_f = e->d_off_f;
+  // extrema of the stable offsets, over all samples and per cluster rank
+  // (the sample clouds' bounding boxes follow from them: FP64 addition of
+  // the point is monotone)
+  for (int d = 0; d < 3; d++) {
+    a.off_min[d] = 1e300;
+    a.off_max[d] = -1e300;
+  }
+  for (int r = 0; r < C; r++)
+    for (int d = 0; d < 3; d++) {
+      double mn = 1e300, mx = -1e300;
+      for (int i = rs[r]; i < rs[r + 1]; i++) {
+        mn = std::min(mn, e->h_offsets[(size_t)i * 3 + d]);
+        mx = std::max(mx, e->h_offsets[(size_t)i * 3 + d]);
+      }
+      a.rank_off_min[r][d] = mn;
+      a.rank_off_max[r][d] = mx;
+      a.off_min[d] = std::min(a.off_min[d], mn);
+      a.off_max[d] = std::max(a.off_max[d], mx);
+    }
   if (getenv("DVC_VERBOSE"))
     fprintf(stderr, "dvc search: %d points, cluster %d, grid %d CTAs, staged %d (box %d x %d x %d), "
             "dynamic smem %zu of %zu, samples/CTA <= %d, grid step %s\n", n_process, C, grid, (int)staged,

@@ -54,7 +54,6 @@ struct SearchArgs {
   int inc_int;  // the grid step when it is a whole number of voxels, else 0
   double inc;
   double rigid[3];
-  const double *sphere_rel;  // n_sub*3 uniform offsets (sphere)
   int n_points, n_process, n_neigh, seed_mode;
   const double *pts;
   const int *order, *rank, *neigh;
@@ -78,13 +77,18 @@ struct SearchArgs {
                                  // CTAs (PhaseClock), [16] Gauss-Newton systems solved by
                                  // the FP64 factorisation
   int local_cap;                 // per-CTA sample capacity of the dynamic arrays
-  const int *cube_order;         // cube samples in space-filling order (natural index)
   // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
   // voxels per evaluation, TMA-loaded into one of two shared buffers
   int stage_on;
   int stage[3];
   int stage_bytes;               // one buffer, padded
   int rank_start[9];             // sample range of each cluster rank
+  // stable offsets of the samples from their point: whole voxels and FP32
+  // fractions; their extrema over all samples and over each rank's samples
+  const int *off_i;
+  const float *off_f;
+  double off_min[3], off_max[3];
+  double rank_off_min[8][3], rank_off_max[8][3];
 };
 
 struct DBox {
@@ -125,6 +129,8 @@ struct CtaState {
   int use_rot, fail, stop, best;
   int lrange;                  // lpmn/lpmx hold the last evaluation's positions of this CTA
   double lpmn[3], lpmx[3];
+  int pi[3], qi[3];            // point - reference box origin, point + seed - correlate box
+  float pf[3], qf[3];          // origin: whole voxels and fractions
   double best_obj, obj, obj_old;
   int giu[kGridChunk][3];
   float gfu[kGridChunk][3];
@@ -317,26 +323,6 @@ __device__ __forceinline__ float dvec(const int *s_ip, const float *s_fp, int i,
 __device__ __forceinline__ void clamp_cell(int c[3], const int bext[3]) {
 #pragma unroll
   for (int d = 0; d < 3; d++) c[d] = min(max(c[d], 0), bext[d] - 1);
-}
-
-// Stable sample position (FloatingCloud constructors, Core/FloatingCloud.cpp:40-128)
-__device__ __forceinline__ void stable_pos(const SearchArgs &a, const double pt[3], int i,
-                                           double p[3]) {
-  if (a.geom == DVC_SPHERE) {
-    for (int d = 0; d < 3; d++)
-      p[d] = __dadd_rn(pt[d], __dmul_rn(a.aspect[d], a.sphere_rel[(size_t)i * 3 + d]));
-  } else {
-    const int nn = a.cube_n;
-    const int j = a.cube_order ? a.cube_order[i] : i;
-    const int idx[3] = {j % nn, (j / nn) % nn, j / (nn * nn)};
-    for (int d = 0; d < 3; d++) {
-      const double r = __dmul_rn(a.subv_rad, a.aspect[d]);
-      const double bmin = __dadd_rn(pt[d], -r);
-      const double bmax = __dadd_rn(pt[d], r);
-      const double inc = __ddiv_rn(__dsub_rn(bmax, bmin), (double)(nn - 1));
-      p[d] = __dadd_rn(bmin, __dmul_rn((double)idx[d], inc));
-    }
-  }
 }
 
 // Objective from one-pass sums: S1 = sum t', S2 = sum t'^2, S3 = sum t' q,
@@ -1243,20 +1229,47 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     // ------------------------------- reference subvolume and samples ---
     // (search_pt_setup: the stable cloud interpolated in the reference box)
+    // Sample positions relative to the boxes: the point's offset from each box
+    // origin (FP64, once) plus the sample's stable offset, each split into
+    // whole voxels and an FP32 fraction. The clouds' bounding boxes are the
+    // point plus the offset extrema (FP64 rounding is monotone, so this is the
+    // bounding box of the rounded FP64 positions); for cubes the reference's
+    // own grid ends (FloatingCloud, Core/FloatingCloud.cpp:84-128).
+    if (tid == 0) {
+      for (int d = 0; d < 3; d++) {
+        split_d(__dsub_rn(S.H.pt[d], (double)S.H.o_ref[d]), S.pi[d], S.pf[d]);
+        split_d(__dsub_rn(__dadd_rn(S.H.pt[d], S.H.seed[d]), (double)S.H.o_cor[d]), S.qi[d], S.qf[d]);
+        if (a.geom == DVC_SPHERE) {
+          S.sbmn[d] = __dadd_rn(S.H.pt[d], a.off_min[d]);
+          S.sbmx[d] = __dadd_rn(S.H.pt[d], a.off_max[d]);
+        } else {
+          const double r = __dmul_rn(a.subv_rad, a.aspect[d]);
+          const double bmin = __dadd_rn(S.H.pt[d], -r);
+          const double bmax = __dadd_rn(S.H.pt[d], r);
+          const double inc = __ddiv_rn(__dsub_rn(bmax, bmin), (double)(a.cube_n - 1));
+          S.sbmn[d] = bmin;
+          S.sbmx[d] = __dadd_rn(bmin, __dmul_rn((double)(a.cube_n - 1), inc));
+        }
+        S.lbmn[d] = __dadd_rn(S.H.pt[d], a.rank_off_min[cl.rank][d]);  // this CTA's share
+        S.lbmx[d] = __dadd_rn(S.H.pt[d], a.rank_off_max[cl.rank][d]);
+      }
+    }
+    __syncthreads();
     {
-      double m[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
       KSum rk[1];
       for (int i = tid; i < nl; i += kThreads) {
-        double p[3];
-        stable_pos(a, S.H.pt, lo + i, p);
         int c[3], ip[3];
         float f[3], fp[3];
+#pragma unroll
         for (int d = 0; d < 3; d++) {
-          m[d] = fmin(m[d], p[d]);
-          m[3 + d] = fmin(m[3 + d], -p[d]);
-          split_d(__dsub_rn(p[d], (double)S.H.o_ref[d]), c[d], f[d]);
-          split_d(__dsub_rn(__dadd_rn(p[d], S.H.seed[d]), (double)S.H.o_cor[d]), ip[d], fp[d]);
-          ip[d] = min(max(ip[d], 0), 1023);
+          const int oi = a.off_i[(size_t)(lo + i) * 3 + d];
+          const float of = a.off_f[(size_t)(lo + i) * 3 + d];
+          const float F = S.pf[d] + of, G = S.qf[d] + of;
+          const float fl = floorf(F), gl = floorf(G);
+          c[d] = S.pi[d] + oi + (int)fl;
+          f[d] = F - fl;
+          ip[d] = min(max(S.qi[d] + oi + (int)gl, 0), 1023);
+          fp[d] = G - gl;
         }
         clamp_cell(c, a.bext);
         bool und;
@@ -1270,19 +1283,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         s_fp[i * 3 + 2] = fp[2];
         rk[0].add(r);
       }
-      cta_min<6>(m, S, S.cbuf[cl.parity]);
-      if (tid == 0)
-        for (int d = 0; d < 3; d++) {  // this CTA's stable sub-bbox (global frame)
-          S.lbmn[d] = S.cbuf[cl.parity][d];
-          S.lbmx[d] = -S.cbuf[cl.parity][3 + d];
-        }
-      cta_sum_comp<1>(rk, S, S.cbuf[cl.parity] + 6);
-      cluster_reduce(cl, S, 7, 6);
+      cta_sum_comp<1>(rk, S, S.cbuf[cl.parity]);
+      cluster_reduce(cl, S, 1, 0);
     }
     if (tid == 0) {
       for (int d = 0; d < 3; d++) {
-        S.sbmn[d] = S.red[d];
-        S.sbmx[d] = -S.red[3 + d];
         // stable reference point (FloatingCloud: centre, or middle of the cube box)
         if (a.geom == DVC_SPHERE) {
           S.sref[d] = S.H.pt[d];
@@ -1296,7 +1301,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         S.kint[d] = ki;
         S.kfrac[d] = kf;
       }
-      S.scal[0] = S.red[6] / nsub;  // reference mean
+      S.scal[0] = S.red[0] / nsub;  // reference mean
     }
     __syncthreads();
     const double rmean = S.scal[0];

@@ -9,7 +9,7 @@ OK, E_ARG, E_CUDA, E_NOMEM, E_TIMEOUT, E_RANGE = 0, -10, -11, -12, -13, -14
 OBJ = {"sad": 0, "ssd": 1, "zssd": 2, "nssd": 3, "znssd": 4}
 INTERP = {"nearest": 0, "trilinear": 1, "tricubic": 2}
 GEOM = {"cube": 0, "sphere": 1}
-SEED_NEIGHBOURS, SEED_GIVEN, SEED_RIGID = 0, 1, 2
+SEED_NEIGHBOURS, SEED_GIVEN, SEED_RIGID, SEED_PARAMS = 0, 1, 2, 3
 
 
 class DvcParams(C.Structure):

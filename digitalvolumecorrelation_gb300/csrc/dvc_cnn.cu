@@ -1,0 +1,570 @@
+// dvc_cnn.cu — the learned initial-guess proposer (no reference counterpart).
+//
+// A small 3D CNN reads the reference and correlate patches (32^3 voxels each,
+// centred on the ROI point, normalised to zero mean and unit variance) and
+// proposes the point's 12 search parameters (u v w, phi the psi, exx eyy ezz
+// exy eyz exz) in place of the reference's start estimate and coarse grid
+// (Search::starting_param + trgrid_global, Core/Search.cpp:277-377,934-1043).
+//
+//   conv 2->16, 3^3, stride 2, pad 1, ReLU      32^3 -> 16^3
+//   conv 16->32                                  16^3 -> 8^3
+//   conv 32->64                                  8^3  -> 4^3
+//   conv 64->96                                  4^3  -> 2^3
+//   dense 768 -> 128, ReLU; dense 128 -> 12
+//
+// Outputs are the parameters divided by fixed scales (kScale). Training: mean
+// squared error against parameters the plain search converged to, Adam.
+// Every kernel here is hand-written FP32 (forward, both backward passes, the
+// optimizer); weight gradients are block reductions in a fixed order, so a
+// training step is deterministic.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/dvc_gpu.h"
+#include "dvc_internal.h"
+
+namespace {
+
+constexpr int kP = 32;  // patch side
+constexpr int kNL = 4;  // conv layers
+const int kCin[kNL] = {2, 16, 32, 64};
+const int kCout[kNL] = {16, 32, 64, 96};
+const int kDin[kNL] = {32, 16, 8, 4};
+constexpr int kF0 = 768, kF1 = 128, kF2 = 12;
+// parameter scales: translations (voxels), rotations (rad), strains
+const float kScale[12] = {10.f, 10.f, 10.f, 0.05f, 0.05f, 0.05f, 0.02f, 0.02f, 0.02f, 0.02f, 0.02f, 0.02f};
+
+struct Layout {
+  size_t w[kNL + 2], b[kNL + 2], total;
+  Layout() {
+    size_t o = 0;
+    for (int l = 0; l < kNL; l++) {
+      w[l] = o;
+      o += (size_t)kCout[l] * kCin[l] * 27;
+      b[l] = o;
+      o += kCout[l];
+    }
+    w[kNL] = o;
+    o += (size_t)kF1 * kF0;
+    b[kNL] = o;
+    o += kF1;
+    w[kNL + 1] = o;
+    o += (size_t)kF2 * kF1;
+    b[kNL + 1] = o;
+    o += kF2;
+    total = o;
+  }
+};
+const Layout kLay;
+
+// ------------------------------------------------------------- kernels ---
+// conv forward: one thread per output (b, co, z, y, x); ReLU
+__global__ void conv_fwd(const float *__restrict__ in, const float *__restrict__ w,
+                         const float *__restrict__ bias, float *__restrict__ out, int B, int Cin,
+                         int Cout, int Din) {
+  const int Do = Din / 2, n3 = Do * Do * Do;
+  const long long total = (long long)B * Cout * n3;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int o = (int)(t % n3);
+    const int co = (int)((t / n3) % Cout);
+    const int b = (int)(t / ((long long)n3 * Cout));
+    const int ox = o % Do, oy = (o / Do) % Do, oz = o / (Do * Do);
+    float acc = bias[co];
+    const float *wc = w + (size_t)co * Cin * 27;
+    for (int ci = 0; ci < Cin; ci++) {
+      const float *ib = in + ((size_t)b * Cin + ci) * Din * Din * Din;
+      const float *wk = wc + ci * 27;
+      for (int kz = 0; kz < 3; kz++) {
+        const int iz = 2 * oz - 1 + kz;
+        if (iz < 0 || iz >= Din) continue;
+        for (int ky = 0; ky < 3; ky++) {
+          const int iy = 2 * oy - 1 + ky;
+          if (iy < 0 || iy >= Din) continue;
+          for (int kx = 0; kx < 3; kx++) {
+            const int ix = 2 * ox - 1 + kx;
+            if (ix < 0 || ix >= Din) continue;
+            acc = fmaf(wk[(kz * 3 + ky) * 3 + kx], ib[((size_t)iz * Din + iy) * Din + ix], acc);
+          }
+        }
+      }
+    }
+    out[t] = fmaxf(acc, 0.f);
+  }
+}
+
+// gradient w.r.t. the conv input activation, times the input's ReLU mask:
+// one thread per input (b, ci, z, y, x)
+__global__ void conv_bwd_data(const float *__restrict__ dz, const float *__restrict__ w,
+                              const float *__restrict__ act_in, float *__restrict__ dz_in, int B,
+                              int Cin, int Cout, int Din) {
+  const int Do = Din / 2, n3 = Din * Din * Din, o3 = Do * Do * Do;
+  const long long total = (long long)B * Cin * n3;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n3);
+    const int ci = (int)((t / n3) % Cin);
+    const int b = (int)(t / ((long long)n3 * Cin));
+    if (act_in[t] <= 0.f) {
+      dz_in[t] = 0.f;
+      continue;
+    }
+    const int ix = i % Din, iy = (i / Din) % Din, iz = i / (Din * Din);
+    float acc = 0.f;
+    for (int kz = 0; kz < 3; kz++) {
+      const int zz = iz + 1 - kz;
+      if (zz < 0 || (zz & 1)) continue;
+      const int oz = zz >> 1;
+      if (oz >= Do) continue;
+      for (int ky = 0; ky < 3; ky++) {
+        const int yy = iy + 1 - ky;
+        if (yy < 0 || (yy & 1)) continue;
+        const int oy = yy >> 1;
+        if (oy >= Do) continue;
+        for (int kx = 0; kx < 3; kx++) {
+          const int xx = ix + 1 - kx;
+          if (xx < 0 || (xx & 1)) continue;
+          const int ox = xx >> 1;
+          if (ox >= Do) continue;
+          const int k = (kz * 3 + ky) * 3 + kx;
+          const size_t od = ((size_t)oz * Do + oy) * Do + ox;
+          for (int co = 0; co < Cout; co++)
+            acc = fmaf(w[((size_t)co * Cin + ci) * 27 + k], dz[((size_t)b * Cout + co) * o3 + od], acc);
+        }
+      }
+    }
+    dz_in[t] = acc;
+  }
+}
+
+// block sum of one value per thread (blockDim 256), result in thread 0
+__device__ __forceinline__ float block_sum(float v) {
+  __shared__ float ws[8];
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float s = 0.f;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 8; k++) s += ws[k];
+  __syncthreads();
+  return s;
+}
+
+// weight gradient: one block per weight (co, ci, k), the batch and output
+// positions strided over the threads; blocks beyond the weights do the biases
+__global__ void __launch_bounds__(256) conv_bwd_weight(const float *__restrict__ act_in,
+                                                       const float *__restrict__ dz,
+                                                       float *__restrict__ dw, float *__restrict__ db,
+                                                       int B, int Cin, int Cout, int Din) {
+  const int Do = Din / 2, o3 = Do * Do * Do, n3 = Din * Din * Din;
+  const int nw = Cout * Cin * 27;
+  const int id = blockIdx.x;
+  const long long terms = (long long)B * o3;
+  float acc = 0.f;
+  if (id < nw) {
+    const int k = id % 27, ci = (id / 27) % Cin, co = id / (27 * Cin);
+    const int kx = k % 3, ky = (k / 3) % 3, kz = k / 9;
+    for (long long q = threadIdx.x; q < terms; q += blockDim.x) {
+      const int o = (int)(q % o3), b = (int)(q / o3);
+      const int ox = o % Do, oy = (o / Do) % Do, oz = o / (Do * Do);
+      const int ix = 2 * ox - 1 + kx, iy = 2 * oy - 1 + ky, iz = 2 * oz - 1 + kz;
+      if (ix < 0 || iy < 0 || iz < 0 || ix >= Din || iy >= Din || iz >= Din) continue;
+      acc = fmaf(dz[((size_t)b * Cout + co) * o3 + o],
+                 act_in[((size_t)b * Cin + ci) * n3 + ((size_t)iz * Din + iy) * Din + ix], acc);
+    }
+    const float s = block_sum(acc);
+    if (threadIdx.x == 0) dw[id] = s;
+  } else {
+    const int co = id - nw;
+    for (long long q = threadIdx.x; q < terms; q += blockDim.x) {
+      const int o = (int)(q % o3), b = (int)(q / o3);
+      acc += dz[((size_t)b * Cout + co) * o3 + o];
+    }
+    const float s = block_sum(acc);
+    if (threadIdx.x == 0) db[co] = s;
+  }
+}
+
+// dense forward y[b][j] = sum_i W[j][i] x[b][i] + bias[j] (optionally ReLU)
+__global__ void fc_fwd(const float *__restrict__ x, const float *__restrict__ w,
+                       const float *__restrict__ bias, float *__restrict__ y, int B, int Nin, int Nout,
+                       int relu) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * Nout) return;
+  const int j = t % Nout, b = t / Nout;
+  float acc = bias[j];
+  for (int i = 0; i < Nin; i++) acc = fmaf(w[(size_t)j * Nin + i], x[(size_t)b * Nin + i], acc);
+  y[t] = relu ? fmaxf(acc, 0.f) : acc;
+}
+
+// dense input gradient times the input's ReLU mask
+__global__ void fc_bwd_data(const float *__restrict__ dz, const float *__restrict__ w,
+                            const float *__restrict__ act_in, float *__restrict__ dz_in, int B,
+                            int Nin, int Nout) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * Nin) return;
+  const int i = t % Nin, b = t / Nin;
+  if (act_in[t] <= 0.f) {
+    dz_in[t] = 0.f;
+    return;
+  }
+  float acc = 0.f;
+  for (int j = 0; j < Nout; j++) acc = fmaf(w[(size_t)j * Nin + i], dz[(size_t)b * Nout + j], acc);
+  dz_in[t] = acc;
+}
+
+// dense weight and bias gradients: one thread per weight (j, i), then biases
+__global__ void fc_bwd_weight(const float *__restrict__ x, const float *__restrict__ dz,
+                              float *__restrict__ dw, float *__restrict__ db, int B, int Nin, int Nout) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < Nout * Nin) {
+    const int i = t % Nin, j = t / Nin;
+    float acc = 0.f;
+    for (int b = 0; b < B; b++) acc = fmaf(dz[(size_t)b * Nout + j], x[(size_t)b * Nin + i], acc);
+    dw[t] = acc;
+  } else if (t < Nout * Nin + Nout) {
+    const int j = t - Nout * Nin;
+    float acc = 0.f;
+    for (int b = 0; b < B; b++) acc += dz[(size_t)b * Nout + j];
+    db[j] = acc;
+  }
+}
+
+struct Scales {
+  float s[12];
+};
+
+// mean squared error of the scaled outputs, its gradient, per-sample sums
+__global__ void mse_grad(const float *__restrict__ y, const float *__restrict__ target, Scales sc,
+                         float *__restrict__ dy, float *__restrict__ sq, int B) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * kF2) return;
+  const float e = y[t] - target[t] / sc.s[t % kF2];
+  dy[t] = 2.f * e / (float)(B * kF2);
+  sq[t] = e * e;
+}
+
+__global__ void __launch_bounds__(256) sum_kernel(const float *__restrict__ v, int n, float *out) {
+  float acc = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += v[i];
+  const float s = block_sum(acc);
+  if (threadIdx.x == 0) *out = s;
+}
+
+__global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                            float *__restrict__ v, size_t n, float lr, float b1, float b2, float eps,
+                            float c1, float c2) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// patches: one block per point; voxel of the patch at (x, y, z) is
+// volume[round(p) - 16 + (x, y, z)] (0 outside); each patch normalised to zero
+// mean and unit variance
+template <typename VT>
+__global__ void __launch_bounds__(256) patch_kernel(const VT *__restrict__ ref, const VT *__restrict__ cor,
+                                                    int nx, int ny, int nz, const double *__restrict__ pts,
+                                                    const int *__restrict__ idx, float *__restrict__ out) {
+  const int n = idx ? idx[blockIdx.x] : blockIdx.x;
+  int o[3];
+  for (int d = 0; d < 3; d++) o[d] = (int)floor(pts[(size_t)n * 3 + d] + 0.5) - kP / 2;
+  constexpr int N3 = kP * kP * kP;
+  for (int v = 0; v < 2; v++) {
+    const VT *vol = v == 0 ? ref : cor;
+    float *dst = out + ((size_t)blockIdx.x * 2 + v) * N3;
+    float s = 0.f;
+    for (int i = threadIdx.x; i < N3; i += blockDim.x) {
+      const int x = o[0] + i % kP, y = o[1] + (i / kP) % kP, z = o[2] + i / (kP * kP);
+      float val = 0.f;
+      if (x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz)
+        val = (float)vol[((size_t)z * ny + y) * nx + x];
+      dst[i] = val;
+      s += val;
+    }
+    __shared__ float mean_s, inv_s;
+    const float tot = block_sum(s);
+    if (threadIdx.x == 0) mean_s = tot / N3;
+    __syncthreads();
+    const float mean = mean_s;
+    float q = 0.f;
+    for (int i = threadIdx.x; i < N3; i += blockDim.x) {
+      const float dv = dst[i] - mean;
+      q += dv * dv;
+    }
+    const float var = block_sum(q);
+    if (threadIdx.x == 0) inv_s = 1.f / sqrtf(var / N3 + 1e-6f);
+    __syncthreads();
+    const float inv = inv_s;
+    for (int i = threadIdx.x; i < N3; i += blockDim.x) dst[i] = (dst[i] - mean) * inv;
+    __syncthreads();
+  }
+}
+
+// network outputs -> start parameters (FP64, [n][12])
+__global__ void denorm_kernel(const float *__restrict__ y, Scales sc, const int *__restrict__ idx,
+                              double *__restrict__ params, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * kF2) return;
+  const int k = t % kF2, r = t / kF2;
+  const int p = idx ? idx[r] : r;
+  params[(size_t)p * kF2 + k] = (double)(y[t] * sc.s[k]);
+}
+
+unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152LL * 64); }
+
+}  // namespace
+
+// ============================================================ network ===
+struct dvc_cnn {
+  float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+  long long step = 0;
+  int cap = 0;                         // batch capacity of the activation buffers
+  float *act[kNL + 3] = {nullptr};     // input, conv1..4 outputs, dense1 output, dense2 output
+  float *dact[kNL + 3] = {nullptr};    // gradients of the same (pre-ReLU where masked)
+  float *sq = nullptr, *loss = nullptr;
+};
+
+namespace {
+
+size_t act_size(int l) {  // floats per sample of act[l]
+  if (l == 0) return (size_t)2 * kP * kP * kP;
+  if (l <= kNL) {
+    const int d = kDin[l - 1] / 2;
+    return (size_t)kCout[l - 1] * d * d * d;
+  }
+  return l == kNL + 1 ? (size_t)kF1 : (size_t)kF2;
+}
+
+int ensure_batch(dvc_cnn *c, int B) {
+  if (B <= c->cap) return DVC_OK;
+  for (int l = 0; l < kNL + 3; l++) {
+    cudaFree(c->act[l]);
+    cudaFree(c->dact[l]);
+    c->act[l] = c->dact[l] = nullptr;
+  }
+  cudaFree(c->sq);
+  c->cap = 0;
+  for (int l = 0; l < kNL + 3; l++) {
+    if (cudaMalloc(&c->act[l], act_size(l) * B * 4) != cudaSuccess ||
+        cudaMalloc(&c->dact[l], act_size(l) * B * 4) != cudaSuccess)
+      return dvc_internal_set_error(DVC_E_NOMEM, "network activations");
+  }
+  if (cudaMalloc(&c->sq, (size_t)B * kF2 * 4) != cudaSuccess)
+    return dvc_internal_set_error(DVC_E_NOMEM, "network loss buffer");
+  c->cap = B;
+  return DVC_OK;
+}
+
+Scales scales() {
+  Scales s;
+  for (int k = 0; k < 12; k++) s.s[k] = kScale[k];
+  return s;
+}
+
+// forward from act[0] (already holding the patches) to act[kNL + 2]
+void forward(dvc_cnn *c, int B, cudaStream_t st) {
+  for (int l = 0; l < kNL; l++) {
+    const int Do = kDin[l] / 2;
+    conv_fwd<<<grid_for((long long)B * kCout[l] * Do * Do * Do), 256, 0, st>>>(
+        c->act[l], c->p + kLay.w[l], c->p + kLay.b[l], c->act[l + 1], B, kCin[l], kCout[l], kDin[l]);
+  }
+  fc_fwd<<<(B * kF1 + 255) / 256, 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL], c->p + kLay.b[kNL],
+                                                c->act[kNL + 1], B, kF0, kF1, 1);
+  fc_fwd<<<(B * kF2 + 255) / 256, 256, 0, st>>>(c->act[kNL + 1], c->p + kLay.w[kNL + 1],
+                                                c->p + kLay.b[kNL + 1], c->act[kNL + 2], B, kF1, kF2, 0);
+}
+
+// loss and gradients into c->g (targets raw parameters [B][12] FP32)
+void backward(dvc_cnn *c, int B, const float *targets, cudaStream_t st) {
+  mse_grad<<<(B * kF2 + 255) / 256, 256, 0, st>>>(c->act[kNL + 2], targets, scales(), c->dact[kNL + 2],
+                                                  c->sq, B);
+  sum_kernel<<<1, 256, 0, st>>>(c->sq, B * kF2, c->loss);
+  // dense 2
+  fc_bwd_weight<<<(kF2 * kF1 + kF2 + 255) / 256, 256, 0, st>>>(c->act[kNL + 1], c->dact[kNL + 2],
+                                                               c->g + kLay.w[kNL + 1], c->g + kLay.b[kNL + 1],
+                                                               B, kF1, kF2);
+  fc_bwd_data<<<(B * kF1 + 255) / 256, 256, 0, st>>>(c->dact[kNL + 2], c->p + kLay.w[kNL + 1],
+                                                     c->act[kNL + 1], c->dact[kNL + 1], B, kF1, kF2);
+  // dense 1
+  fc_bwd_weight<<<(kF1 * kF0 + kF1 + 255) / 256, 256, 0, st>>>(c->act[kNL], c->dact[kNL + 1],
+                                                               c->g + kLay.w[kNL], c->g + kLay.b[kNL], B,
+                                                               kF0, kF1);
+  fc_bwd_data<<<(B * kF0 + 255) / 256, 256, 0, st>>>(c->dact[kNL + 1], c->p + kLay.w[kNL], c->act[kNL],
+                                                     c->dact[kNL], B, kF0, kF1);
+  // conv layers, last to first (dact[l + 1] holds the gradient before ReLU)
+  for (int l = kNL - 1; l >= 0; l--) {
+    conv_bwd_weight<<<kCout[l] * kCin[l] * 27 + kCout[l], 256, 0, st>>>(
+        c->act[l], c->dact[l + 1], c->g + kLay.w[l], c->g + kLay.b[l], B, kCin[l], kCout[l], kDin[l]);
+    if (l > 0)
+      conv_bwd_data<<<grid_for((long long)B * act_size(l)), 256, 0, st>>>(
+          c->dact[l + 1], c->p + kLay.w[l], c->act[l], c->dact[l], B, kCin[l], kCout[l], kDin[l]);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int dvc_cnn_param_count(void) { return (int)kLay.total; }
+
+int dvc_cnn_create(dvc_cnn **out, unsigned seed) {
+  if (!out) return dvc_internal_set_error(DVC_E_ARG, "null argument");
+  dvc_cnn *c = new dvc_cnn();
+  const size_t n = kLay.total;
+  if (cudaMalloc(&c->p, n * 4) != cudaSuccess || cudaMalloc(&c->g, n * 4) != cudaSuccess ||
+      cudaMalloc(&c->m, n * 4) != cudaSuccess || cudaMalloc(&c->v, n * 4) != cudaSuccess ||
+      cudaMalloc(&c->loss, 4) != cudaSuccess) {
+    dvc_cnn_destroy(c);
+    return dvc_internal_set_error(DVC_E_NOMEM, "network parameters");
+  }
+  // He-normal weights (fan-in), zero biases
+  std::vector<float> h(n, 0.f);
+  std::mt19937 gen(seed);
+  auto fill = [&](size_t off, size_t cnt, int fan_in) {
+    std::normal_distribution<float> nd(0.f, std::sqrt(2.f / (float)fan_in));
+    for (size_t i = 0; i < cnt; i++) h[off + i] = nd(gen);
+  };
+  for (int l = 0; l < kNL; l++) fill(kLay.w[l], (size_t)kCout[l] * kCin[l] * 27, kCin[l] * 27);
+  fill(kLay.w[kNL], (size_t)kF1 * kF0, kF0);
+  fill(kLay.w[kNL + 1], (size_t)kF2 * kF1, kF1);
+  cudaMemcpy(c->p, h.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemset(c->m, 0, n * 4);
+  cudaMemset(c->v, 0, n * 4);
+  *out = c;
+  return DVC_OK;
+}
+
+void dvc_cnn_destroy(dvc_cnn *c) {
+  if (!c) return;
+  cudaFree(c->p);
+  cudaFree(c->g);
+  cudaFree(c->m);
+  cudaFree(c->v);
+  cudaFree(c->loss);
+  cudaFree(c->sq);
+  for (int l = 0; l < kNL + 3; l++) {
+    cudaFree(c->act[l]);
+    cudaFree(c->dact[l]);
+  }
+  delete c;
+}
+
+int dvc_cnn_get_weights(dvc_cnn *c, float *host, int n) {
+  if (!c || !host || n != (int)kLay.total) return dvc_internal_set_error(DVC_E_ARG, "bad weight buffer");
+  if (cudaMemcpy(host, c->p, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return dvc_internal_set_error(DVC_E_CUDA, "weight copy");
+  return DVC_OK;
+}
+
+int dvc_cnn_set_weights(dvc_cnn *c, const float *host, int n) {
+  if (!c || !host || n != (int)kLay.total) return dvc_internal_set_error(DVC_E_ARG, "bad weight buffer");
+  if (cudaMemcpy(c->p, host, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+    return dvc_internal_set_error(DVC_E_CUDA, "weight copy");
+  cudaMemset(c->m, 0, (size_t)n * 4);
+  cudaMemset(c->v, 0, (size_t)n * 4);
+  c->step = 0;
+  return DVC_OK;
+}
+
+int dvc_cnn_forward(dvc_cnn *c, int batch, const float *patches_dev, float *out_dev, void *stream) {
+  if (!c || batch <= 0 || !patches_dev || !out_dev) return dvc_internal_set_error(DVC_E_ARG, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = ensure_batch(c, batch);
+  if (rc) return rc;
+  cudaMemcpyAsync(c->act[0], patches_dev, act_size(0) * batch * 4, cudaMemcpyDeviceToDevice, st);
+  forward(c, batch, st);
+  cudaMemcpyAsync(out_dev, c->act[kNL + 2], (size_t)batch * kF2 * 4, cudaMemcpyDeviceToDevice, st);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
+  return DVC_OK;
+}
+
+int dvc_cnn_gradients(dvc_cnn *c, int batch, const float *patches_dev, const float *targets_dev,
+                      float *grad_host, float *loss) {
+  if (!c || batch <= 0 || !patches_dev || !targets_dev) return dvc_internal_set_error(DVC_E_ARG, "bad arguments");
+  int rc = ensure_batch(c, batch);
+  if (rc) return rc;
+  cudaMemcpy(c->act[0], patches_dev, act_size(0) * batch * 4, cudaMemcpyDeviceToDevice);
+  forward(c, batch, 0);
+  backward(c, batch, targets_dev, 0);
+  float l = 0.f;
+  if (cudaMemcpy(&l, c->loss, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return dvc_internal_set_error(DVC_E_CUDA, "loss copy");
+  if (loss) *loss = l / (float)(batch * kF2);
+  if (grad_host) cudaMemcpy(grad_host, c->g, kLay.total * 4, cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
+  return DVC_OK;
+}
+
+int dvc_cnn_train_step(dvc_cnn *c, int batch, const float *patches_dev, const float *targets_dev,
+                       float lr, float *loss) {
+  int rc = dvc_cnn_gradients(c, batch, patches_dev, targets_dev, nullptr, loss);
+  if (rc) return rc;
+  c->step += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)c->step), c2 = 1.f - std::pow(b2, (float)c->step);
+  adam_kernel<<<grid_for((long long)kLay.total), 256>>>(c->p, c->g, c->m, c->v, kLay.total, lr, b1, b2, 1e-8f,
+                                                        c1, c2);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
+  return DVC_OK;
+}
+
+}  // extern "C"
+
+// patches of the points idx[0..n) (or 0..n) of an engine's volume pair
+int dvc_internal_patches(const void *ref, const void *cor, int bpv, int nx, int ny, int nz,
+                         int n, const double *pts_dev, const int *idx_dev, float *out_dev,
+                         cudaStream_t st) {
+  if (n <= 0) return DVC_OK;
+  if (bpv == 1)
+    patch_kernel<uint8_t><<<n, 256, 0, st>>>((const uint8_t *)ref, (const uint8_t *)cor, nx, ny, nz,
+                                             pts_dev, idx_dev, out_dev);
+  else
+    patch_kernel<uint16_t><<<n, 256, 0, st>>>((const uint16_t *)ref, (const uint16_t *)cor, nx, ny, nz,
+                                              pts_dev, idx_dev, out_dev);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
+  return DVC_OK;
+}
+
+// start parameters of points idx[0..n) from the network, written to
+// params_dev[idx[r] * 12 ..] (FP64), in batches
+int dvc_internal_cnn_seed(dvc_cnn *c, const void *ref, const void *cor, int bpv, int nx, int ny,
+                          int nz, int n, const double *pts_dev, const int *idx_dev, double *params_dev,
+                          cudaStream_t st) {
+  const int B = 256;
+  int rc = ensure_batch(c, B);
+  if (rc) return rc;
+  for (int r0 = 0; r0 < n; r0 += B) {
+    const int nb = std::min(B, n - r0);
+    // patches straight into the input activation
+    const double *pb = pts_dev + (idx_dev ? 0 : (size_t)r0 * 3);
+    const int *ib = idx_dev ? idx_dev + r0 : nullptr;
+    if (bpv == 1)
+      patch_kernel<uint8_t><<<nb, 256, 0, st>>>((const uint8_t *)ref, (const uint8_t *)cor, nx, ny, nz, pb,
+                                                ib, c->act[0]);
+    else
+      patch_kernel<uint16_t><<<nb, 256, 0, st>>>((const uint16_t *)ref, (const uint16_t *)cor, nx, ny, nz,
+                                                 pb, ib, c->act[0]);
+    forward(c, nb, st);
+    denorm_kernel<<<(nb * kF2 + 255) / 256, 256, 0, st>>>(c->act[kNL + 2], scales(),
+                                                          idx_dev ? idx_dev + r0 : nullptr,
+                                                          params_dev + (idx_dev ? 0 : (size_t)r0 * kF2), nb);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
+  return DVC_OK;
+}

@@ -391,14 +391,6 @@ void rank_ranges(const std::vector<double> &off, double rad, int C, int out[9]) 
   for (int r = C + 1; r < 9; r++) out[r] = out[C];
 }
 
-std::vector<double> morton_order(const std::vector<double> &rel, double rad) {
-  const std::vector<size_t> perm = morton_perm(rel, rad);
-  std::vector<double> out(rel.size());
-  for (size_t i = 0; i < perm.size(); i++)
-    for (int d = 0; d < 3; d++) out[i * 3 + d] = rel[perm[i] * 3 + d];
-  return out;
-}
-
 int engine_finish(dvc_engine *e) {
   engine_geometry(e);
   if (e->bext[0] > 1023 || e->bext[1] > 1023 || e->bext[2] > 1023)
@@ -650,10 +642,11 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   if (!e) return set_error(DVC_E_ARG, "null engine");
   if (n_points < 0 || n_process < 0 || n_process > n_points)
     return set_error(DVC_E_ARG, "n_process must be in 0..n_points");
-  if (seed_mode < 0 || seed_mode > 2) return set_error(DVC_E_ARG, "bad seed_mode");
+  if (seed_mode < 0 || seed_mode > 3) return set_error(DVC_E_ARG, "bad seed_mode");
   if (seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !neigh_dev)
     return set_error(DVC_E_ARG, "neighbour list required");
-  if (seed_mode == DVC_SEED_GIVEN && !seeds_dev) return set_error(DVC_E_ARG, "seeds required");
+  if ((seed_mode == DVC_SEED_GIVEN || seed_mode == DVC_SEED_PARAMS) && !seeds_dev)
+    return set_error(DVC_E_ARG, "seeds required");
   if (n_points == 0) return DVC_OK;
   cudaStream_t st = (cudaStream_t)stream;
   const dvc_params &p = e->p;
@@ -955,7 +948,8 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
   if (n_process > 0 && !order) return set_error(DVC_E_ARG, "order required");
   if (seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !neigh)
     return set_error(DVC_E_ARG, "neighbour list required");
-  if (seed_mode == DVC_SEED_GIVEN && !seeds) return set_error(DVC_E_ARG, "seeds required");
+  if ((seed_mode == DVC_SEED_GIVEN || seed_mode == DVC_SEED_PARAMS) && !seeds)
+    return set_error(DVC_E_ARG, "seeds required");
   for (int i = 0; i < n_process; i++)
     if (order[i] < 0 || order[i] >= n_points) return set_error(DVC_E_ARG, "order index out of range");
   if (seed_mode == DVC_SEED_NEIGHBOURS && neigh)
@@ -993,9 +987,10 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
     TRYC(cudaMalloc(&d_neigh, N * n_neigh * sizeof(int)));
     TRYC(cudaMemcpy(d_neigh, neigh, N * n_neigh * sizeof(int), cudaMemcpyHostToDevice));
   }
-  if (seed_mode == DVC_SEED_GIVEN) {
-    TRYC(cudaMalloc(&d_seeds, N * 3 * sizeof(double)));
-    TRYC(cudaMemcpy(d_seeds, seeds, N * 3 * sizeof(double), cudaMemcpyHostToDevice));
+  if (seed_mode == DVC_SEED_GIVEN || seed_mode == DVC_SEED_PARAMS) {
+    const size_t per = seed_mode == DVC_SEED_GIVEN ? 3 : 12;
+    TRYC(cudaMalloc(&d_seeds, N * per * sizeof(double)));
+    TRYC(cudaMemcpy(d_seeds, seeds, N * per * sizeof(double), cudaMemcpyHostToDevice));
   }
   TRYC(cudaEventCreate(&ev0));
   TRYC(cudaEventCreate(&ev1));
@@ -1073,6 +1068,95 @@ int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]) {
             "%llu Gauss-Newton systems used the FP64 factorisation\n", slow, fp64);
   }
   return DVC_OK;
+}
+
+// ------------------------------------------------------ learned search ---
+namespace {
+// points of `order` whose search failed or whose objective exceeds thr
+__global__ void fallback_kernel(int n_process, const int *order, const int *status, const double *objmin,
+                                double thr, int *list, int *count) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_process) return;
+  const int i = order[r];
+  if (status[i] != DVC_POINT_GOOD || objmin[i] > thr) list[atomicAdd(count, 1)] = i;
+}
+// translations of the start parameters, [n][3]
+__global__ void seeds3_kernel(int n, const double *p12, double *p3) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n * 3) p3[t] = p12[(size_t)(t / 3) * 12 + t % 3];
+}
+// results of the points in list, from the second search's arrays
+__global__ void merge_kernel(int n, const int *list, const int *st2, const double *ob2, const double *pa2,
+                             const int *it2, int *st, double *ob, double *pa, int *it) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int i = list[r];
+  st[i] = st2[i];
+  ob[i] = ob2[i];
+  for (int k = 0; k < 12; k++) pa[(size_t)i * 12 + k] = pa2[(size_t)i * 12 + k];
+  if (it) it[i] += it2[i];
+}
+}  // namespace
+
+int dvc_cnn_patches(dvc_engine *e, int n, const double *points_dev, const int *idx_dev, float *patches_dev,
+                    void *stream) {
+  if (!e || n < 0 || (n > 0 && (!points_dev || !patches_dev))) return set_error(DVC_E_ARG, "bad arguments");
+  return dvc_internal_patches(e->ref, e->cor, e->p.bytes_per_voxel, e->p.vol_wide, e->p.vol_high,
+                              e->p.vol_tall, n, points_dev, idx_dev, patches_dev, (cudaStream_t)stream);
+}
+
+int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const double *points_dev, int n_process,
+                            const int *order_dev, double obj_threshold, int *status_dev, double *objmin_dev,
+                            double *params_dev, int *gn_iters_dev, int *n_fallback, void *stream) {
+  if (!e || !net) return set_error(DVC_E_ARG, "null engine or network");
+  if (n_points < 0 || n_process < 0 || n_process > n_points) return set_error(DVC_E_ARG, "bad sizes");
+  if (n_fallback) *n_fallback = 0;
+  if (n_process == 0) return DVC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t N = (size_t)n_points;
+  double *p12 = nullptr, *p3 = nullptr, *ob2 = nullptr, *pa2 = nullptr;
+  int *list = nullptr, *cnt = nullptr, *st2 = nullptr, *it2 = nullptr;
+  int rc = DVC_OK, nfb = 0;
+  auto cleanup = [&]() {
+    cudaFree(p12); cudaFree(p3); cudaFree(ob2); cudaFree(pa2);
+    cudaFree(list); cudaFree(cnt); cudaFree(st2); cudaFree(it2);
+  };
+  if (cudaMalloc(&p12, N * 12 * 8) != cudaSuccess || cudaMalloc(&p3, N * 3 * 8) != cudaSuccess ||
+      cudaMalloc(&list, (size_t)n_process * 4) != cudaSuccess || cudaMalloc(&cnt, 4) != cudaSuccess) {
+    cleanup();
+    return set_error(DVC_E_NOMEM, "learned search buffers");
+  }
+  cudaMemsetAsync(p12, 0, N * 12 * 8, st);
+  rc = dvc_internal_cnn_seed(net, e->ref, e->cor, e->p.bytes_per_voxel, e->p.vol_wide, e->p.vol_high,
+                             e->p.vol_tall, n_process, points_dev, order_dev, p12, st);
+  if (!rc)
+    rc = process_device_ws(e, n_points, points_dev, n_process, order_dev, 0, nullptr, DVC_SEED_PARAMS, p12,
+                           status_dev, objmin_dev, params_dev, gn_iters_dev, stream, nullptr);
+  if (!rc) {
+    cudaMemsetAsync(cnt, 0, 4, st);
+    fallback_kernel<<<(n_process + 255) / 256, 256, 0, st>>>(n_process, order_dev, status_dev, objmin_dev,
+                                                             obj_threshold, list, cnt);
+    if (cudaMemcpyAsync(&nfb, cnt, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = set_error(DVC_E_CUDA, "fallback count");
+  }
+  if (!rc && nfb > 0) {
+    if (cudaMalloc(&ob2, N * 8) != cudaSuccess || cudaMalloc(&pa2, N * 96) != cudaSuccess ||
+        cudaMalloc(&st2, N * 4) != cudaSuccess || cudaMalloc(&it2, N * 4) != cudaSuccess) {
+      cleanup();
+      return set_error(DVC_E_NOMEM, "learned search buffers");
+    }
+    seeds3_kernel<<<(int)((N * 3 + 255) / 256), 256, 0, st>>>(n_points, p12, p3);
+    rc = process_device_ws(e, n_points, points_dev, nfb, list, 0, nullptr, DVC_SEED_GIVEN, p3, st2, ob2, pa2,
+                           it2, stream, nullptr);
+    if (!rc)
+      merge_kernel<<<(nfb + 255) / 256, 256, 0, st>>>(nfb, list, st2, ob2, pa2, it2, status_dev, objmin_dev,
+                                                      params_dev, gn_iters_dev);
+  }
+  if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = set_error(DVC_E_CUDA, "learned search");
+  if (!rc && n_fallback) *n_fallback = nfb;
+  cleanup();
+  return rc;
 }
 
 int dvc_gpu_interpolate(dvc_engine *e, int volume, const double center[3], int n, const double *pts,

@@ -403,6 +403,7 @@ __device__ bool point_seed(const SearchArgs &a, PointHeader &H) {
     const int d = lane;
     double sd;
     if (a.seed_mode == DVC_SEED_GIVEN) sd = a.seeds[(size_t)n * 3 + d];
+    else if (a.seed_mode == DVC_SEED_PARAMS) sd = a.seeds[(size_t)n * 12 + d];
     else if (good != 0) sd = sum[d] / good;
     else sd = a.rigid[d];
     H.seed[d] = sd;
@@ -1327,7 +1328,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       S.shift = shift;
       S.rsum2 = (fcn == DVC_NSSD || fcn == DVC_ZNSSD) ? 1.0 : rc2;
       for (int d = 0; d < 3; d++) S.par[d] = S.H.seed[d];
-      for (int d = 3; d < kMaxDof; d++) S.par[d] = 0.0;
+      for (int d = 3; d < kMaxDof; d++)
+        S.par[d] = (a.seed_mode == DVC_SEED_PARAMS && d < ndof) ? a.seeds[(size_t)S.H.n * 12 + d] : 0.0;
       S.best = -1;
       S.best_obj = 1.7976931348623157e308;
       S.lrange = 0;
@@ -1342,7 +1344,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // translation whose sample box leaves the active box fails the point.
     // The correlate region of each translation is staged by TMA into one of
     // two buffers while the previous translation is evaluated.
-    if (a.do_grid) {
+    if (a.do_grid && a.seed_mode != DVC_SEED_PARAMS) {
       const int k = a.num_inc;
       const int side = 2 * k + 1;
       const int total = side * side * side;

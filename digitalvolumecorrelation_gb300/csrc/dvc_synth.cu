@@ -3,7 +3,9 @@
 //
 // value(x) = background + sum_b amp_b exp(-|X(x) - c_b|^2 / (2 sigma_b^2)) + noise
 // where X(x) is the reference position of voxel x under the deformation
-// (X + u(X) = x), blobs contribute within 4 sigma, noise ~ N(0, noise_sigma)
+// (X + u(X) = x; affine: solved, sinusoid and bump field: fixed-point
+// iteration, their gradients being well below 1), blobs contribute within 4
+// sigma, noise ~ N(0, noise_sigma)
 // from a counter-based hash of (seed, voxel index), then the value is rounded
 // and clipped to [0, vmax]. Blobs are binned on the host by their deformed
 // centre so each voxel visits only the blobs of its 27 neighbouring bins.
@@ -20,6 +22,7 @@
 namespace {
 
 constexpr int kBin = 16;
+constexpr int kMaxBumps = 32;
 
 struct SynthArgs {
   void *vol;
@@ -31,6 +34,10 @@ struct SynthArgs {
   int deform;
   float Ainv[9], t[3], c[3];  // affine: X = c + Ainv (x - t - c)
   float amp, len;             // sinusoid
+  // bump field: affine t + E (X - c) plus sum_k a_k exp(-|X - p_k|^2 / (2 s_k^2))
+  float E[9];
+  int nbump;
+  float bump[kMaxBumps][7];   // p (3), 1/(2 s^2), a (3)
   float background, noise_sigma, vmax;
   unsigned long long seed;
 };
@@ -54,6 +61,23 @@ __global__ void synth_kernel(SynthArgs a) {
       const float r[3] = {X[0] - a.t[0] - a.c[0], X[1] - a.t[1] - a.c[1], X[2] - a.t[2] - a.c[2]};
       for (int i = 0; i < 3; i++)
         X[i] = a.c[i] + a.Ainv[i * 3 + 0] * r[0] + a.Ainv[i * 3 + 1] * r[1] + a.Ainv[i * 3 + 2] * r[2];
+    } else if (a.deform == 3) {
+      const float x0[3] = {X[0], X[1], X[2]};
+      for (int it = 0; it < 12; it++) {
+        float u[3];
+        const float r[3] = {X[0] - a.c[0], X[1] - a.c[1], X[2] - a.c[2]};
+        for (int i = 0; i < 3; i++) u[i] = a.t[i] + a.E[i * 3] * r[0] + a.E[i * 3 + 1] * r[1] + a.E[i * 3 + 2] * r[2];
+        for (int k = 0; k < a.nbump; k++) {
+          const float dx = X[0] - a.bump[k][0], dy = X[1] - a.bump[k][1], dz = X[2] - a.bump[k][2];
+          const float g = __expf(-(dx * dx + dy * dy + dz * dz) * a.bump[k][3]);
+          u[0] += a.bump[k][4] * g;
+          u[1] += a.bump[k][5] * g;
+          u[2] += a.bump[k][6] * g;
+        }
+        X[0] = x0[0] - u[0];
+        X[1] = x0[1] - u[1];
+        X[2] = x0[2] - u[2];
+      }
     } else if (a.deform == 2) {
       const float x0[3] = {X[0], X[1], X[2]};
       const float w = 6.283185307179586f / a.len;
@@ -107,7 +131,7 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
                                     const double *coef, float background, float noise_sigma,
                                     unsigned long long noise_seed, float vmax, void *stream) {
   if (!vol_dev || nx <= 0 || ny <= 0 || nz <= 0 || (bytes_per_voxel != 1 && bytes_per_voxel != 2) ||
-      n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 2 || (deform && !coef))
+      n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 3 || (deform && !coef))
     return dvc_internal_set_error(DVC_E_ARG, "bad synth arguments");
   SynthArgs a{};
   a.vol = vol_dev;
@@ -147,6 +171,26 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
   } else if (deform == 2) {
     a.amp = (float)coef[0];
     a.len = (float)coef[1];
+  } else if (deform == 3) {
+    // coef: t (3), E (9), c (3), n, then n x (p (3), s, a (3))
+    const int nb = (int)coef[15];
+    if (nb < 0 || nb > kMaxBumps) return dvc_internal_set_error(DVC_E_ARG, "at most 32 bumps");
+    for (int i = 0; i < 3; i++) {
+      a.t[i] = (float)coef[i];
+      a.c[i] = (float)coef[12 + i];
+    }
+    for (int i = 0; i < 9; i++) a.E[i] = (float)coef[3 + i];
+    a.nbump = nb;
+    for (int k = 0; k < nb; k++) {
+      const double *b = coef + 16 + 7 * k;
+      a.bump[k][0] = (float)b[0];
+      a.bump[k][1] = (float)b[1];
+      a.bump[k][2] = (float)b[2];
+      a.bump[k][3] = (float)(1.0 / (2.0 * b[3] * b[3]));
+      a.bump[k][4] = (float)b[4];
+      a.bump[k][5] = (float)b[5];
+      a.bump[k][6] = (float)b[6];
+    }
   }
   const int nbins = a.gx * a.gy * a.gz;
   std::vector<int> bin_of((size_t)n_blobs), count((size_t)nbins + 1, 0);
@@ -163,6 +207,18 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
       x[0] = X[0] + coef[0] * sin(w * X[1]);
       x[1] = X[1] + coef[0] * sin(w * X[2]);
       x[2] = X[2] + coef[0] * sin(w * X[0]);
+    } else if (deform == 3) {
+      const double *E = coef + 3;
+      for (int i = 0; i < 3; i++)
+        x[i] = X[i] + coef[i] + E[i * 3 + 0] * (X[0] - coef[12]) + E[i * 3 + 1] * (X[1] - coef[13]) +
+               E[i * 3 + 2] * (X[2] - coef[14]);
+      for (int q = 0; q < (int)coef[15]; q++) {
+        const double *bp = coef + 16 + 7 * q;
+        const double d2 = (X[0] - bp[0]) * (X[0] - bp[0]) + (X[1] - bp[1]) * (X[1] - bp[1]) +
+                          (X[2] - bp[2]) * (X[2] - bp[2]);
+        const double g = exp(-d2 / (2.0 * bp[3] * bp[3]));
+        for (int i = 0; i < 3; i++) x[i] += bp[4 + i] * g;
+      }
     }
     int bx = std::min(std::max((int)floor(x[0] / kBin), 0), a.gx - 1);
     int by = std::min(std::max((int)floor(x[1] / kBin), 0), a.gy - 1);

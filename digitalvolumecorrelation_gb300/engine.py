@@ -16,8 +16,8 @@ import os
 
 import numpy as np
 
-from .abi import (DvcParams, DvcStats, E_RANGE, OK, SEED_GIVEN, SEED_NEIGHBOURS, SEED_RIGID,
-                  make_params)
+from .abi import (DvcParams, DvcStats, E_RANGE, OK, SEED_GIVEN, SEED_NEIGHBOURS, SEED_PARAMS,
+                  SEED_RIGID, make_params)
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "lib", "libdvcgpu.so")
@@ -62,6 +62,20 @@ def load(path: str | None = None):
     L.dvc_gpu_objective.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp]
     L.dvc_gpu_strain.argtypes = [C.c_int, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double,
                                  C.c_int, C.c_int, _dp, _ip, _dp, _dp, _dp, _dp]
+    L.dvc_cnn_create.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
+    L.dvc_cnn_destroy.argtypes = [C.c_void_p]
+    L.dvc_cnn_destroy.restype = None
+    L.dvc_cnn_get_weights.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int]
+    L.dvc_cnn_set_weights.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int]
+    L.dvc_cnn_patches.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.dvc_cnn_forward.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.dvc_cnn_gradients.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float)]
+    L.dvc_cnn_train_step.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_float,
+                                     C.POINTER(C.c_float)]
+    L.dvc_gpu_process_learned.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                          C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.POINTER(C.c_int), C.c_void_p]
     L.dvc_gpu_synth_volume.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.POINTER(C.c_float), C.c_int, _dp, C.c_float, C.c_float,
                                        C.c_ulonglong, C.c_float, C.c_void_p]
@@ -124,7 +138,7 @@ class Engine:
             nn = neigh.shape[1]
             neigh_p = _p(neigh, _ip)
         seeds_p = None
-        if seed_mode == SEED_GIVEN:
+        if seed_mode in (SEED_GIVEN, SEED_PARAMS):
             seeds = np.ascontiguousarray(seeds, np.float64)
             seeds_p = _p(seeds, _dp)
         status = np.zeros(n, np.int32)
@@ -148,6 +162,18 @@ class Engine:
                                            int(seed_mode), ptr(seeds_dev), ptr(status_dev),
                                            ptr(objmin_dev), ptr(params_dev), ptr(gn_iters_dev),
                                            C.c_void_p(stream)))
+
+    def process_learned(self, net, n_points, points_dev, order_dev, n_process, obj_threshold,
+                        status_dev, objmin_dev, params_dev, gn_iters_dev=None, stream=0):
+        """The learned search (dvc_gpu_process_learned); returns the number of
+        points searched again by the plain method."""
+        ptr = lambda t: C.c_void_p(_dev_ptr(t)) if t is not None else None
+        nfb = C.c_int(0)
+        _check(_lib.dvc_gpu_process_learned(self._h, net._h, int(n_points), ptr(points_dev),
+                                            int(n_process), ptr(order_dev), float(obj_threshold),
+                                            ptr(status_dev), ptr(objmin_dev), ptr(params_dev),
+                                            ptr(gn_iters_dev), C.byref(nfb), C.c_void_p(stream)))
+        return nfb.value
 
     def last_counters(self):
         """(evaluations, Gauss-Newton iterations, undefined-cell evaluations)
@@ -175,6 +201,62 @@ class Engine:
             return None
         _check(rc)
         return out
+
+
+class Cnn:
+    """The learned initial-guess network (dvc_cnn_* of dvc_gpu.h)."""
+
+    def __init__(self, seed=1):
+        L = load()
+        self._h = C.c_void_p()
+        _check(L.dvc_cnn_create(C.byref(self._h), int(seed)))
+        self.n_params = L.dvc_cnn_param_count()
+
+    def close(self):
+        if self._h:
+            _lib.dvc_cnn_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_weights(self):
+        w = np.zeros(self.n_params, np.float32)
+        _check(_lib.dvc_cnn_get_weights(self._h, w.ctypes.data_as(C.POINTER(C.c_float)), self.n_params))
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        _check(_lib.dvc_cnn_set_weights(self._h, w.ctypes.data_as(C.POINTER(C.c_float)), len(w)))
+
+    @staticmethod
+    def patches(engine, n, points_dev, patches_dev, idx_dev=None, stream=0):
+        """[n][2][32][32][32] patches of an engine's volume pair (device)."""
+        load()
+        _check(_lib.dvc_cnn_patches(engine._h, int(n), C.c_void_p(_dev_ptr(points_dev)),
+                                    C.c_void_p(_dev_ptr(idx_dev)) if idx_dev is not None else None,
+                                    C.c_void_p(_dev_ptr(patches_dev)), C.c_void_p(stream)))
+
+    def forward(self, batch, patches_dev, out_dev, stream=0):
+        _check(_lib.dvc_cnn_forward(self._h, int(batch), C.c_void_p(_dev_ptr(patches_dev)),
+                                    C.c_void_p(_dev_ptr(out_dev)), C.c_void_p(stream)))
+
+    def gradients(self, batch, patches_dev, targets_dev):
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_float(0.0)
+        _check(_lib.dvc_cnn_gradients(self._h, int(batch), C.c_void_p(_dev_ptr(patches_dev)),
+                                      C.c_void_p(_dev_ptr(targets_dev)),
+                                      g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)))
+        return g, loss.value
+
+    def train_step(self, batch, patches_dev, targets_dev, lr):
+        loss = C.c_float(0.0)
+        _check(_lib.dvc_cnn_train_step(self._h, int(batch), C.c_void_p(_dev_ptr(patches_dev)),
+                                       C.c_void_p(_dev_ptr(targets_dev)), float(lr), C.byref(loss)))
+        return loss.value
 
 
 def _dev_ptr(t):
@@ -229,5 +311,5 @@ def synth_volume_device(vol_dev, shape_xyz, bytes_per_voxel, blobs, deform=None,
                                      C.c_void_p(stream)))
 
 
-__all__ = ["Engine", "objective", "strain", "synth_volume_device", "make_params", "load",
-           "DvcError", "SEED_NEIGHBOURS", "SEED_GIVEN", "SEED_RIGID"]
+__all__ = ["Engine", "Cnn", "objective", "strain", "synth_volume_device", "make_params", "load",
+           "DvcError", "SEED_NEIGHBOURS", "SEED_GIVEN", "SEED_RIGID", "SEED_PARAMS"]

@@ -68,6 +68,53 @@ class Sinusoid:
 
 
 @dataclass
+class Bumps:
+    """u(X) = t + E (X - c) + sum_k a_k exp(-|X - p_k|^2 / (2 s_k^2)): a smooth
+    affine field with Gaussian bumps (rows of `bumps`: px, py, pz, s, ax, ay, az)."""
+    t: tuple = (0.0, 0.0, 0.0)
+    E: tuple = ((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+    c: tuple = (0.0, 0.0, 0.0)
+    bumps: tuple = ()
+
+    def u(self, X):
+        X = np.asarray(X, dtype=np.float64)
+        out = np.asarray(self.t) + (X - np.asarray(self.c)) @ np.asarray(self.E).T
+        for px, py, pz, s, ax, ay, az in self.bumps:
+            d2 = np.sum((X - np.array([px, py, pz])) ** 2, axis=-1)
+            out = out + np.exp(-d2 / (2.0 * s * s))[..., None] * np.array([ax, ay, az])
+        return out
+
+    def inverse(self, x, iters: int = 12):
+        x = np.asarray(x, np.float64)
+        X = x.copy()
+        for _ in range(iters):
+            X = x - self.u(X)
+        return X
+
+    def coef(self):
+        out = [*self.t, *np.asarray(self.E).ravel(), *self.c, float(len(self.bumps))]
+        for b in self.bumps:
+            out += list(map(float, b))
+        return out
+
+    kind = 3
+
+
+def random_bumps(shape_xyz, rng, max_disp=10.0, max_strain=0.02, n_bumps=12):
+    """A random smooth field with |u| <= max_disp and |grad u| <~ max_strain:
+    a translation, a uniform strain about the centre and Gaussian bumps."""
+    c = np.asarray(shape_xyz, np.float64) / 2.0
+    E = rng.uniform(-max_strain / 2, max_strain / 2, (3, 3))
+    t = rng.uniform(-max_disp / 3, max_disp / 3, 3)
+    b = []
+    for _ in range(n_bumps):
+        s = rng.uniform(48.0, 96.0)
+        amp = rng.uniform(-1.0, 1.0, 3) * min(max_disp / 6, max_strain * s)
+        b.append((*rng.uniform(0, shape_xyz), s, *amp))
+    return Bumps(t=tuple(t), E=tuple(map(tuple, E)), c=tuple(c), bumps=tuple(b))
+
+
+@dataclass
 class Identity:
     def u(self, X):
         return np.zeros_like(np.asarray(X, np.float64))

@@ -58,7 +58,12 @@ enum dvc_seed_mode {
   /* caller supplies one (u,v,w) seed per point; points are independent */
   DVC_SEED_GIVEN = 1,
   /* every point starts from rigid_trans; points are independent */
-  DVC_SEED_RIGID = 2
+  DVC_SEED_RIGID = 2,
+  /* caller supplies all 12 start parameters per point (u v w phi the psi exx
+     eyy ezz exy eyz exz, the first num_srch_dof used): the start estimate and
+     the coarse grid are skipped, Gauss-Newton starts there. The learned
+     proposer's mode (dvc_gpu_process_learned); points are independent. */
+  DVC_SEED_PARAMS = 3
 };
 
 /* Search configuration: the `dvc` input-file keys that shape the hot path
@@ -189,6 +194,46 @@ int dvc_gpu_last_counters(dvc_engine *e, long long out[3]);
    counterpart in the reference (it has no per-phase timing). */
 #define DVC_N_PHASES 11
 int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]);
+
+/* ---- learned initial guess (no counterpart in the reference) ------------
+ * A small 3D CNN proposes each point's start parameters from its reference
+ * and correlate patches (32^3 voxels centred on the point, each normalised to
+ * zero mean and unit variance), in place of Search::starting_param and
+ * trgrid_global (Core/Search.cpp:277-377,934-1043). Conv 2->16->32->64->96
+ * (3^3, stride 2, ReLU), dense 768->128 (ReLU) ->12; outputs are the
+ * parameters divided by fixed scales (translations 10 voxels, rotations
+ * 0.05 rad, strains 0.02). FP32 weights; training by mean squared error and
+ * Adam, all on the GPU. */
+typedef struct dvc_cnn dvc_cnn;
+int dvc_cnn_create(dvc_cnn **out, unsigned seed);  /* He-normal initial weights */
+void dvc_cnn_destroy(dvc_cnn *net);
+int dvc_cnn_param_count(void);
+int dvc_cnn_get_weights(dvc_cnn *net, float *host, int n);
+int dvc_cnn_set_weights(dvc_cnn *net, const float *host, int n); /* resets the optimizer */
+/* patches of points idx[0..n) (all points if idx is NULL) of the engine's
+   volume pair: patches_dev [n][2][32][32][32] FP32 (reference, correlate) */
+int dvc_cnn_patches(dvc_engine *e, int n, const double *points_dev, const int *idx_dev,
+                    float *patches_dev, void *stream);
+/* network outputs (scaled parameters) [batch][12] */
+int dvc_cnn_forward(dvc_cnn *net, int batch, const float *patches_dev, float *out_dev, void *stream);
+/* loss (mean squared error of the scaled outputs against targets [batch][12],
+   raw parameters, FP32) and its gradient w.r.t. every weight (grad_host may be
+   NULL); no update */
+int dvc_cnn_gradients(dvc_cnn *net, int batch, const float *patches_dev, const float *targets_dev,
+                      float *grad_host, float *loss);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) at learning rate lr */
+int dvc_cnn_train_step(dvc_cnn *net, int batch, const float *patches_dev, const float *targets_dev,
+                       float lr, float *loss);
+/* The learned search: the network's start parameters for every point in
+   `order`, Gauss-Newton from there (DVC_SEED_PARAMS), then, for the points
+   whose search failed or whose objective exceeds obj_threshold, the plain
+   search (coarse grid + Gauss-Newton) seeded with the network's translation.
+   Device arrays as in dvc_gpu_process_device; *n_fallback (host) receives the
+   number of points searched again. Synchronises the stream. */
+int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const double *points_dev,
+                            int n_process, const int *order_dev, double obj_threshold,
+                            int *status_dev, double *objmin_dev, double *params_dev,
+                            int *gn_iters_dev, int *n_fallback, void *stream);
 
 /* ---- function-level entry points ----------------------------------------
  * Interpolate one volume (0 = reference, 1 = correlate) at n points, with the

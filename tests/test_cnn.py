@@ -1,0 +1,179 @@
+"""The learned initial-guess network (dvc_cnn_*) and the learned search.
+
+The network has no counterpart in the reference. Its FP64 oracle
+(oracle/cnn_oracle.py) is pinned by a finite-difference check of its own
+gradients (CPU); the GPU's patches, outputs and every weight gradient are
+checked against the oracle (GPU); training must reduce the loss; and the
+learned search (network start + Gauss-Newton + plain-search fallback) must
+agree with the plain search.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import cnn_oracle as O
+
+
+def test_oracle_gradients_by_finite_differences():
+    rng = np.random.default_rng(0)
+    lay, total = O.layout()
+    p = np.zeros(total)
+    for shape, w, b in lay:
+        fan_in = int(np.prod(shape[1:]))
+        p[w:w + int(np.prod(shape))] = rng.normal(0, np.sqrt(2.0 / fan_in), int(np.prod(shape)))
+        p[b:b + shape[0]] = rng.normal(0, 0.05, shape[0])
+    x = rng.normal(0, 1, (2, 2, 32, 32, 32))
+    t = rng.normal(0, 1, (2, 12)) * O.SCALE
+    loss, g = O.loss_and_grad(p, x, t)
+    h = 1e-6
+    checked = 0
+    for shape, w, b in lay:  # a few weights and a bias of every layer
+        for i in list(rng.choice(int(np.prod(shape)), 3, replace=False) + w) + [b]:
+            pp, pm = p.copy(), p.copy()
+            pp[i] += h
+            pm[i] -= h
+            fd = (O.loss_and_grad(pp, x, t)[0] - O.loss_and_grad(pm, x, t)[0]) / (2 * h)
+            assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])
+            checked += 1
+    assert checked == 24
+
+
+def _volumes(shape=(64, 64, 64), bpv=1):
+    from digitalvolumecorrelation_gb300 import synth
+    amp = (40.0, 200.0) if bpv == 1 else (2000.0, 60000.0)
+    b = synth.blobs(shape, 260, amp=amp, seed=41)
+    aff = synth.Affine(t=(1.2, -0.7, 0.5), E=((0.004, 0, 0), (0, -0.003, 0), (0, 0, 0.002)),
+                       c=tuple(s / 2 for s in shape))
+    dt = np.uint8 if bpv == 1 else np.uint16
+    ns = 2.0 if bpv == 1 else 150.0
+    ref = synth.render(shape, b, noise_sigma=ns, noise_seed=42, dtype=dt)
+    cor = synth.render(shape, b, deform=aff, noise_sigma=ns, noise_seed=43, dtype=dt)
+    return ref, cor, aff
+
+
+def _he_weights(seed):
+    rng = np.random.default_rng(seed)
+    lay, total = O.layout()
+    p = np.zeros(total, np.float32)
+    for shape, w, b in lay:
+        fan_in = int(np.prod(shape[1:]))
+        p[w:w + int(np.prod(shape))] = rng.normal(0, np.sqrt(2.0 / fan_in), int(np.prod(shape)))
+        p[b:b + shape[0]] = rng.normal(0, 0.05, shape[0])
+    return p
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bpv", [1, 2])
+def test_patches_vs_oracle(bpv):
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    from digitalvolumecorrelation_gb300.abi import make_params
+    ref, cor, _ = _volumes(bpv=bpv)
+    E = engine.Engine(make_params((64, 64, 64), bytes_per_voxel=bpv, subvol_size=11, subvol_npts=200,
+                                  disp_max=3), ref, cor)
+    pts = np.array([[32.0, 32.0, 32.0], [10.4, 50.6, 31.5], [3.0, 61.0, 60.2], [40.2, 20.7, 8.9]])
+    pd = torch.from_numpy(pts).cuda()
+    out = torch.zeros((len(pts), 2, 32, 32, 32), dtype=torch.float32, device="cuda")
+    engine.Cnn.patches(E, len(pts), pd, out)
+    got = out.cpu().numpy()
+    for i, p in enumerate(pts):
+        np.testing.assert_allclose(got[i, 0], O.patch(ref, p), atol=2e-4)
+        np.testing.assert_allclose(got[i, 1], O.patch(cor, p), atol=2e-4)
+    E.close()
+
+
+@pytest.mark.gpu
+def test_forward_and_gradients_vs_oracle():
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    rng = np.random.default_rng(3)
+    ref, cor, aff = _volumes()
+    x = np.stack([np.stack([O.patch(ref, p), O.patch(cor, p)])
+                  for p in rng.uniform(16, 48, (3, 3))]).astype(np.float32)
+    t = (rng.normal(0, 1, (3, 12)) * O.SCALE).astype(np.float32)
+    p = _he_weights(5)
+    net = engine.Cnn(seed=1)
+    net.set_weights(p)
+    xd = torch.from_numpy(x).cuda()
+    td = torch.from_numpy(t).cuda()
+    y = torch.zeros((3, 12), dtype=torch.float32, device="cuda")
+    net.forward(3, xd, y)
+    y_ref, _, _, _ = O.forward(p.astype(np.float64), x)
+    np.testing.assert_allclose(y.cpu().numpy(), y_ref, rtol=1e-4, atol=1e-4 * np.abs(y_ref).max())
+    g, loss = net.gradients(3, xd, td)
+    loss_ref, g_ref = O.loss_and_grad(p.astype(np.float64), x, t)
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    lay, _ = O.layout()
+    for shape, w, b in lay:  # every layer's weights and biases
+        for lo, n in ((w, int(np.prod(shape))), (b, shape[0])):
+            a, r = g[lo:lo + n], g_ref[lo:lo + n]
+            scale = np.abs(r).max()
+            assert np.abs(a - r).max() <= 1e-3 * scale + 1e-9, (shape, np.abs(a - r).max(), scale)
+    net.close()
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss():
+    """Adam on patches of an affine pair with their true (u, v, w) as targets."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    from digitalvolumecorrelation_gb300.abi import make_params
+    ref, cor, aff = _volumes()
+    E = engine.Engine(make_params((64, 64, 64), subvol_size=11, subvol_npts=200, disp_max=3), ref, cor)
+    rng = np.random.default_rng(8)
+    pts = rng.uniform(14, 50, (64, 3))
+    tgt = np.zeros((64, 12), np.float32)
+    tgt[:, :3] = aff.u(pts)
+    pd = torch.from_numpy(pts).cuda()
+    x = torch.zeros((64, 2, 32, 32, 32), dtype=torch.float32, device="cuda")
+    engine.Cnn.patches(E, 64, pd, x)
+    td = torch.from_numpy(tgt).cuda()
+    net = engine.Cnn(seed=2)
+    first = net.train_step(64, x, td, 1e-3)
+    for _ in range(150):
+        last = net.train_step(64, x, td, 1e-3)
+    assert last < 0.2 * first, (first, last)
+    net.close()
+    E.close()
+
+
+@pytest.mark.gpu
+def test_learned_search_and_fallback():
+    """A network with zero weights proposes zero start parameters. Every point
+    falling back (threshold -1) must give exactly the plain search seeded at
+    zero (the rigid seed); with a real threshold the converged points agree
+    with it within 0.01 voxel."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    from digitalvolumecorrelation_gb300.abi import make_params
+    from digitalvolumecorrelation_gb300 import synth
+    ref, cor, aff = _volumes()
+    p = make_params((64, 64, 64), subvol_geom="cube", subvol_size=13, subvol_npts=400, num_srch_dof=6,
+                    disp_max=3, basin_radius=1.5)
+    E = engine.Engine(p, ref, cor)
+    pts = synth.grid_points((3, 3, 3), 7.0, (32.0, 32.0, 32.0))
+    n = len(pts)
+    plain = E.process(pts, seed_mode=engine.SEED_RIGID)
+    net = engine.Cnn(seed=3)
+    net.set_weights(np.zeros(net.n_params, np.float32))
+    dev = "cuda"
+    pd = torch.from_numpy(pts).to(dev)
+    od = torch.arange(n, dtype=torch.int32, device=dev)
+    for thr, exact in ((-1.0, True), (0.1, False)):
+        st = torch.empty(n, dtype=torch.int32, device=dev)
+        ob = torch.empty(n, dtype=torch.float64, device=dev)
+        pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
+        nfb = E.process_learned(net, n, pd, od, n, thr, st, ob, pa)
+        s, o, q = st.cpu().numpy(), ob.cpu().numpy(), pa.cpu().numpy()
+        good = (s == 0) & (plain["status"] == 0)
+        if exact:
+            assert nfb == n
+            np.testing.assert_array_equal(s, plain["status"])
+            np.testing.assert_array_equal(q, plain["params"])
+            np.testing.assert_array_equal(o, plain["objmin"])
+        else:
+            assert good.sum() >= n - 2
+            assert np.abs(q[good, :3] - plain["params"][good, :3]).max() <= 0.01
+    net.close()
+    E.close()

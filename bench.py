@@ -52,6 +52,9 @@ def parse():
                          "configuration's subvolumes and search on 384^3 uint16 volumes, "
                          "216 points with given seeds")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-initial-guess comparison (configuration 4)")
+    ap.add_argument("--learned-steps", type=int, default=3000)
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -306,10 +309,41 @@ def main():
                                   "sample": f"{len(sample)} points of the same workload (evenly "
                                             "spaced in processing order) with the GPU run's seeds",
                                   "max_abs_du_gpu_vs_oracle_vox": err}
+    if rank == 0 and not args.no_learned and world == 1:
+        result["learned"] = learned_leg(args.learned_steps)
     if rank == 0:
         print(json.dumps(result))
     if world > 1:
         dist.destroy_process_group()
+
+
+def learned_leg(steps, oracle_sample=32):
+    """Configuration 4: the learned initial guess trained on the GPU, then the
+    plain and the learned method on a held-out pair, both checked against the
+    FP64 oracle on a sample of points (from the true translation, no grid:
+    the converged optimum)."""
+    from digitalvolumecorrelation_gb300 import learned
+    from digitalvolumecorrelation_gb300.abi import make_params
+    from oracle.oracle import Oracle
+    summary, held, res = learned.run(steps=steps, keep=True)
+    rng = np.random.default_rng(5)
+    n = len(held.points)
+    sample = np.sort(rng.choice(n, oracle_sample, replace=False))
+    shape = learned.SHAPE
+    ref = held.ref[: held.w.nvox].cpu().numpy().reshape(shape[::-1])
+    cor = held.cor[: held.w.nvox].cpu().numpy().reshape(shape[::-1])
+    p0 = make_params(shape, **dict(learned.SEARCH, basin_radius=0.0))
+    o = Oracle().process(p0, ref, cor, held.points[sample], seed_mode=1, seeds=held.truth[sample],
+                         n_threads=os.cpu_count() or 1)
+    ok = o["status"] == 0
+    for name in ("plain", "learned"):
+        st, pa = res[name]
+        good = ok & (st[sample] == 0)
+        err = np.abs(pa[sample][good, :3] - o["params"][good, :3]).max(axis=1)
+        summary[name]["oracle_sample"] = int(ok.sum())
+        summary[name]["within_0p01_vox_of_oracle"] = float(np.mean(err <= 0.01)) if len(err) else None
+        summary[name]["max_err_vs_oracle_vox"] = float(err.max()) if len(err) else None
+    return summary
 
 
 def e2e_leg(W, p, order, neigh, ref_d, cor_d, n):

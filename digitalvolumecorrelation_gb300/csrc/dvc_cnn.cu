@@ -63,39 +63,54 @@ struct Layout {
 const Layout kLay;
 
 // ------------------------------------------------------------- kernels ---
-// conv forward: one thread per output (b, co, z, y, x); ReLU
-__global__ void conv_fwd(const float *__restrict__ in, const float *__restrict__ w,
-                         const float *__restrict__ bias, float *__restrict__ out, int B, int Cin,
-                         int Cout, int Din) {
-  const int Do = Din / 2, n3 = Do * Do * Do;
-  const long long total = (long long)B * Cout * n3;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int o = (int)(t % n3);
-    const int co = (int)((t / n3) % Cout);
-    const int b = (int)(t / ((long long)n3 * Cout));
-    const int ox = o % Do, oy = (o / Do) % Do, oz = o / (Do * Do);
-    float acc = bias[co];
-    const float *wc = w + (size_t)co * Cin * 27;
-    for (int ci = 0; ci < Cin; ci++) {
-      const float *ib = in + ((size_t)b * Cin + ci) * Din * Din * Din;
-      const float *wk = wc + ci * 27;
-      for (int kz = 0; kz < 3; kz++) {
-        const int iz = 2 * oz - 1 + kz;
-        if (iz < 0 || iz >= Din) continue;
-        for (int ky = 0; ky < 3; ky++) {
-          const int iy = 2 * oy - 1 + ky;
-          if (iy < 0 || iy >= Din) continue;
-          for (int kx = 0; kx < 3; kx++) {
-            const int ix = 2 * ox - 1 + kx;
-            if (ix < 0 || ix >= Din) continue;
-            acc = fmaf(wk[(kz * 3 + ky) * 3 + kx], ib[((size_t)iz * Din + iy) * Din + ix], acc);
-          }
-        }
-      }
-    }
-    out[t] = fmaxf(acc, 0.f);
+// conv forward, register-blocked: each thread computes one output voxel of
+// one sample for 8 consecutive output channels; the block's 8 channels of
+// weights sit in shared memory as [ci][tap][8] (two 16-byte loads per tap,
+// the same address for every lane). blockIdx.y = channel group.
+constexpr int kCoG = 8;
+__global__ void __launch_bounds__(256) conv_fwd8(const float *__restrict__ in, const float *__restrict__ w,
+                                                 const float *__restrict__ bias, float *__restrict__ out, int B,
+                                                 int Cin, int Cout, int Din) {
+  extern __shared__ float4 sw4[];  // [Cin * 27][2]
+  const int Do = Din / 2, n3 = Do * Do * Do, din3 = Din * Din * Din;
+  const int co0 = blockIdx.y * kCoG;
+  float *sw = reinterpret_cast<float *>(sw4);
+  for (int e = threadIdx.x; e < Cin * 27 * kCoG; e += blockDim.x) {
+    const int c = e % kCoG, ck = e / kCoG;  // ck = ci * 27 + k
+    sw[e] = w[((size_t)(co0 + c) * Cin) * 27 + ck];
   }
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)B * n3) return;
+  const int o = (int)(t % n3), b = (int)(t / n3);
+  const int ox = o % Do, oy = (o / Do) % Do, oz = o / (Do * Do);
+  float acc[kCoG];
+#pragma unroll
+  for (int c = 0; c < kCoG; c++) acc[c] = bias[co0 + c];
+  // taps inside the volume (padding 1): ranges per axis
+  const int z0 = 2 * oz - 1, y0 = 2 * oy - 1, x0 = 2 * ox - 1;
+  for (int ci = 0; ci < Cin; ci++) {
+    const float *ib = in + ((size_t)b * Cin + ci) * din3;
+    const float4 *wk = sw4 + (size_t)ci * 27 * 2;
+#pragma unroll
+    for (int k = 0; k < 27; k++) {
+      const int kx = k % 3, ky = (k / 3) % 3, kz = k / 9;
+      const int iz = z0 + kz, iy = y0 + ky, ix = x0 + kx;
+      if (iz < 0 || iy < 0 || ix < 0 || iz >= Din || iy >= Din || ix >= Din) continue;
+      const float v = ib[((size_t)iz * Din + iy) * Din + ix];
+      const float4 wa = wk[2 * k], wb = wk[2 * k + 1];
+      acc[0] = fmaf(wa.x, v, acc[0]);
+      acc[1] = fmaf(wa.y, v, acc[1]);
+      acc[2] = fmaf(wa.z, v, acc[2]);
+      acc[3] = fmaf(wa.w, v, acc[3]);
+      acc[4] = fmaf(wb.x, v, acc[4]);
+      acc[5] = fmaf(wb.y, v, acc[5]);
+      acc[6] = fmaf(wb.z, v, acc[6]);
+      acc[7] = fmaf(wb.w, v, acc[7]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < kCoG; c++) out[((size_t)b * Cout + co0 + c) * n3 + o] = fmaxf(acc[c], 0.f);
 }
 
 // gradient w.r.t. the conv input activation, times the input's ReLU mask:
@@ -376,8 +391,10 @@ Scales scales() {
 void forward(dvc_cnn *c, int B, cudaStream_t st) {
   for (int l = 0; l < kNL; l++) {
     const int Do = kDin[l] / 2;
-    conv_fwd<<<grid_for((long long)B * kCout[l] * Do * Do * Do), 256, 0, st>>>(
-        c->act[l], c->p + kLay.w[l], c->p + kLay.b[l], c->act[l + 1], B, kCin[l], kCout[l], kDin[l]);
+    const size_t smem = (size_t)kCin[l] * 27 * kCoG * 4;
+    const dim3 grid((unsigned)(((long long)B * Do * Do * Do + 255) / 256), (unsigned)(kCout[l] / kCoG));
+    conv_fwd8<<<grid, 256, smem, st>>>(c->act[l], c->p + kLay.w[l], c->p + kLay.b[l], c->act[l + 1], B,
+                                       kCin[l], kCout[l], kDin[l]);
   }
   fc_fwd<<<(B * kF1 + 255) / 256, 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL], c->p + kLay.b[kNL],
                                                 c->act[kNL + 1], B, kF0, kF1, 1);
@@ -420,6 +437,11 @@ int dvc_cnn_param_count(void) { return (int)kLay.total; }
 
 int dvc_cnn_create(dvc_cnn **out, unsigned seed) {
   if (!out) return dvc_internal_set_error(DVC_E_ARG, "null argument");
+  // the largest layer's weight group (64 x 27 x 8 floats) exceeds the default
+  // 48 KB of dynamic shared memory
+  if (cudaFuncSetAttribute(conv_fwd8, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kCin[kNL - 1] * 27 * kCoG * 4) != cudaSuccess)
+    return dvc_internal_set_error(DVC_E_CUDA, "conv kernel attribute");
   dvc_cnn *c = new dvc_cnn();
   const size_t n = kLay.total;
   if (cudaMalloc(&c->p, n * 4) != cudaSuccess || cudaMalloc(&c->g, n * 4) != cudaSuccess ||
@@ -545,7 +567,7 @@ int dvc_internal_patches(const void *ref, const void *cor, int bpv, int nx, int 
 int dvc_internal_cnn_seed(dvc_cnn *c, const void *ref, const void *cor, int bpv, int nx, int ny,
                           int nz, int n, const double *pts_dev, const int *idx_dev, double *params_dev,
                           cudaStream_t st) {
-  const int B = 256;
+  const int B = 1024;
   int rc = ensure_batch(c, B);
   if (rc) return rc;
   for (int r0 = 0; r0 < n; r0 += B) {

@@ -10,7 +10,10 @@
 //    (Core/Search.cpp:100-110), which no two runs reproduce;
 //  * `.disp` rows are written once, after the search (the reference appends
 //    each row as it goes, then rewrites the file in the same order);
-//  * a file name may end its line (the reference needs a tab after it).
+//  * a file name may end its line (the reference needs a tab after it);
+//  * with DVC_GPU_NEIGHBOURS set, order and neighbour lists come from the GPU
+//    (same distances, ties by point index instead of std::sort's order).
+#include <algorithm>
 #include <chrono>
 #include <cstdlib>
 #include <ctime>
@@ -95,7 +98,20 @@ int main(int argc, char *argv[]) {
   // distances NaN when it is absent, and the order is std::sort's)
   std::vector<int> order;
   std::vector<std::vector<int>> neigh;
-  order_neighbours(pts, run.starting_point, 75, order, neigh);
+  if (std::getenv("DVC_GPU_NEIGHBOURS")) {
+    // the GPU path: same distances, ties by point index
+    const int kk = std::min(75, n);
+    std::vector<int> flat((size_t)n * kk);
+    order.resize((size_t)n);
+    if (dvc_gpu_order_neighbours(n, pts.data(), run.starting_point, 75, order.data(), flat.data()) != DVC_OK) {
+      std::cout << "\nNeighbour search on the GPU failed: " << dvc_gpu_last_error() << "\n\n";
+      return 0;
+    }
+    neigh.assign((size_t)n, std::vector<int>());
+    for (int i = 0; i < n; i++) neigh[(size_t)i].assign(flat.begin() + (size_t)i * kk, flat.begin() + (size_t)(i + 1) * kk);
+  } else {
+    order_neighbours(pts, run.starting_point, 75, order, neigh);
+  }
   std::cout << "sorting finished" << std::endl;
   write_sort_csv(run.pts_fname, neigh);
 

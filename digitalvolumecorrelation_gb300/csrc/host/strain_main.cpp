@@ -3,6 +3,7 @@
 // `strain` (Core/strain.cpp:166-661); the per-point strain-window fits run on
 // the GPU (dvc_gpu_strain, FP64).
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <fstream>
 #include <iostream>
@@ -159,7 +160,20 @@ int main(int argc, char *argv[]) {
   if (!sort_read) {
     std::cout << "-> creating a new sort file: " << base + ".sort.csv" << std::endl;
     std::vector<int> order;
-    order_neighbours(pts, &pts[0], kNdpMax, order, neigh);
+    if (std::getenv("DVC_GPU_NEIGHBOURS")) {  // GPU path: ties by point index
+      const int kk = std::min(kNdpMax, n);
+      std::vector<int> flat((size_t)n * kk);
+      order.resize((size_t)n);
+      if (dvc_gpu_order_neighbours(n, pts.data(), &pts[0], kNdpMax, order.data(), flat.data()) != DVC_OK) {
+        std::cout << "-> neighbour search on the GPU failed: " << dvc_gpu_last_error() << std::endl;
+        return 0;
+      }
+      neigh.assign((size_t)n, std::vector<int>());
+      for (int i = 0; i < n; i++)
+        neigh[(size_t)i].assign(flat.begin() + (size_t)i * kk, flat.begin() + (size_t)(i + 1) * kk);
+    } else {
+      order_neighbours(pts, &pts[0], kNdpMax, order, neigh);
+    }
     std::cout << "sorting finished" << std::endl;
     write_sort_csv(base, neigh);
   }

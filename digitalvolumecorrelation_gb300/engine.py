@@ -76,6 +76,7 @@ def load(path: str | None = None):
     L.dvc_gpu_process_learned.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                           C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.POINTER(C.c_int), C.c_void_p]
+    L.dvc_gpu_order_neighbours.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip]
     L.dvc_gpu_synth_volume.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.POINTER(C.c_float), C.c_int, _dp, C.c_float, C.c_float,
                                        C.c_ulonglong, C.c_float, C.c_void_p]
@@ -296,6 +297,21 @@ def strain(pts, status, objmin, disp, neigh, ndp=25, objt=1.0, refill=False, pla
     return out
 
 
+def order_neighbours(points, start=None, k=75):
+    """Processing order by distance from `start` (default the first point) and
+    the k nearest points of every point, on the GPU (ties by index)."""
+    load()
+    pts = np.ascontiguousarray(points, np.float64)
+    n = len(pts)
+    s = np.ascontiguousarray(pts[0] if start is None else start, np.float64)
+    kk = min(k, n)
+    order = np.zeros(n, np.int32)
+    neigh = np.zeros((n, kk), np.int32)
+    _check(_lib.dvc_gpu_order_neighbours(n, _p(pts, _dp), _p(s, _dp), int(k), _p(order, _ip),
+                                         _p(neigh, _ip)))
+    return order, neigh
+
+
 def synth_volume_device(vol_dev, shape_xyz, bytes_per_voxel, blobs, deform=None,
                         background=0.0, noise_sigma=2.0, noise_seed=1, vmax=None, stream=0):
     """Render a speckle volume into a device buffer (see dvc_gpu_synth_volume)."""
@@ -311,5 +327,5 @@ def synth_volume_device(vol_dev, shape_xyz, bytes_per_voxel, blobs, deform=None,
                                      C.c_void_p(stream)))
 
 
-__all__ = ["Engine", "Cnn", "objective", "strain", "synth_volume_device", "make_params", "load",
+__all__ = ["Engine", "Cnn", "objective", "strain", "order_neighbours", "synth_volume_device", "make_params", "load",
            "DvcError", "SEED_NEIGHBOURS", "SEED_GIVEN", "SEED_RIGID", "SEED_PARAMS"]

@@ -235,6 +235,15 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
                             int *status_dev, double *objmin_dev, double *params_dev,
                             int *gn_iters_dev, int *n_fallback, void *stream);
 
+/* ---- processing order and neighbours on the GPU --------------------------
+ * DataCloud::sort_order_neighbors (Core/DataCloud.cpp:69-144): order[n] the
+ * points by distance from `start`, neigh[n * min(k, n)] each point's k
+ * nearest (itself first), distances bit-identical to the reference's, ties by
+ * point index (the reference's std::sort leaves ties in an order of its own).
+ * Host arrays. */
+int dvc_gpu_order_neighbours(int n, const double *points, const double start[3], int k, int *order,
+                             int *neigh);
+
 /* ---- function-level entry points ----------------------------------------
  * Interpolate one volume (0 = reference, 1 = correlate) at n points, with the
  * interpolation box of this engine's search (Search::Search est_box_nom,

@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-initial-guess comparison (configuration 4)")
     ap.add_argument("--learned-steps", type=int, default=3000)
+    ap.add_argument("--no-batching", action="store_true",
+                    help="skip configuration 3 (60 configurations in one launch)")
+    ap.add_argument("--batching-only", action="store_true",
+                    help="run only the configuration 3 leg and print its JSON")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -191,6 +195,11 @@ def main():
         return run_reference(args, rank, world)
     if args.profile_case:
         return profile_case()
+    if args.batching_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"batching": batching_leg()}))
+        return
 
     import torch
     from digitalvolumecorrelation_gb300 import engine, workloads
@@ -311,6 +320,8 @@ def main():
                                   "max_abs_du_gpu_vs_oracle_vox": err}
     if rank == 0 and not args.no_learned and world == 1:
         result["learned"] = learned_leg(args.learned_steps)
+    if rank == 0 and not args.no_batching and world == 1:
+        result["batching"] = batching_leg()
     if rank == 0:
         print(json.dumps(result))
     if world > 1:
@@ -344,6 +355,132 @@ def learned_leg(steps, oracle_sample=32):
         summary[name]["within_0p01_vox_of_oracle"] = float(np.mean(err <= 0.01)) if len(err) else None
         summary[name]["max_err_vs_oracle_vox"] = float(err.max()) if len(err) else None
     return summary
+
+
+BATCHING_ORACLE_CONFIGS = ((21, "cube", 3, "ssd"), (41, "sphere", 12, "znssd"), (61, "cube", 6, "znssd"),
+                           (81, "sphere", 12, "ssd"))
+
+
+def batching_leg(steps=3, warmup=1, tune_points=4000, oracle_per_config=16):
+    """Configuration 3: 40,000 scattered points, each with its own search
+    configuration (60 in all), searched by one persistent launch of a plan
+    whose launch shape the autotuner picks; the launch is also captured in a
+    CUDA graph and replayed. Neighbour order and lists from the GPU kNN, the
+    strain window (7 points) fitted on the GPU afterwards. A sample of points
+    of four configurations is checked against the FP64 oracle with the seeds
+    those points saw."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine, workloads
+    from digitalvolumecorrelation_gb300.abi import make_params
+    W, cfg, settings = workloads.config3()
+    n = len(W.points)
+    ref_d, cor_d = W.render_device()
+    engines = [engine.Engine(make_params(W.shape, bytes_per_voxel=1, **kw), ref_dev=ref_d, cor_dev=cor_d)
+               for kw in settings]
+    t0 = time.perf_counter()
+    order, neigh = engine.order_neighbours(W.points, start=W.points[0], k=75)
+    knn_s = time.perf_counter() - t0
+    plan = engine.Plan(engines)
+    shape0 = plan.info()
+    dev = torch.device("cuda")
+    t = lambda a, dt=None: torch.as_tensor(a, dtype=dt, device=dev)
+    cfg_d, pts_d, order_d, neigh_d = t(cfg), t(W.points), t(order), t(neigh)
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+    ob = torch.empty(n, dtype=torch.float64, device=dev)
+    pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
+    its = torch.empty(n, dtype=torch.int32, device=dev)
+    # autotune on the first points of the processing order
+    tune = plan.autotune(cfg_d, n, pts_d, order_d, min(tune_points, n), neigh_d, neigh.shape[1],
+                         engine.SEED_NEIGHBOURS, None, st, ob, pa, reps=1)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        plan.process_device(cfg_d, n, pts_d, order_d, n, neigh_d, neigh.shape[1], engine.SEED_NEIGHBOURS,
+                            None, st, ob, pa, its, stream=stream.cuda_stream)
+
+    for _ in range(max(1, warmup)):
+        step()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(steps):
+        step()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    # the same launch captured once in a CUDA graph and replayed
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+            plan.process_device(cfg_d, n, pts_d, order_d, n, neigh_d, neigh.shape[1], engine.SEED_NEIGHBOURS,
+                                None, st, ob, pa, its, stream=side.cuda_stream)
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(steps):
+        g.replay()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_graph = ev0.elapsed_time(ev1) / steps
+    status, objmin, params = st.cpu().numpy(), ob.cpu().numpy(), pa.cpu().numpy()
+    good = status == 0
+    truth = W.truth()
+    # strain window of 7 points over the scattered cloud
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sw = engine.strain(W.points, status, objmin, params[:, :3], neigh, ndp=7)
+    strain_s = time.perf_counter() - t0
+    # oracle sample
+    from oracle.oracle import Oracle
+    O = Oracle()
+    seeds = seeds_from_results(order, neigh, status, params, (0.0, 0.0, 0.0), n)
+    ref_np = ref_d[: W.nvox].cpu().numpy().reshape(W.shape[::-1])
+    cor_np = cor_d[: W.nvox].cpu().numpy().reshape(W.shape[::-1])
+    rank = np.empty(n, np.int64)
+    rank[order] = np.arange(n)
+    errs, same_status, checked, osec = [], 0, 0, 0.0
+    threads = os.cpu_count() or 1
+    for size, geom, dof, obj in BATCHING_ORACLE_CONFIGS:
+        ci = [i for i, kw in enumerate(settings) if (kw["subvol_size"], kw["subvol_geom"], kw["num_srch_dof"],
+                                                      kw["obj_function"]) == (size, geom, dof, obj)][0]
+        members = np.nonzero(cfg == ci)[0]
+        members = members[np.argsort(rank[members])]
+        sel = members[:: max(1, len(members) // oracle_per_config)][:oracle_per_config]
+        p = make_params(W.shape, bytes_per_voxel=1, **settings[ci])
+        t1 = time.perf_counter()
+        o = O.process(p, ref_np, cor_np, W.points[sel], seed_mode=1, seeds=seeds[sel], n_threads=threads)
+        osec += time.perf_counter() - t1
+        checked += len(sel)
+        same_status += int((o["status"] == status[sel]).sum())
+        ok = (o["status"] == 0) & (status[sel] == 0)
+        if ok.any():
+            errs.append(np.abs(o["params"][ok, :3] - params[sel][ok, :3]).max(axis=1))
+    err = np.concatenate(errs) if errs else np.zeros(0)
+    plan_shape = plan.info()
+    plan.close()
+    for E in engines:
+        E.close()
+    return {
+        "workload": W.name, "points": n, "configurations": len(settings),
+        "value": round(n / (ms / 1e3), 2), "unit": "points/s", "ms_per_step": round(ms, 2),
+        "graph_replay": {"value": round(n / (ms_graph / 1e3), 2), "ms_per_step": round(ms_graph, 2)},
+        "launch_shape": plan_shape, "default_shape": shape0,
+        "autotune_ms": {f"C{c}_stage{s_}": round(v, 2) for (c, s_), v in tune.items()},
+        "autotune_sample_points": min(tune_points, n),
+        "seeding": "reference (neighbours, processing order; order and lists from the GPU kNN)",
+        "knn_seconds": round(knn_s, 3), "strain_window": 7, "strain_seconds": round(strain_s, 3),
+        "strain_points_fitted": int((sw["pts_in_sw"] >= 7).sum()),
+        "good": int(good.sum()), "range_fail": int((status == -1).sum()),
+        "convg_fail": int((status == -2).sum()),
+        "median_abs_err_vs_truth_vox": float(np.median(np.abs(params[good, :3] - truth[good]))),
+        "oracle_sample": checked, "oracle_same_status": same_status,
+        "within_0p01_vox_of_oracle": float(np.mean(err <= 0.01)) if len(err) else None,
+        "max_err_vs_oracle_vox": float(err.max()) if len(err) else None,
+        "oracle_points_per_s": round(checked / osec, 3), "oracle_threads": threads,
+    }
 
 
 def e2e_leg(W, p, order, neigh, ref_d, cor_d, n):

@@ -263,6 +263,20 @@ struct dvc_engine {
   int last_cluster = 0, last_grid = 0, last_staged = 0;
 };
 
+// Several configurations on the same volumes, one launch shape for all.
+struct dvc_plan {
+  std::vector<dvc_engine *> cfgs;  // not owned
+  std::vector<SearchCfg> h_cfgs;   // the device table's host copy
+  int cluster = 0;                 // CTAs per point
+  int staging = 1;                 // staging allowed
+  int n_staged = 0;
+  int cap = 0;                     // per-CTA sample capacity (largest over configurations)
+  size_t stage_bytes = 0, smem_dyn = 0;
+  int max_clusters = 0;            // clusters resident at once
+  SearchCfg *d_cfgs = nullptr;     // device: one record per configuration
+  CUtensorMap *d_tmaps = nullptr;  // device: one tensor map per configuration
+};
+
 namespace {
 
 int validate(const dvc_params *p) {
@@ -550,6 +564,239 @@ int dispatch_launch(int bpv, int it, SearchArgs &a, const CUtensorMap &tm, size_
   return launch_search<uint16_t, 0>(a, tm, smem, grid, cluster, st, max_clusters);
 }
 
+// ---- launch preparation ------------------------------------------------------
+// Dynamic shared memory a search CTA may use on the current device: what a
+// block may opt into, less the kernel's static CtaState and a little slack.
+int dyn_budget(size_t *out) {
+  static int optin[64] = {0};
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(DVC_E_ARG, "device index out of range");
+  if (!optin[dev]) CUDA_TRY(cudaDeviceGetAttribute(&optin[dev], cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  *out = (size_t)optin[dev] - sizeof(CtaState) - 1024;
+  return DVC_OK;
+}
+
+// TMA staging of the correlate volume needs 16-byte aligned rows and planes.
+bool tma_layout(const dvc_engine *e) {
+  const dvc_params &p = e->p;
+  const int esize = p.bytes_per_voxel;
+  return encode_tiled_fn() != nullptr && ((size_t)p.vol_wide * esize) % 16 == 0 &&
+         ((size_t)p.vol_wide * p.vol_high * esize) % 16 == 0 && ((uintptr_t)e->cor % 16) == 0 &&
+         !getenv("DVC_NO_STAGE");
+}
+
+// Engine e's settings as one search configuration at cluster width C:
+// subvolume geometry, coarse grid, sample tables, each rank's sample range and
+// the offset extrema over all samples and per rank (the sample clouds'
+// bounding boxes follow from them: FP64 addition of the point is monotone).
+// Staging is left off. Returns the largest per-rank sample count.
+int fill_config(const dvc_engine *e, int C, SearchCfg &k) {
+  const dvc_params &p = e->p;
+  k = SearchCfg{};
+  k.geom = p.subvol_geom;
+  k.ndof = p.num_srch_dof;
+  k.objfcn = p.obj_function;
+  k.n_sub = e->n_sub;
+  k.cube_n = e->cube_n;
+  k.subv_rad = e->subv_rad;
+  for (int d = 0; d < 3; d++) {
+    k.aspect[d] = p.subvol_aspect[d];
+    k.nom_mn[d] = e->nom_mn[d];
+    k.nom_mx[d] = e->nom_mx[d];
+    k.nom_cen[d] = e->nom_cen[d];
+    k.bext[d] = e->bext[d];
+    k.rigid[d] = p.rigid_trans[d];
+  }
+  k.do_grid = p.basin_radius != 0.0;
+  if (k.do_grid) {
+    const double displ_max = p.disp_max;
+    k.num_inc = (int)(displ_max / p.basin_radius);
+    k.inc = displ_max / k.num_inc;
+    k.inc_int = (k.inc == std::floor(k.inc) && k.inc <= 64.0 && !getenv("DVC_GENERAL_GRID")) ? (int)k.inc : 0;
+  }
+  rank_ranges(e->h_offsets, e->morton_rad, C, k.rank_start);
+  k.off_i = e->d_off_i;
+  k.off_f = e->d_off_f;
+  for (int d = 0; d < 3; d++) {
+    k.off_min[d] = 1e300;
+    k.off_max[d] = -1e300;
+  }
+  int cap = 0;
+  for (int r = 0; r < C; r++) {
+    cap = std::max(cap, k.rank_start[r + 1] - k.rank_start[r]);
+    for (int d = 0; d < 3; d++) {
+      double mn = 1e300, mx = -1e300;
+      for (int i = k.rank_start[r]; i < k.rank_start[r + 1]; i++) {
+        mn = std::min(mn, e->h_offsets[(size_t)i * 3 + d]);
+        mx = std::max(mx, e->h_offsets[(size_t)i * 3 + d]);
+      }
+      k.rank_off_min[r][d] = mn;
+      k.rank_off_max[r][d] = mx;
+      k.off_min[d] = std::min(k.off_min[d], mn);
+      k.off_max[d] = std::max(k.off_max[d], mx);
+    }
+  }
+  return cap;
+}
+
+// Staging box of configuration k (filled at width C) when it fits `budget`
+// together with `state` bytes of per-CTA sample state: one region per point
+// covers every grid translation (reach k * inc); odd row pitch (in 16-byte
+// units) first, then the plain one. Returns the staging buffer's bytes, 0
+// when the box does not fit (k then stays unstaged).
+size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, SearchCfg &k) {
+  const dvc_params &p = e->p;
+  const int esize = p.bytes_per_voxel;
+  double reach = 0.0;
+  if (p.basin_radius != 0.0) {
+    const int n = (int)((double)p.disp_max / p.basin_radius);
+    reach = n * ((double)p.disp_max / n);
+  }
+  int stage[3] = {0, 0, 0};
+  size_t bytes = 0;
+  for (int odd = 1; odd >= 0; odd--) {
+    stage_dims(e, C, esize, reach, k.rank_start, odd != 0, stage);
+    bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;
+    if (bytes + state <= budget) break;
+  }
+  if (stage[0] > 256 || stage[1] > 256 || stage[2] > 256 || bytes + state > budget) return 0;
+  k.stage_on = 1;
+  for (int d = 0; d < 3; d++) k.stage[d] = stage[d];
+  k.stage_tx = (unsigned)((size_t)stage[0] * stage[1] * stage[2] * esize);
+  return bytes;
+}
+
+// Tensor map of the correlate volume with configuration k's staging box.
+bool encode_stage_map(const dvc_engine *e, const SearchCfg &k, CUtensorMap *tm) {
+  const dvc_params &p = e->p;
+  const int esize = p.bytes_per_voxel;
+  memset(tm, 0, sizeof *tm);
+  const cuuint64_t gdim[3] = {(cuuint64_t)p.vol_wide, (cuuint64_t)p.vol_high, (cuuint64_t)p.vol_tall};
+  const cuuint64_t gstride[2] = {(cuuint64_t)p.vol_wide * esize, (cuuint64_t)p.vol_wide * p.vol_high * esize};
+  const cuuint32_t box[3] = {(cuuint32_t)k.stage[0], (cuuint32_t)k.stage[1], (cuuint32_t)k.stage[2]};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  return encode_tiled_fn()(tm, esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3,
+                           e->cor, gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// One search call's points, seeds and outputs (device pointers).
+struct RunIO {
+  int n_points;
+  const double *points;
+  int n_process;
+  const int *order;
+  int n_neigh;
+  const int *neigh;
+  int seed_mode;
+  const double *seeds;
+  int *status;
+  double *objmin;
+  double *params;
+  int *gn_iters;
+};
+
+int check_run(const dvc_engine *e, const RunIO &io) {
+  if (!e) return set_error(DVC_E_ARG, "null engine");
+  if (io.n_points < 0 || io.n_process < 0 || io.n_process > io.n_points)
+    return set_error(DVC_E_ARG, "n_process must be in 0..n_points");
+  if (io.seed_mode < 0 || io.seed_mode > 3) return set_error(DVC_E_ARG, "bad seed_mode");
+  if (io.seed_mode == DVC_SEED_NEIGHBOURS && io.n_neigh > 0 && !io.neigh)
+    return set_error(DVC_E_ARG, "neighbour list required");
+  if ((io.seed_mode == DVC_SEED_GIVEN || io.seed_mode == DVC_SEED_PARAMS) && !io.seeds)
+    return set_error(DVC_E_ARG, "seeds required");
+  return DVC_OK;
+}
+
+// The run's scratch and per-call preparation, enqueued on `st`: scratch in
+// engine e's grow-only workspace (or `ws_fixed`), outputs initialised, ranks
+// of the processing order, and with dataflow scheduling the predecessor
+// counts, successor lists and ready queue. Fills the run fields of `a`.
+int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed, SearchArgs &a) {
+  const int n_points = io.n_points, n_process = io.n_process, n_neigh = io.n_neigh;
+  // workspace: done[n], rank[n], counter/error/counters; with dataflow
+  // scheduling also the predecessor counts, successor lists and ready queue
+  const size_t off_done = 0;
+  const size_t off_rank = off_done + (size_t)n_points * 4;
+  const size_t off_ctl = (off_rank + (size_t)n_points * 4 + 255) & ~(size_t)255;
+  const bool dataflow = io.seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !ws_fixed &&
+                        !getenv("DVC_IN_ORDER");
+  const size_t off_pend = off_ctl + 256;
+  const size_t off_soff = off_pend + (size_t)n_points * 4;
+  const size_t off_cursor = off_soff + ((size_t)n_points + 1) * 4;
+  const size_t off_queue = off_cursor + (size_t)n_points * 4;
+  const size_t off_succ = off_queue + (size_t)n_process * 4;
+  const size_t ws_need = dataflow ? off_succ + (size_t)n_process * n_neigh * 4 : off_ctl + 256;
+  char *ws = ws_fixed;
+  if (!ws) {
+    const int rc = ensure_ws(e, ws_need);
+    if (rc) return rc;
+    ws = (char *)e->ws;
+    e->counters_off = off_ctl + 64;
+  }
+  int *done = (int *)(ws + off_done);
+  int *rank = (int *)(ws + off_rank);
+  int *ctl = (int *)(ws + off_ctl);
+  CUDA_TRY(cudaMemsetAsync(ws + off_ctl, 0, 256, st));
+  {
+    const int T = 256;
+    const int G = (n_points + T - 1) / T;
+    init_outputs_kernel<<<G, T, 0, st>>>(n_points, io.status, io.objmin, io.params, io.gn_iters, done, rank);
+    if (n_process > 0)
+      rank_kernel<<<(n_process + T - 1) / T, T, 0, st>>>(n_process, io.order, rank, n_points);
+    CUDA_TRY(cudaGetLastError());
+  }
+  if (dataflow && n_process > 0) {
+    const int T = 256;
+    int *pend = (int *)(ws + off_pend), *soff = (int *)(ws + off_soff);
+    int *cursor = (int *)(ws + off_cursor), *queue = (int *)(ws + off_queue);
+    CUDA_TRY(cudaMemsetAsync(ws + off_pend, 0, off_queue - off_pend, st));  // pend, counts, cursor
+    CUDA_TRY(cudaMemsetAsync(queue, 0xFF, (size_t)n_process * 4, st));       // -1: slot empty
+    const long long edges = (long long)n_process * n_neigh;
+    const unsigned eg = (unsigned)((edges + T - 1) / T);
+    dep_count_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, io.order, io.neigh, rank, pend, soff);
+    exclusive_scan_kernel<<<1, 1024, 0, st>>>(n_points, soff, soff);
+    dep_fill_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, io.order, io.neigh, rank, soff, cursor,
+                                      (int *)(ws + off_succ));
+    ready_kernel<<<(n_process + T - 1) / T, T, 0, st>>>(n_process, n_points, io.order, pend, queue, ctl + 2);
+    CUDA_TRY(cudaGetLastError());
+  }
+  a.ref = e->ref;
+  a.cor = e->cor;
+  a.nx = e->p.vol_wide;
+  a.ny = e->p.vol_high;
+  a.nz = e->p.vol_tall;
+  a.itype = e->p.interp_type;
+  a.n_points = n_points;
+  a.n_process = n_process;
+  a.n_neigh = (io.seed_mode == DVC_SEED_NEIGHBOURS) ? n_neigh : 0;
+  a.seed_mode = io.seed_mode;
+  a.pts = io.points;
+  a.order = io.order;
+  a.rank = rank;
+  a.neigh = io.neigh;
+  a.seeds = io.seeds;
+  a.status = io.status;
+  a.objmin = io.objmin;
+  a.params = io.params;
+  a.gn_iters = io.gn_iters;
+  a.work_counter = ctl;
+  a.error_flag = ctl + 1;
+  a.dataflow = dataflow ? 1 : 0;
+  if (dataflow) {
+    a.pend = (int *)(ws + off_pend);
+    a.succ_off = (const int *)(ws + off_soff);
+    a.succ = (const int *)(ws + off_succ);
+    a.queue = (int *)(ws + off_queue);
+    a.queue_tail = ctl + 2;
+  }
+  a.done = done;
+  a.counters = (unsigned long long *)(ws + off_ctl + 64);
+  return DVC_OK;
+}
+
 }  // namespace
 
 // ================================================================== C API ===
@@ -633,20 +880,17 @@ void dvc_gpu_destroy(dvc_engine *e) {
   delete e;
 }
 
-// The search launch. Scratch (done flags, ranks, work counter, counters) is
-// the engine's grow-only workspace, or `ws_fixed` when the caller supplies it.
+// The search launch with one configuration (the engine's). Scratch (done
+// flags, ranks, work counter, counters) is the engine's grow-only workspace,
+// or `ws_fixed` when the caller supplies it.
 static int process_device_ws(dvc_engine *e, int n_points, const double *points_dev, int n_process,
                              const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
                              const double *seeds_dev, int *status_dev, double *objmin_dev,
                              double *params_dev, int *gn_iters_dev, void *stream, char *ws_fixed) {
-  if (!e) return set_error(DVC_E_ARG, "null engine");
-  if (n_points < 0 || n_process < 0 || n_process > n_points)
-    return set_error(DVC_E_ARG, "n_process must be in 0..n_points");
-  if (seed_mode < 0 || seed_mode > 3) return set_error(DVC_E_ARG, "bad seed_mode");
-  if (seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !neigh_dev)
-    return set_error(DVC_E_ARG, "neighbour list required");
-  if ((seed_mode == DVC_SEED_GIVEN || seed_mode == DVC_SEED_PARAMS) && !seeds_dev)
-    return set_error(DVC_E_ARG, "seeds required");
+  const RunIO io{n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev, seed_mode,
+                 seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev};
+  int rc = check_run(e, io);
+  if (rc) return rc;
   if (n_points == 0) return DVC_OK;
   cudaStream_t st = (cudaStream_t)stream;
   const dvc_params &p = e->p;
@@ -657,228 +901,64 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   // points favour narrow ones (fewer cluster barriers). Each CTA stages the
   // correlate region of its samples in shared memory (TMA) when the volume's
   // layout allows it and the box fits.
-  const int esize = p.bytes_per_voxel;
-  // dynamic shared memory: what a block may opt into, less the kernel's
-  // static CtaState and a little slack
-  static int optin[64] = {0};
-  {
-    int dev = 0;
-    CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return set_error(DVC_E_ARG, "device index out of range");
-    if (!optin[dev]) CUDA_TRY(cudaDeviceGetAttribute(&optin[dev], cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  }
-  int dev_now = 0;
-  CUDA_TRY(cudaGetDevice(&dev_now));
-  const size_t kDynBudget = (size_t)optin[dev_now] - sizeof(CtaState) - 1024;
-  const bool tma_layout = encode_tiled_fn() != nullptr &&
-                          ((size_t)p.vol_wide * esize) % 16 == 0 &&
-                          ((size_t)p.vol_wide * p.vol_high * esize) % 16 == 0 &&
-                          ((uintptr_t)e->cor % 16) == 0 && !getenv("DVC_NO_STAGE");
+  size_t budget = 0;
+  rc = dyn_budget(&budget);
+  if (rc) return rc;
+  const bool tma_ok = tma_layout(e);
   int C = e->cluster;
   if (C <= 0) {
     const int per = (seed_mode == DVC_SEED_NEIGHBOURS) ? 256 : 1024;
     C = 1;
     while (C < 8 && e->n_sub / (2 * C) >= per) C *= 2;
   }
-  int cap = 0, stage[3] = {0, 0, 0}, rs[9];
+  SearchCfg k;
+  int cap = 0;
   size_t stage_bytes = 0;
-  bool staged = false;
   for (;;) {
-    rank_ranges(e->h_offsets, e->morton_rad, C, rs);
-    cap = 0;
-    for (int r = 0; r < C; r++) cap = std::max(cap, rs[r + 1] - rs[r]);
-    staged = tma_layout;
-    if (staged) {
-      // one region per point covers every grid translation (reach k * inc)
-      double reach = 0.0;
-      if (p.basin_radius != 0.0) {
-        const int k = (int)((double)p.disp_max / p.basin_radius);
-        reach = k * ((double)p.disp_max / k);
-      }
-      // odd row pitch (in 16-byte units) when it fits, else the plain one
-      for (int odd = 1; odd >= 0; odd--) {
-        stage_dims(e, C, esize, reach, rs, odd != 0, stage);
-        stage_bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;
-        if (stage_bytes + state_bytes(cap) <= kDynBudget) break;
-      }
-      if (stage[0] > 256 || stage[1] > 256 || stage[2] > 256) staged = false;
-      if (staged && stage_bytes + state_bytes(cap) > kDynBudget) staged = false;
+    cap = fill_config(e, C, k);
+    stage_bytes = tma_ok ? stage_config(e, C, budget, state_bytes(cap), k) : 0;
+    const size_t need = stage_bytes + state_bytes(cap);
+    if (((tma_ok && !stage_bytes) || need > budget) && C < 8) {
+      C *= 2;
+      continue;
     }
-    const size_t need = (staged ? stage_bytes : 0) + state_bytes(cap);
-    if ((tma_layout && !staged) || need > kDynBudget) {
-      if (C < 8) {
-        C *= 2;
-        continue;
-      }
-    }
-    if (need > kDynBudget && !staged && state_bytes(cap) > kDynBudget)
-      return set_error(DVC_E_ARG, "subvolume too large for the search kernel");
+    if (need > budget) return set_error(DVC_E_ARG, "subvolume too large for the search kernel");
     break;
   }
-  const size_t smem_dyn = (staged ? stage_bytes : 0) + state_bytes(cap);
   CUtensorMap tmap;
   memset(&tmap, 0, sizeof tmap);
-  if (staged) {
-    const cuuint64_t gdim[3] = {(cuuint64_t)p.vol_wide, (cuuint64_t)p.vol_high, (cuuint64_t)p.vol_tall};
-    const cuuint64_t gstride[2] = {(cuuint64_t)p.vol_wide * esize,
-                                   (cuuint64_t)p.vol_wide * p.vol_high * esize};
-    const cuuint32_t box[3] = {(cuuint32_t)stage[0], (cuuint32_t)stage[1], (cuuint32_t)stage[2]};
-    const cuuint32_t estride[3] = {1, 1, 1};
-    const CUresult r = encode_tiled_fn()(
-        &tmap, esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, e->cor,
-        gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) staged = false;
+  if (stage_bytes && !encode_stage_map(e, k, &tmap)) {
+    k = SearchCfg{};
+    cap = fill_config(e, C, k);
+    stage_bytes = 0;
   }
+  const size_t smem_dyn = stage_bytes + state_bytes(cap);
   int max_clusters = 0;
   SearchArgs probe{};
-  int rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tmap, smem_dyn, 0, C, st,
-                           &max_clusters);
+  rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tmap, smem_dyn, 0, C, st, &max_clusters);
   if (rc) return rc;
   if (max_clusters < 1) return set_error(DVC_E_ARG, "search kernel cluster does not fit");
   const int grid = C * std::max(1, std::min(max_clusters, n_process));
 
-  // workspace: done[n], rank[n], counter/error/counters; with dataflow
-  // scheduling also the predecessor counts, successor lists and ready queue
-  const size_t off_done = 0;
-  const size_t off_rank = off_done + (size_t)n_points * 4;
-  const size_t off_ctl = (off_rank + (size_t)n_points * 4 + 255) & ~(size_t)255;
-  const bool dataflow = seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !ws_fixed &&
-                        !getenv("DVC_IN_ORDER");
-  const size_t off_pend = off_ctl + 256;
-  const size_t off_soff = off_pend + (size_t)n_points * 4;
-  const size_t off_cursor = off_soff + ((size_t)n_points + 1) * 4;
-  const size_t off_queue = off_cursor + (size_t)n_points * 4;
-  const size_t off_succ = off_queue + (size_t)n_process * 4;
-  const size_t ws_need = dataflow ? off_succ + (size_t)n_process * n_neigh * 4 : off_ctl + 256;
-  char *ws = ws_fixed;
-  if (!ws) {
-    rc = ensure_ws(e, ws_need);
-    if (rc) return rc;
-    ws = (char *)e->ws;
-    e->counters_off = off_ctl + 64;
-  }
-  int *done = (int *)(ws + off_done);
-  int *rank = (int *)(ws + off_rank);
-  int *ctl = (int *)(ws + off_ctl);
-  unsigned long long *counters = (unsigned long long *)(ws + off_ctl + 64);
-  CUDA_TRY(cudaMemsetAsync(ws + off_ctl, 0, 256, st));
-  {
-    const int T = 256;
-    const int G = (n_points + T - 1) / T;
-    init_outputs_kernel<<<G, T, 0, st>>>(n_points, status_dev, objmin_dev, params_dev, gn_iters_dev,
-                                         done, rank);
-    if (n_process > 0) rank_kernel<<<(n_process + T - 1) / T, T, 0, st>>>(n_process, order_dev, rank, n_points);
-    CUDA_TRY(cudaGetLastError());
-  }
-  if (n_process == 0) return DVC_OK;
-  if (dataflow) {
-    const int T = 256;
-    int *pend = (int *)(ws + off_pend), *soff = (int *)(ws + off_soff);
-    int *cursor = (int *)(ws + off_cursor), *queue = (int *)(ws + off_queue);
-    CUDA_TRY(cudaMemsetAsync(ws + off_pend, 0, off_queue - off_pend, st));  // pend, counts, cursor
-    CUDA_TRY(cudaMemsetAsync(queue, 0xFF, (size_t)n_process * 4, st));       // -1: slot empty
-    const long long edges = (long long)n_process * n_neigh;
-    const unsigned eg = (unsigned)((edges + T - 1) / T);
-    dep_count_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, order_dev, neigh_dev, rank, pend,
-                                       soff);
-    exclusive_scan_kernel<<<1, 1024, 0, st>>>(n_points, soff, soff);
-    dep_fill_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, order_dev, neigh_dev, rank, soff,
-                                      cursor, (int *)(ws + off_succ));
-    ready_kernel<<<(n_process + T - 1) / T, T, 0, st>>>(n_process, n_points, order_dev, pend, queue,
-                                                        (int *)(ws + off_ctl) + 2);
-    CUDA_TRY(cudaGetLastError());
-  }
-
   SearchArgs a{};
-  a.ref = e->ref;
-  a.cor = e->cor;
-  a.nx = p.vol_wide;
-  a.ny = p.vol_high;
-  a.nz = p.vol_tall;
-  a.geom = p.subvol_geom;
-  a.ndof = p.num_srch_dof;
-  a.objfcn = p.obj_function;
-  a.itype = p.interp_type;
-  a.n_sub = e->n_sub;
-  a.cube_n = e->cube_n;
-  a.subv_rad = e->subv_rad;
-  for (int d = 0; d < 3; d++) {
-    a.aspect[d] = p.subvol_aspect[d];
-    a.nom_mn[d] = e->nom_mn[d];
-    a.nom_mx[d] = e->nom_mx[d];
-    a.nom_cen[d] = e->nom_cen[d];
-    a.bext[d] = e->bext[d];
-    a.rigid[d] = p.rigid_trans[d];
-  }
-  a.do_grid = p.basin_radius != 0.0;
-  if (a.do_grid) {
-    const double displ_max = p.disp_max;
-    a.num_inc = (int)(displ_max / p.basin_radius);
-    a.inc = displ_max / a.num_inc;
-    a.inc_int = (a.inc == std::floor(a.inc) && a.inc <= 64.0 && !getenv("DVC_GENERAL_GRID")) ? (int)a.inc : 0;
-  }
-  a.n_points = n_points;
-  a.n_process = n_process;
-  a.n_neigh = (seed_mode == DVC_SEED_NEIGHBOURS) ? n_neigh : 0;
-  a.seed_mode = seed_mode;
-  a.pts = points_dev;
-  a.order = order_dev;
-  a.rank = rank;
-  a.neigh = neigh_dev;
-  a.seeds = seeds_dev;
-  a.status = status_dev;
-  a.objmin = objmin_dev;
-  a.params = params_dev;
-  a.gn_iters = gn_iters_dev;
-  a.work_counter = ctl;
-  a.error_flag = ctl + 1;
-  a.dataflow = dataflow ? 1 : 0;
-  if (dataflow) {
-    a.pend = (int *)(ws + off_pend);
-    a.succ_off = (const int *)(ws + off_soff);
-    a.succ = (const int *)(ws + off_succ);
-    a.queue = (int *)(ws + off_queue);
-    a.queue_tail = ctl + 2;
-  }
-  a.done = done;
-  a.counters = counters;
+  rc = prepare_run(e, io, st, ws_fixed, a);
+  if (rc) return rc;
+  if (n_process == 0) return DVC_OK;
+  a.cfg0 = k;
+  a.n_cfg = 1;
   a.local_cap = cap;
-  a.stage_on = staged ? 1 : 0;
-  for (int d = 0; d < 3; d++) a.stage[d] = stage[d];
   a.stage_bytes = (int)stage_bytes;
-  for (int r = 0; r < 9; r++) a.rank_start[r] = rs[r];
-  a.off_i = e->d_off_i;
-  a.off_f = e->d_off_f;
-  // extrema of the stable offsets, over all samples and per cluster rank
-  // (the sample clouds' bounding boxes follow from them: FP64 addition of
-  // the point is monotone)
-  for (int d = 0; d < 3; d++) {
-    a.off_min[d] = 1e300;
-    a.off_max[d] = -1e300;
-  }
-  for (int r = 0; r < C; r++)
-    for (int d = 0; d < 3; d++) {
-      double mn = 1e300, mx = -1e300;
-      for (int i = rs[r]; i < rs[r + 1]; i++) {
-        mn = std::min(mn, e->h_offsets[(size_t)i * 3 + d]);
-        mx = std::max(mx, e->h_offsets[(size_t)i * 3 + d]);
-      }
-      a.rank_off_min[r][d] = mn;
-      a.rank_off_max[r][d] = mx;
-      a.off_min[d] = std::min(a.off_min[d], mn);
-      a.off_max[d] = std::max(a.off_max[d], mx);
-    }
   if (getenv("DVC_VERBOSE"))
     fprintf(stderr, "dvc search: %d points, cluster %d, grid %d CTAs, staged %d (box %d x %d x %d), "
-            "dynamic smem %zu of %zu, samples/CTA <= %d, grid step %s\n", n_process, C, grid, (int)staged,
-            stage[0], stage[1], stage[2], smem_dyn, kDynBudget, cap,
-            a.inc_int ? "integral" : (a.do_grid ? "general" : "none"));
+            "dynamic smem %zu of %zu, samples/CTA <= %d, grid step %s\n", n_process, C, grid,
+            k.stage_on, k.stage[0], k.stage[1], k.stage[2], smem_dyn, budget, cap,
+            k.inc_int ? "integral" : (k.do_grid ? "general" : "none"));
   e->last_cluster = C;
   e->last_grid = grid;
-  e->last_staged = staged;
+  e->last_staged = k.stage_on;
   return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, tmap, smem_dyn, grid, C, st, nullptr);
 }
+
 
 int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev, int n_process,
                            const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
@@ -938,13 +1018,21 @@ int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *po
                            stream, ws);
 }
 
-int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_process,
-                    const int *order, int n_neigh, const int *neigh, int seed_mode,
-                    const double *seeds, int *status, double *objmin, double *params, int *gn_iters,
-                    dvc_stats *stats) {
+// Host-array search: arguments checked, arrays copied in, the engine's (or
+// the plan's) device search, results and counters copied out.
+static int host_process(dvc_engine *e, dvc_plan *plan, const int *point_cfg, int n_points,
+                        const double *points, int n_process, const int *order, int n_neigh,
+                        const int *neigh, int seed_mode, const double *seeds, int *status,
+                        double *objmin, double *params, int *gn_iters, dvc_stats *stats) {
   if (!e || !points || !status || !objmin || !params) return set_error(DVC_E_ARG, "null argument");
   if (n_points < 0 || n_process < 0 || n_process > n_points)
     return set_error(DVC_E_ARG, "n_process must be in 0..n_points");
+  if (plan) {
+    if (!point_cfg) return set_error(DVC_E_ARG, "point_cfg required");
+    const int nc = (int)plan->cfgs.size();
+    for (int i = 0; i < n_points; i++)
+      if (point_cfg[i] < 0 || point_cfg[i] >= nc) return set_error(DVC_E_ARG, "configuration index out of range");
+  }
   if (n_process > 0 && !order) return set_error(DVC_E_ARG, "order required");
   if (seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !neigh)
     return set_error(DVC_E_ARG, "neighbour list required");
@@ -958,12 +1046,12 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
   auto t0 = std::chrono::steady_clock::now();
   const size_t N = (size_t)n_points;
   double *d_pts = nullptr, *d_seeds = nullptr, *d_obj = nullptr, *d_par = nullptr;
-  int *d_order = nullptr, *d_neigh = nullptr, *d_status = nullptr, *d_its = nullptr;
+  int *d_order = nullptr, *d_neigh = nullptr, *d_status = nullptr, *d_its = nullptr, *d_cfg = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int rc = DVC_OK;
   auto cleanup = [&]() {
     cudaFree(d_pts); cudaFree(d_seeds); cudaFree(d_obj); cudaFree(d_par);
-    cudaFree(d_order); cudaFree(d_neigh); cudaFree(d_status); cudaFree(d_its);
+    cudaFree(d_order); cudaFree(d_neigh); cudaFree(d_status); cudaFree(d_its); cudaFree(d_cfg);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
   };
@@ -992,11 +1080,17 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
     TRYC(cudaMalloc(&d_seeds, N * per * sizeof(double)));
     TRYC(cudaMemcpy(d_seeds, seeds, N * per * sizeof(double), cudaMemcpyHostToDevice));
   }
+  if (plan) {
+    TRYC(cudaMalloc(&d_cfg, std::max<size_t>(1, N) * sizeof(int)));
+    TRYC(cudaMemcpy(d_cfg, point_cfg, N * sizeof(int), cudaMemcpyHostToDevice));
+  }
   TRYC(cudaEventCreate(&ev0));
   TRYC(cudaEventCreate(&ev1));
   TRYC(cudaEventRecord(ev0, 0));
-  rc = dvc_gpu_process_device(e, n_points, d_pts, n_process, d_order, n_neigh, d_neigh, seed_mode,
-                              d_seeds, d_status, d_obj, d_par, d_its, nullptr);
+  rc = plan ? dvc_gpu_plan_process_device(plan, d_cfg, n_points, d_pts, n_process, d_order, n_neigh, d_neigh,
+                                          seed_mode, d_seeds, d_status, d_obj, d_par, d_its, nullptr)
+            : dvc_gpu_process_device(e, n_points, d_pts, n_process, d_order, n_neigh, d_neigh, seed_mode,
+                                     d_seeds, d_status, d_obj, d_par, d_its, nullptr);
   if (rc) {
     cleanup();
     return rc;
@@ -1019,7 +1113,8 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
   cudaEventElapsedTime(&kms, ev0, ev1);
   cleanup();
 #undef TRYC
-  if (ctl[1] != 0) return set_error(ctl[1], "a bounded dependency wait gave up; points left unsearched");
+  if (ctl[1] == DVC_E_TIMEOUT) return set_error(ctl[1], "a bounded dependency wait gave up; points left unsearched");
+  if (ctl[1] != 0) return set_error(ctl[1], "a point named no configuration of the plan; it was left unsearched");
   if (stats) {
     memset(stats, 0, sizeof *stats);
     stats->n_processed = n_process;
@@ -1034,6 +1129,247 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
     stats->total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
+  return DVC_OK;
+}
+
+int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_process,
+                    const int *order, int n_neigh, const int *neigh, int seed_mode,
+                    const double *seeds, int *status, double *objmin, double *params, int *gn_iters,
+                    dvc_stats *stats) {
+  return host_process(e, nullptr, nullptr, n_points, points, n_process, order, n_neigh, neigh, seed_mode,
+                      seeds, status, objmin, params, gn_iters, stats);
+}
+
+// ---- several configurations in one launch ------------------------------------
+// Lay out plan `pl` at cluster width C: per configuration its rank ranges and
+// offset extrema, then, with staging, its box when it fits beside the largest
+// per-CTA sample state. The configuration table and tensor maps are uploaded
+// only once the shape is known to fit, so a failed call leaves the plan as it
+// was.
+static int plan_build(dvc_plan *pl, int C, int staging) {
+  if (C != 1 && C != 2 && C != 4 && C != 8) return set_error(DVC_E_ARG, "cluster width must be 1, 2, 4 or 8");
+  size_t budget = 0;
+  int rc = dyn_budget(&budget);
+  if (rc) return rc;
+  const int n = (int)pl->cfgs.size();
+  std::vector<SearchCfg> ks((size_t)n);
+  int cap = 0;
+  for (int i = 0; i < n; i++) cap = std::max(cap, fill_config(pl->cfgs[i], C, ks[i]));
+  if (state_bytes(cap) > budget)
+    return set_error(DVC_E_ARG, "the largest subvolume does not fit the search kernel at cluster width " +
+                                    std::to_string(C));
+  const bool tma_ok = staging && tma_layout(pl->cfgs[0]);
+  std::vector<CUtensorMap> maps((size_t)n);
+  size_t sb = 0;
+  int n_staged = 0;
+  for (int i = 0; i < n; i++) {
+    memset(&maps[(size_t)i], 0, sizeof(CUtensorMap));
+    if (!tma_ok) continue;
+    const size_t b = stage_config(pl->cfgs[i], C, budget, state_bytes(cap), ks[(size_t)i]);
+    if (b && encode_stage_map(pl->cfgs[i], ks[(size_t)i], &maps[(size_t)i])) {
+      sb = std::max(sb, b);
+      n_staged++;
+    } else {
+      ks[(size_t)i].stage_on = 0;
+      for (int d = 0; d < 3; d++) ks[(size_t)i].stage[d] = 0;
+      ks[(size_t)i].stage_tx = 0;
+    }
+  }
+  const size_t smem = sb + state_bytes(cap);
+  const dvc_params &p = pl->cfgs[0]->p;
+  int mc = 0;
+  SearchArgs probe{};
+  CUtensorMap tm0;
+  memset(&tm0, 0, sizeof tm0);
+  rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tm0, smem, 0, C, 0, &mc);
+  if (rc) return rc;
+  if (mc < 1) return set_error(DVC_E_ARG, "search kernel cluster does not fit");
+  if (!pl->d_cfgs) {
+    CUDA_TRY(cudaMalloc(&pl->d_cfgs, (size_t)n * sizeof(SearchCfg)));
+    CUDA_TRY(cudaMalloc(&pl->d_tmaps, (size_t)n * sizeof(CUtensorMap)));
+  }
+  for (int i = 0; i < n; i++) ks[(size_t)i].tmap = ks[(size_t)i].stage_on ? pl->d_tmaps + i : nullptr;
+  CUDA_TRY(cudaDeviceSynchronize());  // no launch still reads the old table
+  CUDA_TRY(cudaMemcpy(pl->d_tmaps, maps.data(), (size_t)n * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(pl->d_cfgs, ks.data(), (size_t)n * sizeof(SearchCfg), cudaMemcpyHostToDevice));
+  pl->h_cfgs = ks;
+  pl->cluster = C;
+  pl->staging = staging;
+  pl->n_staged = n_staged;
+  pl->cap = cap;
+  pl->stage_bytes = sb;
+  pl->smem_dyn = smem;
+  pl->max_clusters = mc;
+  return DVC_OK;
+}
+
+int dvc_gpu_plan_create(dvc_plan **out, dvc_engine *const *configs, int n_configs, int cluster) {
+  if (!out || !configs) return set_error(DVC_E_ARG, "null argument");
+  *out = nullptr;
+  if (n_configs < 1) return set_error(DVC_E_ARG, "a plan needs at least one configuration");
+  const dvc_engine *e0 = configs[0];
+  for (int i = 0; i < n_configs; i++) {
+    const dvc_engine *e = configs[i];
+    if (!e) return set_error(DVC_E_ARG, "null configuration");
+    if (e->ref != e0->ref || e->cor != e0->cor || e->p.vol_wide != e0->p.vol_wide ||
+        e->p.vol_high != e0->p.vol_high || e->p.vol_tall != e0->p.vol_tall ||
+        e->p.bytes_per_voxel != e0->p.bytes_per_voxel || e->p.interp_type != e0->p.interp_type)
+      return set_error(DVC_E_ARG, "the configurations of a plan must share volumes, voxel type and interpolation");
+  }
+  if (cluster != 0 && cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8)
+    return set_error(DVC_E_ARG, "cluster must be 0, 1, 2, 4 or 8");
+  dvc_plan *pl = new dvc_plan();
+  pl->cfgs.assign(configs, configs + n_configs);
+  int rc = DVC_OK;
+  if (cluster > 0) {
+    rc = plan_build(pl, cluster, 1);
+  } else {
+    // from the largest sample count (about 512 samples per CTA and up), then
+    // wider while the largest subvolume does not fit
+    int nmax = 0;
+    for (const dvc_engine *e : pl->cfgs) nmax = std::max(nmax, e->n_sub);
+    int C = 1;
+    while (C < 8 && nmax / (2 * C) >= 512) C *= 2;
+    for (;; C *= 2) {
+      rc = plan_build(pl, C, 1);
+      if (rc == DVC_OK || C == 8) break;
+    }
+  }
+  if (rc) {
+    dvc_gpu_plan_destroy(pl);
+    return rc;
+  }
+  *out = pl;
+  return DVC_OK;
+}
+
+void dvc_gpu_plan_destroy(dvc_plan *plan) {
+  if (!plan) return;
+  if (plan->d_cfgs) cudaFree(plan->d_cfgs);
+  if (plan->d_tmaps) cudaFree(plan->d_tmaps);
+  delete plan;
+}
+
+int dvc_gpu_plan_info(const dvc_plan *plan, int *cluster, int *staging, int *n_staged, long long *smem_bytes) {
+  if (!plan) return set_error(DVC_E_ARG, "null plan");
+  if (cluster) *cluster = plan->cluster;
+  if (staging) *staging = plan->staging;
+  if (n_staged) *n_staged = plan->n_staged;
+  if (smem_bytes) *smem_bytes = (long long)plan->smem_dyn;
+  return DVC_OK;
+}
+
+int dvc_gpu_plan_set_shape(dvc_plan *plan, int cluster, int staging) {
+  if (!plan) return set_error(DVC_E_ARG, "null plan");
+  return plan_build(plan, cluster, staging ? 1 : 0);
+}
+
+int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_points,
+                                const double *points_dev, int n_process, const int *order_dev,
+                                int n_neigh, const int *neigh_dev, int seed_mode,
+                                const double *seeds_dev, int *status_dev, double *objmin_dev,
+                                double *params_dev, int *gn_iters_dev, void *stream) {
+  if (!plan) return set_error(DVC_E_ARG, "null plan");
+  dvc_engine *e = plan->cfgs[0];
+  const RunIO io{n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev, seed_mode,
+                 seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev};
+  int rc = check_run(e, io);
+  if (rc) return rc;
+  if (n_process > 0 && !point_cfg_dev) return set_error(DVC_E_ARG, "point_cfg required");
+  if (n_points == 0) return DVC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  SearchArgs a{};
+  rc = prepare_run(e, io, st, nullptr, a);
+  if (rc) return rc;
+  if (n_process == 0) return DVC_OK;
+  const int n = (int)plan->cfgs.size();
+  if (n == 1) {
+    a.cfg0 = plan->h_cfgs[0];
+    a.n_cfg = 1;
+  } else {
+    a.cfgs = plan->d_cfgs;
+    a.point_cfg = point_cfg_dev;
+    a.n_cfg = n;
+  }
+  a.local_cap = plan->cap;
+  a.stage_bytes = (int)plan->stage_bytes;
+  const int C = plan->cluster;
+  const int grid = C * std::max(1, std::min(plan->max_clusters, n_process));
+  if (getenv("DVC_VERBOSE"))
+    fprintf(stderr, "dvc plan search: %d points, %d configurations (%d staged), cluster %d, grid %d CTAs, "
+            "dynamic smem %zu, samples/CTA <= %d\n", n_process, n, plan->n_staged, C, grid, plan->smem_dyn,
+            plan->cap);
+  e->last_cluster = C;
+  e->last_grid = grid;
+  e->last_staged = plan->n_staged > 0;
+  CUtensorMap tm0;
+  memset(&tm0, 0, sizeof tm0);
+  return dispatch_launch(e->p.bytes_per_voxel, e->p.interp_type, a, tm0, plan->smem_dyn, grid, C, st, nullptr);
+}
+
+int dvc_gpu_plan_process(dvc_plan *plan, const int *point_cfg, int n_points, const double *points,
+                         int n_process, const int *order, int n_neigh, const int *neigh,
+                         int seed_mode, const double *seeds, int *status, double *objmin,
+                         double *params, int *gn_iters, dvc_stats *stats) {
+  if (!plan) return set_error(DVC_E_ARG, "null plan");
+  return host_process(plan->cfgs[0], plan, point_cfg, n_points, points, n_process, order, n_neigh, neigh,
+                      seed_mode, seeds, status, objmin, params, gn_iters, stats);
+}
+
+int dvc_gpu_plan_autotune(dvc_plan *plan, const int *point_cfg_dev, int n_points,
+                          const double *points_dev, int n_process, const int *order_dev,
+                          int n_neigh, const int *neigh_dev, int seed_mode,
+                          const double *seeds_dev, int *status_dev, double *objmin_dev,
+                          double *params_dev, int reps, double ms_out[8]) {
+  if (!plan) return set_error(DVC_E_ARG, "null plan");
+  if (reps < 1) return set_error(DVC_E_ARG, "reps must be >= 1");
+  const int C0 = plan->cluster, S0 = plan->staging;
+  double best = -1.0;
+  int bestC = C0, bestS = S0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  CUDA_TRY(cudaEventCreate(&ev0));
+  CUDA_TRY(cudaEventCreate(&ev1));
+  int rc = DVC_OK;
+  for (int j = 0; j < 4 && rc == DVC_OK; j++)
+    for (int s = 0; s < 2 && rc == DVC_OK; s++) {
+      if (ms_out) ms_out[2 * j + s] = -1.0;
+      if (plan_build(plan, 1 << j, s) != DVC_OK) continue;  // this shape does not fit
+      if (s == 1 && plan->n_staged == 0) continue;         // same as without staging
+      auto run = [&]() {
+        return dvc_gpu_plan_process_device(plan, point_cfg_dev, n_points, points_dev, n_process, order_dev,
+                                           n_neigh, neigh_dev, seed_mode, seeds_dev, status_dev, objmin_dev,
+                                           params_dev, nullptr, nullptr);
+      };
+      rc = run();
+      if (rc) break;
+      if (cudaEventRecord(ev0, 0) != cudaSuccess) { rc = set_error(DVC_E_CUDA, "event record"); break; }
+      for (int r = 0; r < reps && rc == DVC_OK; r++) rc = run();
+      if (rc) break;
+      float ms = 0.f;
+      if (cudaEventRecord(ev1, 0) != cudaSuccess || cudaEventSynchronize(ev1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess) {
+        rc = set_error(DVC_E_CUDA, "autotune timing failed");
+        break;
+      }
+      const double mean = ms / reps;
+      if (ms_out) ms_out[2 * j + s] = mean;
+      if (best < 0 || mean < best) {
+        best = mean;
+        bestC = 1 << j;
+        bestS = s;
+      }
+    }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  const int rc2 = plan_build(plan, rc == DVC_OK ? bestC : C0, rc == DVC_OK ? bestS : S0);
+  return rc ? rc : rc2;
+}
+
+int dvc_gpu_set_cluster(dvc_engine *e, int cluster) {
+  if (!e) return set_error(DVC_E_ARG, "null engine");
+  if (cluster != 0 && cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8)
+    return set_error(DVC_E_ARG, "cluster must be 0, 1, 2, 4 or 8");
+  e->cluster = cluster;
   return DVC_OK;
 }
 

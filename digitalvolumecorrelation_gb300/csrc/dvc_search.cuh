@@ -42,10 +42,10 @@ constexpr long long kWaitPolls = 1LL << 25;   // bounded dependency wait (~secon
 constexpr int kCB = 384;                      // cluster reduction buffer length
 constexpr int kGRows = kMaxDof + 3;           // Gauss-Newton chunk rows: g[12], 1, t', q
 
-struct SearchArgs {
-  const void *ref, *cor;
-  int nx, ny, nz;
-  int geom, ndof, objfcn, itype;
+// One search configuration (the settings of one `dvc` input file that shape a
+// point's search): a launch holds one, or one per group of points.
+struct SearchCfg {
+  int geom, ndof, objfcn;
   int n_sub, cube_n;
   double subv_rad, aspect[3];
   double nom_mn[3], nom_mx[3], nom_cen[3];  // nominal interpolation box (Search::Search)
@@ -54,6 +54,31 @@ struct SearchArgs {
   int inc_int;  // the grid step when it is a whole number of voxels, else 0
   double inc;
   double rigid[3];
+  // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
+  // voxels (stage_tx bytes), TMA-loaded into the staging buffer
+  int stage_on;
+  int stage[3];
+  unsigned stage_tx;
+  const CUtensorMap *tmap;       // this configuration's tensor map, or null: the kernel's
+  int rank_start[9];             // sample range of each cluster rank
+  // stable offsets of the samples from their point: whole voxels and FP32
+  // fractions; their extrema over all samples and over each rank's samples
+  const int *off_i;
+  const float *off_f;
+  double off_min[3], off_max[3];
+  double rank_off_min[8][3], rank_off_max[8][3];
+};
+
+struct SearchArgs {
+  const void *ref, *cor;
+  int nx, ny, nz;
+  int itype;
+  // the configuration of every point (n_cfg == 1), or per point
+  // cfgs[point_cfg[point]] (n_cfg > 1)
+  SearchCfg cfg0;
+  const SearchCfg *cfgs;
+  const int *point_cfg;
+  int n_cfg;
   int n_points, n_process, n_neigh, seed_mode;
   const double *pts;
   const int *order, *rank, *neigh;
@@ -77,18 +102,7 @@ struct SearchArgs {
                                  // CTAs (PhaseClock), [16] Gauss-Newton systems solved by
                                  // the FP64 factorisation
   int local_cap;                 // per-CTA sample capacity of the dynamic arrays
-  // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
-  // voxels per evaluation, TMA-loaded into one of two shared buffers
-  int stage_on;
-  int stage[3];
-  int stage_bytes;               // one buffer, padded
-  int rank_start[9];             // sample range of each cluster rank
-  // stable offsets of the samples from their point: whole voxels and FP32
-  // fractions; their extrema over all samples and over each rank's samples
-  const int *off_i;
-  const float *off_f;
-  double off_min[3], off_max[3];
-  double rank_off_min[8][3], rank_off_max[8][3];
+  int stage_bytes;               // staging buffer (0: none), padded
 };
 
 struct DBox {
@@ -111,6 +125,7 @@ struct Region {
 };
 
 struct CtaState {
+  SearchCfg cfg;  // the current point's configuration
   PointHeader H;
   unsigned long long wkey[kWarps][6];  // per-warp position keys (range checks)
   double sref[3], sbmn[3], sbmx[3];
@@ -354,7 +369,7 @@ __device__ __forceinline__ double objective_from_sums(int fcn, double S1, double
 // and sum the displacements of the converged ones: per lane in list order,
 // then a fixed shuffle tree, where the reference keeps one running sum (the
 // two differ only in FP64 rounding). H.n and H.rank are set by lane 0.
-__device__ bool point_seed(const SearchArgs &a, PointHeader &H) {
+__device__ bool point_seed(const SearchArgs &a, const SearchCfg &K, PointHeader &H) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int n = H.n;
@@ -405,13 +420,13 @@ __device__ bool point_seed(const SearchArgs &a, PointHeader &H) {
     if (a.seed_mode == DVC_SEED_GIVEN) sd = a.seeds[(size_t)n * 3 + d];
     else if (a.seed_mode == DVC_SEED_PARAMS) sd = a.seeds[(size_t)n * 12 + d];
     else if (good != 0) sd = sum[d] / good;
-    else sd = a.rigid[d];
+    else sd = K.rigid[d];
     H.seed[d] = sd;
     const double cref = H.pt[d];
     const double ccor = __dadd_rn(H.pt[d], sd);  // Point::move_by
-    const double ref_mn = __dadd_rn(a.nom_mn[d], __dsub_rn(cref, a.nom_cen[d]));
-    const double cor_mn = __dadd_rn(a.nom_mn[d], __dsub_rn(ccor, a.nom_cen[d]));
-    const double amn = __dadd_rn(a.nom_mn[d], 1.0), amx = __dadd_rn(a.nom_mx[d], -1.0);
+    const double ref_mn = __dadd_rn(K.nom_mn[d], __dsub_rn(cref, K.nom_cen[d]));
+    const double cor_mn = __dadd_rn(K.nom_mn[d], __dsub_rn(ccor, K.nom_cen[d]));
+    const double amn = __dadd_rn(K.nom_mn[d], 1.0), amx = __dadd_rn(K.nom_mx[d], -1.0);
     const double acen = __ddiv_rn(__dadd_rn(amn, amx), 2.0);
     const double dact = __dsub_rn(ccor, acen);
     H.act_cor.mn[d] = __dadd_rn(amn, dact);
@@ -425,8 +440,8 @@ __device__ bool point_seed(const SearchArgs &a, PointHeader &H) {
     H.chk_ref = 0;
     H.chk_cor = 0;
     for (int d = 0; d < 3; d++) {
-      if (H.o_ref[d] - 1 < 0 || H.o_ref[d] + a.bext[d] > vol[d] - 1) H.chk_ref = 1;
-      if (H.o_cor[d] - 1 < 0 || H.o_cor[d] + a.bext[d] > vol[d] - 1) H.chk_cor = 1;
+      if (H.o_ref[d] - 1 < 0 || H.o_ref[d] + K.bext[d] > vol[d] - 1) H.chk_ref = 1;
+      if (H.o_cor[d] - 1 < 0 || H.o_cor[d] + K.bext[d] > vol[d] - 1) H.chk_cor = 1;
     }
   }
   __syncwarp();
@@ -793,7 +808,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
 
 // Staged region covering positions [pmin, pmax] (global voxel coordinates)
 // with the stencil margin; ok = 0 when it does not fit the staging box.
-__device__ __forceinline__ Region make_region(const SearchArgs &a, const double pmin[3],
+__device__ __forceinline__ Region make_region(const SearchCfg &a, const double pmin[3],
                                               const double pmax[3], int esize) {
   Region r;
   r.ok = a.stage_on;
@@ -883,7 +898,7 @@ __device__ __forceinline__ void grid_chunk_lanes(
   const int j = tid % span, grp = tid / span;
   const bool live = j < nch;
   // this lane's translation
-  const int step = a.inc_int;
+  const int step = S.cfg.inc_int;
   const int o = o0 + min(j, nch - 1);
   const int dc[3] = {(o % side - k) * step, ((o / side) % side - k) * step, (o / (side * side) - k) * step};
   const int dbytes = ((dc[2] * B[1] + dc[1]) * B[0] + dc[0]) * esize;
@@ -893,7 +908,7 @@ __device__ __forceinline__ void grid_chunk_lanes(
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     lo[d] = max(IT == 2 ? 1 : 0, r0[d] + 1 - o3[d]) - dc[d];
-    hi[d] = min(min(n3[d] - (IT == 2 ? 3 : 2), a.bext[d] - 1), r0[d] + B[d] - 3 - o3[d]) - dc[d];
+    hi[d] = min(min(n3[d] - (IT == 2 ? 3 : 2), S.cfg.bext[d] - 1), r0[d] + B[d] - 3 - o3[d]) - dc[d];
   }
   int iu0[3];
   float fu0[3];
@@ -937,7 +952,7 @@ __device__ __forceinline__ void grid_chunk_lanes(
                                         w[0], w[1], w[2], g);
       } else {
         int cc[3] = {cx + dc[0], cy + dc[1], cz + dc[2]};
-        clamp_cell(cc, a.bext);
+        clamp_cell(cc, S.cfg.bext);
         float g[3];
         bool und;
         t = eval_sample_t<VT, IT, false, true>(ss, r0, B, gsc, G, cc, fm, g, und);
@@ -989,11 +1004,11 @@ __device__ __forceinline__ int restage(const SearchArgs &a, CtaState &S, const d
     bool in = true;
     for (int d = 0; d < 3; d++) {
       const double lo = floor(pmn[d]) - 2.0, hi = floor(pmx[d]) + 3.0;
-      if (!(lo >= cur.r0[d] && hi < cur.r0[d] + a.stage[d])) in = false;
+      if (!(lo >= cur.r0[d] && hi < cur.r0[d] + S.cfg.stage[d])) in = false;
     }
     if (in) return 0;
   }
-  const Region r = make_region(a, pmn, pmx, esize);
+  const Region r = make_region(S.cfg, pmn, pmx, esize);
   S.reg[0] = r;
   if (!r.ok) return 0;
   tma_load_3d(tm, buf, bar, r.r0[0], r.r0[1], r.r0[2], tx);
@@ -1127,15 +1142,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   cl.rank = cl.g.block_rank();
   cl.size = cl.g.num_blocks();
   const int tid = threadIdx.x;
-  const int nsub = a.n_sub;
-  const int lo = a.rank_start[cl.rank];
-  const int nl = a.rank_start[cl.rank + 1] - lo;
   constexpr int esize = (int)sizeof(VT);
 
   // dynamic shared memory: two staging buffers, then the per-CTA sample
   // state (packed cell base, fraction x3, reference quantity, final value)
   // and the Gauss-Newton chunk rows
-  const int sb = a.stage_on ? a.stage_bytes : 0;
+  const int sb = a.stage_bytes;
   unsigned char *stage_buf[2] = {dsm, dsm};
   const int cap = a.local_cap;
   int *s_ip = reinterpret_cast<int *>(dsm + sb);
@@ -1151,16 +1163,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     mbar_init(bar_addr[1]);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // the configuration of every point, when there is one
+  if (a.n_cfg <= 1)
+    for (int k = tid; k < (int)(sizeof(SearchCfg) / 4); k += kThreads)
+      reinterpret_cast<int *>(&S.cfg)[k] = reinterpret_cast<const int *>(&a.cfg0)[k];
   __syncthreads();
-  const int B[3] = {a.stage[0], a.stage[1], a.stage[2]};
-  const uint32_t stage_tx = (uint32_t)(B[0] * B[1] * B[2] * esize);
 
   const GSrc<VT> gref{reinterpret_cast<const VT *>(a.ref), a.nx, a.ny, a.nz, false};
   const GSrc<VT> gcor0{reinterpret_cast<const VT *>(a.cor), a.nx, a.ny, a.nz, false};
-  const int ndof = a.ndof;
-  const int fcn = a.objfcn;
-  const bool sad = (fcn == DVC_SAD);
-  const double inv_nsub = 1.0 / (double)nsub;
   PhaseClock pc;
   pc.start();
 
@@ -1196,7 +1206,21 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int d = 0; d < 3; d++) H.pt[d] = a.pts[(size_t)H.n * 3 + d];
       }
       __syncwarp();
-      if (H.flag == 0 && !point_seed(a, H) && tid == 0) H.flag = 2;
+      if (a.n_cfg > 1 && H.flag == 0) {  // this point's configuration
+        const int ci = a.point_cfg[H.n];
+        if ((unsigned)ci >= (unsigned)a.n_cfg) {
+          // no such configuration: the point is left unsearched, the call fails
+          if (tid == 0) {
+            atomicExch(a.error_flag, DVC_E_ARG);
+            H.flag = 2;
+          }
+        } else {
+          const int *src = reinterpret_cast<const int *>(a.cfgs + ci);
+          for (int k = tid; k < (int)(sizeof(SearchCfg) / 4); k += 32) reinterpret_cast<int *>(&S.cfg)[k] = src[k];
+        }
+        __syncwarp();
+      }
+      if (H.flag == 0 && !point_seed(a, S.cfg, H) && tid == 0) H.flag = 2;
     }
     cl.g.sync();
     if (cl.rank != 0) {
@@ -1219,11 +1243,33 @@ __global__ void __launch_bounds__(kThreads, 1)
       cl.g.sync();
       continue;
     }
+    if (a.n_cfg > 1) {
+      if (cl.rank != 0) {
+        const int *src = reinterpret_cast<const int *>(a.cfgs + a.point_cfg[S.H.n]);
+        for (int k = tid; k < (int)(sizeof(SearchCfg) / 4); k += kThreads) reinterpret_cast<int *>(&S.cfg)[k] = src[k];
+      }
+      __syncthreads();
+    }
+    const SearchCfg &K = S.cfg;
+    const int nsub = K.n_sub;
+    const int lo = K.rank_start[cl.rank];
+    const int nl = K.rank_start[cl.rank + 1] - lo;
+    const int B[3] = {K.stage[0], K.stage[1], K.stage[2]};
+    const uint32_t stage_tx = K.stage_tx;
+    const CUtensorMap *tmp = K.tmap ? K.tmap : &tmap;
+    if (K.tmap && tid == 0)  // a tensor map in global memory: its latest contents for the TMA unit
+      asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                       reinterpret_cast<unsigned long long>(tmp))
+                   : "memory");
+    const int ndof = K.ndof;
+    const int fcn = K.objfcn;
+    const bool sad = (fcn == DVC_SAD);
+    const double inv_nsub = 1.0 / (double)nsub;
     GSrc<VT> gsr = gref, gsc = gcor0;
     gsr.checked = S.H.chk_ref;
     gsc.checked = S.H.chk_cor;
-    const BoxGeom Gref{S.H.o_ref[0], S.H.o_ref[1], S.H.o_ref[2], a.bext[0], a.bext[1], a.bext[2]};
-    const BoxGeom Gcor{S.H.o_cor[0], S.H.o_cor[1], S.H.o_cor[2], a.bext[0], a.bext[1], a.bext[2]};
+    const BoxGeom Gref{S.H.o_ref[0], S.H.o_ref[1], S.H.o_ref[2], K.bext[0], K.bext[1], K.bext[2]};
+    const BoxGeom Gcor{S.H.o_cor[0], S.H.o_cor[1], S.H.o_cor[2], K.bext[0], K.bext[1], K.bext[2]};
     unsigned long long n_eval = 0, n_undef = 0, n_slow = 0;
     if (tid == 0) S.fail = 0;
     pc.to(1);
@@ -1240,19 +1286,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int d = 0; d < 3; d++) {
         split_d(__dsub_rn(S.H.pt[d], (double)S.H.o_ref[d]), S.pi[d], S.pf[d]);
         split_d(__dsub_rn(__dadd_rn(S.H.pt[d], S.H.seed[d]), (double)S.H.o_cor[d]), S.qi[d], S.qf[d]);
-        if (a.geom == DVC_SPHERE) {
-          S.sbmn[d] = __dadd_rn(S.H.pt[d], a.off_min[d]);
-          S.sbmx[d] = __dadd_rn(S.H.pt[d], a.off_max[d]);
+        if (K.geom == DVC_SPHERE) {
+          S.sbmn[d] = __dadd_rn(S.H.pt[d], K.off_min[d]);
+          S.sbmx[d] = __dadd_rn(S.H.pt[d], K.off_max[d]);
         } else {
-          const double r = __dmul_rn(a.subv_rad, a.aspect[d]);
+          const double r = __dmul_rn(K.subv_rad, K.aspect[d]);
           const double bmin = __dadd_rn(S.H.pt[d], -r);
           const double bmax = __dadd_rn(S.H.pt[d], r);
-          const double inc = __ddiv_rn(__dsub_rn(bmax, bmin), (double)(a.cube_n - 1));
+          const double inc = __ddiv_rn(__dsub_rn(bmax, bmin), (double)(K.cube_n - 1));
           S.sbmn[d] = bmin;
-          S.sbmx[d] = __dadd_rn(bmin, __dmul_rn((double)(a.cube_n - 1), inc));
+          S.sbmx[d] = __dadd_rn(bmin, __dmul_rn((double)(K.cube_n - 1), inc));
         }
-        S.lbmn[d] = __dadd_rn(S.H.pt[d], a.rank_off_min[cl.rank][d]);  // this CTA's share
-        S.lbmx[d] = __dadd_rn(S.H.pt[d], a.rank_off_max[cl.rank][d]);
+        S.lbmn[d] = __dadd_rn(S.H.pt[d], K.rank_off_min[cl.rank][d]);  // this CTA's share
+        S.lbmx[d] = __dadd_rn(S.H.pt[d], K.rank_off_max[cl.rank][d]);
       }
     }
     __syncthreads();
@@ -1263,8 +1309,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         float f[3], fp[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-          const int oi = a.off_i[(size_t)(lo + i) * 3 + d];
-          const float of = a.off_f[(size_t)(lo + i) * 3 + d];
+          const int oi = K.off_i[(size_t)(lo + i) * 3 + d];
+          const float of = K.off_f[(size_t)(lo + i) * 3 + d];
           const float F = S.pf[d] + of, G = S.qf[d] + of;
           const float fl = floorf(F), gl = floorf(G);
           c[d] = S.pi[d] + oi + (int)fl;
@@ -1272,7 +1318,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           ip[d] = min(max(S.qi[d] + oi + (int)gl, 0), 1023);
           fp[d] = G - gl;
         }
-        clamp_cell(c, a.bext);
+        clamp_cell(c, K.bext);
         bool und;
         float g[3];
         const float r = interp_global<VT, IT, false>(gsr, Gref, c, f, g, und);
@@ -1290,10 +1336,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (tid == 0) {
       for (int d = 0; d < 3; d++) {
         // stable reference point (FloatingCloud: centre, or middle of the cube box)
-        if (a.geom == DVC_SPHERE) {
+        if (K.geom == DVC_SPHERE) {
           S.sref[d] = S.H.pt[d];
         } else {
-          const double r = __dmul_rn(a.subv_rad, a.aspect[d]);
+          const double r = __dmul_rn(K.subv_rad, K.aspect[d]);
           S.sref[d] = __ddiv_rn(__dadd_rn(__dadd_rn(S.H.pt[d], r), __dadd_rn(S.H.pt[d], -r)), 2.0);
         }
         int ki;
@@ -1344,11 +1390,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     // translation whose sample box leaves the active box fails the point.
     // The correlate region of each translation is staged by TMA into one of
     // two buffers while the previous translation is evaluated.
-    if (a.do_grid && a.seed_mode != DVC_SEED_PARAMS) {
-      const int k = a.num_inc;
+    if (K.do_grid && a.seed_mode != DVC_SEED_PARAMS) {
+      const int k = K.num_inc;
       const int side = 2 * k + 1;
       const int total = side * side * side;
-      const double inc = a.inc;
+      const double inc = K.inc;
       // range check of every translation first (exact FP64; one thread each)
       {
         int bad = 0;
@@ -1374,9 +1420,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           pmn[d] = S.lbmn[d] + S.par[d] - k * inc;
           pmx[d] = S.lbmx[d] + S.par[d] + k * inc;
         }
-        Region r = make_region(a, pmn, pmx, esize);
+        Region r = make_region(K, pmn, pmx, esize);
         S.reg[0] = r;
-        if (r.ok) tma_load_3d(&tmap, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
+        if (r.ok) tma_load_3d(tmp, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
       }
       __syncthreads();
       const Region rg = S.reg[0];
@@ -1397,7 +1443,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
         __syncthreads();
-        if (IT != 0 && rg.ok && a.inc_int > 0) {
+        if (IT != 0 && rg.ok && K.inc_int > 0) {
           grid_chunk_lanes<VT, IT>(a, S, s_ip, s_fp, s_r, nl, s_G, ss, rg.r0, B, gsc, Gcor, o0, nch,
                                    side, k, cl.parity, sad, n_undef, n_slow);
         } else {
@@ -1414,7 +1460,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               int c[3];
               float f[3], g[3];
               sample_pos(s_ip, s_fp, i, S, iu, fu, false, c, f);
-              clamp_cell(c, a.bext);
+              clamp_cell(c, K.bext);
               bool und;
               const float t = eval_sample_t<VT, IT, false, ST>(ss, rg.r0, B, gsc, Gcor, c, f, g, und) - S.shift;
               n_undef += und;
@@ -1548,11 +1594,11 @@ __global__ void __launch_bounds__(kThreads, 1)
               }
             }
           }
-          if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, &tmap, buf_addr[0], bar_addr[0], stage_tx);
+          if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, tmp, buf_addr[0], bar_addr[0], stage_tx);
           __syncthreads();
         } else if (tid == 0) {
           // restage when the last evaluation's positions left the region
-          S.stop = S.lrange ? restage(a, S, S.lpmn, S.lpmx, esize, &tmap, buf_addr[0], bar_addr[0],
+          S.stop = S.lrange ? restage(a, S, S.lpmn, S.lpmx, esize, tmp, buf_addr[0], bar_addr[0],
                                       stage_tx)
                             : 0;
           S.lrange = 0;
@@ -1582,7 +1628,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             float f[3], gv[3];
             sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
             if (rot) key_update(kv, c, f);
-            clamp_cell(c, a.bext);
+            clamp_cell(c, K.bext);
             bool und;
             t = (rg.ok ? eval_sample_t<VT, IT, true, true>(ss, rg.r0, B, gsc, Gcor, c, f, gv, und)
                        : eval_sample_t<VT, IT, true, false>(ss, rg.r0, B, gsc, Gcor, c, f, gv, und)) -
@@ -1811,7 +1857,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
       n_eval += 1;
       if (S.fail) goto point_done;
-      if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, &tmap, buf_addr[0], bar_addr[0], stage_tx);
+      if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, tmp, buf_addr[0], bar_addr[0], stage_tx);
       __syncthreads();
       const Region rg = S.reg[0];
       if (S.stop) {
@@ -1825,7 +1871,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           int c[3];
           float f[3], g[3];
           sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
-          clamp_cell(c, a.bext);
+          clamp_cell(c, K.bext);
           bool und;
           const float t = (rg.ok ? eval_sample_t<VT, IT, false, true>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)
                                  : eval_sample_t<VT, IT, false, false>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)) -

@@ -4,8 +4,9 @@
 // value(x) = background + sum_b amp_b exp(-|X(x) - c_b|^2 / (2 sigma_b^2)) + noise
 // where X(x) is the reference position of voxel x under the deformation
 // (X + u(X) = x; affine: solved, sinusoid and bump field: fixed-point
-// iteration, their gradients being well below 1), blobs contribute within 4
-// sigma, noise ~ N(0, noise_sigma)
+// iteration, their gradients being well below 1; two affine pieces split by
+// the plane X_x = split: piece 1's solution where it lies left of the plane,
+// else piece 2's), blobs contribute within 4 sigma, noise ~ N(0, noise_sigma)
 // from a counter-based hash of (seed, voxel index), then the value is rounded
 // and clipped to [0, vmax]. Blobs are binned on the host by their deformed
 // centre so each voxel visits only the blobs of its 27 neighbouring bins.
@@ -29,7 +30,8 @@ struct SynthArgs {
   int nx, ny, nz, bpv;
   int gx, gy, gz;             // bin grid
   const float4 *blobs;        // x y z 1/(2 sigma^2), sorted by bin
-  const float2 *amp_r2;       // amplitude, (4 sigma)^2
+  const float2 *amp_r2;       // amplitude, (4 sigma)^2; split field: negative amplitude
+                              // for the copy binned by piece 2
   const int *bin_start;       // gx*gy*gz + 1
   int deform;
   float Ainv[9], t[3], c[3];  // affine: X = c + Ainv (x - t - c)
@@ -38,6 +40,8 @@ struct SynthArgs {
   float E[9];
   int nbump;
   float bump[kMaxBumps][7];   // p (3), 1/(2 s^2), a (3)
+  // split field: piece 2's X = c2 + Ainv2 (x - t2 - c2), the plane X_x = split
+  float Ainv2[9], t2[3], c2[3], split;
   float background, noise_sigma, vmax;
   unsigned long long seed;
 };
@@ -57,10 +61,18 @@ __global__ void synth_kernel(SynthArgs a) {
     const int y = (int)((idx / a.nx) % a.ny);
     const int z = (int)(idx / ((long long)a.nx * a.ny));
     float X[3] = {(float)x, (float)y, (float)z};
-    if (a.deform == 1) {
+    bool piece2 = false;
+    if (a.deform == 1 || a.deform == 4) {
+      const float x0[3] = {X[0], X[1], X[2]};
       const float r[3] = {X[0] - a.t[0] - a.c[0], X[1] - a.t[1] - a.c[1], X[2] - a.t[2] - a.c[2]};
       for (int i = 0; i < 3; i++)
         X[i] = a.c[i] + a.Ainv[i * 3 + 0] * r[0] + a.Ainv[i * 3 + 1] * r[1] + a.Ainv[i * 3 + 2] * r[2];
+      if (a.deform == 4 && !(X[0] < a.split)) {
+        piece2 = true;
+        const float q[3] = {x0[0] - a.t2[0] - a.c2[0], x0[1] - a.t2[1] - a.c2[1], x0[2] - a.t2[2] - a.c2[2]};
+        for (int i = 0; i < 3; i++)
+          X[i] = a.c2[i] + a.Ainv2[i * 3 + 0] * q[0] + a.Ainv2[i * 3 + 1] * q[1] + a.Ainv2[i * 3 + 2] * q[2];
+      }
     } else if (a.deform == 3) {
       const float x0[3] = {X[0], X[1], X[2]};
       for (int it = 0; it < 12; it++) {
@@ -105,7 +117,8 @@ __global__ void synth_kernel(SynthArgs a) {
             const float ex = X[0] - bl.x, ey = X[1] - bl.y, ez = X[2] - bl.z;
             const float d2 = ex * ex + ey * ey + ez * ez;
             const float2 ar = a.amp_r2[k];
-            if (d2 <= ar.y) v += ar.x * __expf(-d2 * bl.w);
+            if (a.deform == 4 && ((ar.x < 0.f) != piece2)) continue;  // the other piece's copy
+            if (d2 <= ar.y) v += (a.deform == 4 ? fabsf(ar.x) : ar.x) * __expf(-d2 * bl.w);
           }
         }
       }
@@ -131,7 +144,7 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
                                     const double *coef, float background, float noise_sigma,
                                     unsigned long long noise_seed, float vmax, void *stream) {
   if (!vol_dev || nx <= 0 || ny <= 0 || nz <= 0 || (bytes_per_voxel != 1 && bytes_per_voxel != 2) ||
-      n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 3 || (deform && !coef))
+      n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 4 || (deform && !coef))
     return dvc_internal_set_error(DVC_E_ARG, "bad synth arguments");
   SynthArgs a{};
   a.vol = vol_dev;
@@ -148,25 +161,35 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
   a.vmax = vmax;
   a.seed = noise_seed;
   // deformed blob centres and bins (host)
-  double Ainv[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-  if (deform == 1) {
-    const double *E = coef + 3;
+  // inverse of I + E (E row-major)
+  auto inverse = [](const double *E, float out[9]) {
     const double A[9] = {1 + E[0], E[1], E[2], E[3], 1 + E[4], E[5], E[6], E[7], 1 + E[8]};
     const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
                        A[2] * (A[3] * A[7] - A[4] * A[6]);
-    Ainv[0] = (A[4] * A[8] - A[5] * A[7]) / det;
-    Ainv[1] = (A[2] * A[7] - A[1] * A[8]) / det;
-    Ainv[2] = (A[1] * A[5] - A[2] * A[4]) / det;
-    Ainv[3] = (A[5] * A[6] - A[3] * A[8]) / det;
-    Ainv[4] = (A[0] * A[8] - A[2] * A[6]) / det;
-    Ainv[5] = (A[2] * A[3] - A[0] * A[5]) / det;
-    Ainv[6] = (A[3] * A[7] - A[4] * A[6]) / det;
-    Ainv[7] = (A[1] * A[6] - A[0] * A[7]) / det;
-    Ainv[8] = (A[0] * A[4] - A[1] * A[3]) / det;
-    for (int i = 0; i < 9; i++) a.Ainv[i] = (float)Ainv[i];
+    const double inv[9] = {(A[4] * A[8] - A[5] * A[7]) / det, (A[2] * A[7] - A[1] * A[8]) / det,
+                           (A[1] * A[5] - A[2] * A[4]) / det, (A[5] * A[6] - A[3] * A[8]) / det,
+                           (A[0] * A[8] - A[2] * A[6]) / det, (A[2] * A[3] - A[0] * A[5]) / det,
+                           (A[3] * A[7] - A[4] * A[6]) / det, (A[1] * A[6] - A[0] * A[7]) / det,
+                           (A[0] * A[4] - A[1] * A[3]) / det};
+    for (int i = 0; i < 9; i++) out[i] = (float)inv[i];
+  };
+  if (deform == 1 || deform == 4) {
+    // coef: t (3), E (9), c (3); split field: then piece 2's t, E, c and the plane
+    inverse(coef + 3, a.Ainv);
     for (int i = 0; i < 3; i++) {
       a.t[i] = (float)coef[i];
       a.c[i] = (float)coef[12 + i];
+    }
+    if (deform == 4) {
+      inverse(coef + 18, a.Ainv2);
+      for (int i = 0; i < 3; i++) {
+        a.t2[i] = (float)coef[15 + i];
+        a.c2[i] = (float)coef[27 + i];
+      }
+      a.split = (float)coef[30];
+      for (int k = 0; k < n_blobs; k++)
+        if (!(blobs[(size_t)k * 5 + 4] >= 0.f))
+          return dvc_internal_set_error(DVC_E_ARG, "a split field needs blob amplitudes >= 0");
     }
   } else if (deform == 2) {
     a.amp = (float)coef[0];
@@ -193,15 +216,20 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
     }
   }
   const int nbins = a.gx * a.gy * a.gz;
-  std::vector<int> bin_of((size_t)n_blobs), count((size_t)nbins + 1, 0);
-  for (int k = 0; k < n_blobs; k++) {
+  // one entry per blob; a split field has two, each binned by one piece's
+  // map (entry k + n_blobs: piece 2's, stored with a negative amplitude)
+  const int n_entries = deform == 4 ? 2 * n_blobs : n_blobs;
+  std::vector<int> bin_of((size_t)n_entries), count((size_t)nbins + 1, 0);
+  for (int e = 0; e < n_entries; e++) {
+    const int k = e % std::max(n_blobs, 1);
     const float *b = blobs + (size_t)k * 5;
     double X[3] = {b[0], b[1], b[2]}, x[3] = {b[0], b[1], b[2]};
-    if (deform == 1) {
-      const double *E = coef + 3;
+    if (deform == 1 || deform == 4) {
+      const double *P = coef + (e >= n_blobs ? 15 : 0);  // t (3), E (9), c (3)
+      const double *E = P + 3;
       for (int i = 0; i < 3; i++)
-        x[i] = X[i] + coef[i] + E[i * 3 + 0] * (X[0] - coef[12]) + E[i * 3 + 1] * (X[1] - coef[13]) +
-               E[i * 3 + 2] * (X[2] - coef[14]);
+        x[i] = X[i] + P[i] + E[i * 3 + 0] * (X[0] - P[12]) + E[i * 3 + 1] * (X[1] - P[13]) +
+               E[i * 3 + 2] * (X[2] - P[14]);
     } else if (deform == 2) {
       const double w = 2.0 * M_PI / coef[1];
       x[0] = X[0] + coef[0] * sin(w * X[1]);
@@ -223,20 +251,21 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
     int bx = std::min(std::max((int)floor(x[0] / kBin), 0), a.gx - 1);
     int by = std::min(std::max((int)floor(x[1] / kBin), 0), a.gy - 1);
     int bz = std::min(std::max((int)floor(x[2] / kBin), 0), a.gz - 1);
-    bin_of[(size_t)k] = (bz * a.gy + by) * a.gx + bx;
-    count[(size_t)bin_of[(size_t)k] + 1]++;
+    bin_of[(size_t)e] = (bz * a.gy + by) * a.gx + bx;
+    count[(size_t)bin_of[(size_t)e] + 1]++;
   }
   for (int b = 0; b < nbins; b++) count[(size_t)b + 1] += count[(size_t)b];
   std::vector<int> fill(count.begin(), count.end() - 1);
-  std::vector<float> h_blob((size_t)std::max(n_blobs, 1) * 4), h_ar((size_t)std::max(n_blobs, 1) * 2);
-  for (int k = 0; k < n_blobs; k++) {
+  std::vector<float> h_blob((size_t)std::max(n_entries, 1) * 4), h_ar((size_t)std::max(n_entries, 1) * 2);
+  for (int e = 0; e < n_entries; e++) {
+    const int k = e % std::max(n_blobs, 1);
     const float *b = blobs + (size_t)k * 5;
-    const int pos = fill[(size_t)bin_of[(size_t)k]]++;
+    const int pos = fill[(size_t)bin_of[(size_t)e]]++;
     h_blob[(size_t)pos * 4 + 0] = b[0];
     h_blob[(size_t)pos * 4 + 1] = b[1];
     h_blob[(size_t)pos * 4 + 2] = b[2];
     h_blob[(size_t)pos * 4 + 3] = 1.0f / (2.0f * b[3] * b[3]);
-    h_ar[(size_t)pos * 2 + 0] = b[4];
+    h_ar[(size_t)pos * 2 + 0] = e >= n_blobs ? -b[4] : b[4];
     h_ar[(size_t)pos * 2 + 1] = 16.0f * b[3] * b[3];
   }
   // blobs reach 4 sigma; bins are 16 voxels and neighbours one bin away, so

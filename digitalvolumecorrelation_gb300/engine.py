@@ -16,7 +16,7 @@ import os
 
 import numpy as np
 
-from .abi import (DvcParams, DvcStats, E_RANGE, OK, SEED_GIVEN, SEED_NEIGHBOURS, SEED_PARAMS,
+from .abi import (DvcParams, DvcStats, E_ARG, E_RANGE, OK, SEED_GIVEN, SEED_NEIGHBOURS, SEED_PARAMS,
                   SEED_RIGID, make_params)
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
@@ -77,6 +77,20 @@ def load(path: str | None = None):
                                           C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.POINTER(C.c_int), C.c_void_p]
     L.dvc_gpu_order_neighbours.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip]
+    L.dvc_gpu_set_cluster.argtypes = [C.c_void_p, C.c_int]
+    L.dvc_gpu_plan_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int]
+    L.dvc_gpu_plan_destroy.argtypes = [C.c_void_p]
+    L.dvc_gpu_plan_destroy.restype = None
+    L.dvc_gpu_plan_info.argtypes = [C.c_void_p, _ip, _ip, _ip, C.POINTER(C.c_longlong)]
+    L.dvc_gpu_plan_set_shape.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.dvc_gpu_plan_process_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                              C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.dvc_gpu_plan_process.argtypes = [C.c_void_p, _ip, C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int,
+                                       _dp, _ip, _dp, _dp, _ip, C.POINTER(DvcStats)]
+    L.dvc_gpu_plan_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                        C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_int, _dp]
     L.dvc_gpu_synth_volume.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.POINTER(C.c_float), C.c_int, _dp, C.c_float, C.c_float,
                                        C.c_ulonglong, C.c_float, C.c_void_p]
@@ -125,33 +139,15 @@ class Engine:
         except Exception:
             pass
 
+    def set_cluster(self, cluster):
+        """CTAs per point for this engine's searches (1, 2, 4, 8; 0: chosen per call)."""
+        _check(_lib.dvc_gpu_set_cluster(self._h, int(cluster)))
+
     def process(self, points, order=None, neigh=None, n_process=None, seed_mode=SEED_NEIGHBOURS,
                 seeds=None):
         """Search::process_point over `order` (Core/dvc.cpp:233-303)."""
-        pts = np.ascontiguousarray(points, np.float64)
-        n = len(pts)
-        order = np.arange(n, dtype=np.int32) if order is None else np.ascontiguousarray(order, np.int32)
-        n_process = len(order) if n_process is None else int(n_process)
-        nn = 0
-        neigh_p = None
-        if neigh is not None and seed_mode == SEED_NEIGHBOURS:
-            neigh = np.ascontiguousarray(neigh, np.int32)
-            nn = neigh.shape[1]
-            neigh_p = _p(neigh, _ip)
-        seeds_p = None
-        if seed_mode in (SEED_GIVEN, SEED_PARAMS):
-            seeds = np.ascontiguousarray(seeds, np.float64)
-            seeds_p = _p(seeds, _dp)
-        status = np.zeros(n, np.int32)
-        objmin = np.zeros(n)
-        par = np.zeros((n, 12))
-        its = np.zeros(n, np.int32)
-        st = DvcStats()
-        _check(_lib.dvc_gpu_process(self._h, n, _p(pts, _dp), n_process, _p(order, _ip), nn,
-                                    neigh_p, int(seed_mode), seeds_p, _p(status, _ip),
-                                    _p(objmin, _dp), _p(par, _dp), _p(its, _ip), C.byref(st)))
-        return dict(status=status, objmin=objmin, params=par, gn_iters=its,
-                    stats={f: getattr(st, f) for f, _ in DvcStats._fields_})
+        return _host_search(lambda *args: _lib.dvc_gpu_process(self._h, *args), points, order, neigh,
+                            n_process, seed_mode, seeds)
 
     def process_device(self, n_points, points_dev, order_dev, n_process, neigh_dev, n_neigh,
                        seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev=None,
@@ -202,6 +198,94 @@ class Engine:
             return None
         _check(rc)
         return out
+
+
+def _host_search(call, points, order, neigh, n_process, seed_mode, seeds):
+    """Host arrays in, the C search call, result arrays and stats out."""
+    pts = np.ascontiguousarray(points, np.float64)
+    n = len(pts)
+    order = np.arange(n, dtype=np.int32) if order is None else np.ascontiguousarray(order, np.int32)
+    n_process = len(order) if n_process is None else int(n_process)
+    nn = 0
+    neigh_p = None
+    if neigh is not None and seed_mode == SEED_NEIGHBOURS:
+        neigh = np.ascontiguousarray(neigh, np.int32)
+        nn = neigh.shape[1]
+        neigh_p = _p(neigh, _ip)
+    seeds_p = None
+    if seed_mode in (SEED_GIVEN, SEED_PARAMS):
+        seeds = np.ascontiguousarray(seeds, np.float64)
+        seeds_p = _p(seeds, _dp)
+    status = np.zeros(n, np.int32)
+    objmin = np.zeros(n)
+    par = np.zeros((n, 12))
+    its = np.zeros(n, np.int32)
+    st = DvcStats()
+    _check(call(n, _p(pts, _dp), n_process, _p(order, _ip), nn, neigh_p, int(seed_mode), seeds_p,
+                _p(status, _ip), _p(objmin, _dp), _p(par, _dp), _p(its, _ip), C.byref(st)))
+    return dict(status=status, objmin=objmin, params=par, gn_iters=its,
+                stats={f: getattr(st, f) for f, _ in DvcStats._fields_})
+
+
+class Plan:
+    """Several search configurations (engines on the same volumes) searched in
+    one launch, each point by its own configuration (dvc_gpu_plan_*)."""
+
+    def __init__(self, engines, cluster=0):
+        L = load()
+        self.engines = list(engines)  # the plan uses their sample tables
+        arr = (C.c_void_p * len(self.engines))(*[e._h.value for e in self.engines])
+        self._h = C.c_void_p()
+        _check(L.dvc_gpu_plan_create(C.byref(self._h), arr, len(self.engines), int(cluster)))
+
+    def close(self):
+        if self._h:
+            _lib.dvc_gpu_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        """dict(cluster, staging, n_staged, smem_bytes) of the launch shape."""
+        c, s, n = C.c_int(), C.c_int(), C.c_int()
+        m = C.c_longlong()
+        _check(_lib.dvc_gpu_plan_info(self._h, C.byref(c), C.byref(s), C.byref(n), C.byref(m)))
+        return dict(cluster=c.value, staging=s.value, n_staged=n.value, smem_bytes=m.value)
+
+    def set_shape(self, cluster, staging=1):
+        _check(_lib.dvc_gpu_plan_set_shape(self._h, int(cluster), int(staging)))
+
+    def process(self, point_cfg, points, order=None, neigh=None, n_process=None,
+                seed_mode=SEED_NEIGHBOURS, seeds=None):
+        cfg = np.ascontiguousarray(point_cfg, np.int32)
+        return _host_search(lambda *args: _lib.dvc_gpu_plan_process(self._h, _p(cfg, _ip), *args), points,
+                            order, neigh, n_process, seed_mode, seeds)
+
+    def process_device(self, point_cfg_dev, n_points, points_dev, order_dev, n_process, neigh_dev, n_neigh,
+                       seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev=None,
+                       stream=0):
+        ptr = lambda t: C.c_void_p(_dev_ptr(t)) if t is not None else None
+        _check(_lib.dvc_gpu_plan_process_device(self._h, ptr(point_cfg_dev), int(n_points), ptr(points_dev),
+                                                int(n_process), ptr(order_dev), int(n_neigh), ptr(neigh_dev),
+                                                int(seed_mode), ptr(seeds_dev), ptr(status_dev),
+                                                ptr(objmin_dev), ptr(params_dev), ptr(gn_iters_dev),
+                                                C.c_void_p(stream)))
+
+    def autotune(self, point_cfg_dev, n_points, points_dev, order_dev, n_process, neigh_dev, n_neigh,
+                 seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, reps=2):
+        """Time every launch shape on these points and keep the fastest;
+        returns {(cluster, staging): mean ms} of the shapes that fit."""
+        ptr = lambda t: C.c_void_p(_dev_ptr(t)) if t is not None else None
+        ms = np.zeros(8)
+        _check(_lib.dvc_gpu_plan_autotune(self._h, ptr(point_cfg_dev), int(n_points), ptr(points_dev),
+                                          int(n_process), ptr(order_dev), int(n_neigh), ptr(neigh_dev),
+                                          int(seed_mode), ptr(seeds_dev), ptr(status_dev), ptr(objmin_dev),
+                                          ptr(params_dev), int(reps), _p(ms, _dp)))
+        return {(1 << (j // 2), j % 2): float(ms[j]) for j in range(8) if ms[j] >= 0}
 
 
 class Cnn:
@@ -327,5 +411,5 @@ def synth_volume_device(vol_dev, shape_xyz, bytes_per_voxel, blobs, deform=None,
                                      C.c_void_p(stream)))
 
 
-__all__ = ["Engine", "Cnn", "objective", "strain", "order_neighbours", "synth_volume_device", "make_params", "load",
-           "DvcError", "SEED_NEIGHBOURS", "SEED_GIVEN", "SEED_RIGID", "SEED_PARAMS"]
+__all__ = ["Engine", "Plan", "Cnn", "objective", "strain", "order_neighbours", "synth_volume_device", "make_params", "load",
+           "DvcError", "E_ARG", "SEED_NEIGHBOURS", "SEED_GIVEN", "SEED_RIGID", "SEED_PARAMS"]

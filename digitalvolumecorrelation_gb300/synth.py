@@ -115,6 +115,49 @@ def random_bumps(shape_xyz, rng, max_disp=10.0, max_strain=0.02, n_bumps=12):
 
 
 @dataclass
+class Piecewise:
+    """Two affine fields split by the plane X_x = split (reference positions):
+    u = t1 + E1 (X - c1) where X_x < split, else t2 + E2 (X - c2). The field
+    jumps across the plane."""
+    t1: tuple = (0.0, 0.0, 0.0)
+    E1: tuple = ((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+    c1: tuple = (0.0, 0.0, 0.0)
+    t2: tuple = (0.0, 0.0, 0.0)
+    E2: tuple = ((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+    c2: tuple = (0.0, 0.0, 0.0)
+    split: float = 0.0
+
+    def _pieces(self):
+        return Affine(self.t1, self.E1, self.c1), Affine(self.t2, self.E2, self.c2)
+
+    def u(self, X):
+        X = np.asarray(X, dtype=np.float64)
+        a, b = self._pieces()
+        left = (X[..., 0] < self.split)[..., None]
+        return np.where(left, a.u(X), b.u(X))
+
+    def inverse(self, x):
+        """Piece 1's inverse where it lands left of the plane, else piece 2's
+        (the device renderer's rule)."""
+        a, b = self._pieces()
+        X1 = a.inverse(x)
+        return np.where((X1[..., 0] < self.split)[..., None], X1, b.inverse(x))
+
+    def coef(self):
+        return [*self.t1, *np.asarray(self.E1).ravel(), *self.c1, *self.t2, *np.asarray(self.E2).ravel(),
+                *self.c2, float(self.split)]
+
+    kind = 4
+
+
+def rotation_z(deg):
+    """R - I for a rotation by `deg` degrees about the z axis."""
+    th = math.radians(deg)
+    c, s = math.cos(th), math.sin(th)
+    return ((c - 1.0, -s, 0.0), (s, c - 1.0, 0.0), (0.0, 0.0, 0.0))
+
+
+@dataclass
 class Identity:
     def u(self, X):
         return np.zeros_like(np.asarray(X, np.float64))
@@ -154,10 +197,13 @@ def render(shape_xyz, blob_list, deform=None, noise_sigma=2.0, noise_seed=2, bac
     nx, ny, nz = shape_xyz
     field = np.full((nz, ny, nx), background, dtype=np.float64)
     for bx, by, bz, s, a in blob_list:
-        centre = np.array([bx, by, bz]) + deform.u(np.array([bx, by, bz]))
+        # the blob's image under the field (under each piece of a split field)
+        X0 = np.array([bx, by, bz], np.float64)
+        fields = deform._pieces() if isinstance(deform, Piecewise) else (deform,)
+        img = np.array([X0 + f.u(X0) for f in fields])
         r = reach * s * 1.1 + 1.0
-        lo = np.maximum(np.floor(centre - r).astype(int), 0)
-        hi = np.minimum(np.ceil(centre + r).astype(int) + 1, [nx, ny, nz])
+        lo = np.maximum(np.floor(img.min(0) - r).astype(int), 0)
+        hi = np.minimum(np.ceil(img.max(0) + r).astype(int) + 1, [nx, ny, nz])
         if np.any(hi <= lo):
             continue
         zz, yy, xx = np.meshgrid(np.arange(lo[2], hi[2]), np.arange(lo[1], hi[1]),

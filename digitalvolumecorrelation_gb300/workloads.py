@@ -15,6 +15,17 @@ configuration. Volumes are rendered on the GPU by `dvc_gpu_synth_volume`
       40 x 40 x 38 = 60,800-point grid (spacing 24); sphere of diameter 41 /
       4000 samples, znssd, tricubic, 12 dof; disp_max 6 and basin_radius 3
       (chosen here: the configuration leaves them open).
+  config 3 ("batching, uneven workload"): 768^3 uint8, one blob per 1000
+      voxels (sigma 1.5-3, amplitude 40-200), noise sigma 2; target = a split
+      field: left of x = 384 a rigid rotation of 1.5 degrees about the z axis
+      through (192, 384, 384) plus a translation (1, -0.5, 0.5), right of it
+      1% uniaxial compression along z about z = 384; 40,000 ROI points at
+      uniform random positions (64 voxels from the faces; the first at the
+      rotation centre, where the processing order starts), each point its own
+      configuration: subvol_size from {21, 31, 41, 61, 81}, cube or sphere,
+      subvol_npts = 0.15 x the subvolume's voxel count (at most the
+      reference's 50,000), 3, 6 or 12 dof, ssd or znssd; tricubic, disp_max 8
+      and basin_radius 4 (chosen here); strain window 7.
 """
 from __future__ import annotations
 
@@ -92,6 +103,49 @@ def config2(grid=(40, 40, 38), spacing=24.0):
     b = synth.blobs(shape, n_blobs, sigma=(1.5, 3.0), amp=(2000.0, 60000.0), seed=2)
     return Workload("config2_1024cube_u16_60800pts_sphere41_dof12", shape, 2, kw, pts, deform, b,
                     150.0, 201, 202)
+
+
+CONFIG3_SIZES = (21, 31, 41, 61, 81)
+CONFIG3_GEOMS = ("cube", "sphere")
+CONFIG3_DOFS = (3, 6, 12)
+CONFIG3_OBJS = ("ssd", "znssd")
+
+
+def config3_settings():
+    """The 60 search configurations of configuration 3, index
+    ((size * 2 + geom) * 3 + dof) * 2 + objective."""
+    out = []
+    for size in CONFIG3_SIZES:
+        for geom in CONFIG3_GEOMS:
+            vox = size ** 3 if geom == "cube" else 4.0 / 3.0 * np.pi * (size / 2.0) ** 3
+            npts = int(min(50000, round(0.15 * vox)))
+            for dof in CONFIG3_DOFS:
+                for obj in CONFIG3_OBJS:
+                    out.append(dict(subvol_geom=geom, subvol_size=size, subvol_npts=npts, obj_function=obj,
+                                    interp_type="tricubic", num_srch_dof=dof, disp_max=8, basin_radius=4.0))
+    return out
+
+
+def config3(n_points=40000, shape=(768, 768, 768), seed=3):
+    """Returns (workload, per-point configuration index, configuration list);
+    the workload's params_kw is the first configuration's (volumes only)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    split = nx / 2.0
+    rc = (nx / 4.0, ny / 2.0, nz / 2.0)
+    deform = synth.Piecewise(t1=(1.0, -0.5, 0.5), E1=synth.rotation_z(1.5), c1=rc,
+                             t2=(0.0, 0.0, 0.0), E2=((0, 0, 0), (0, 0, 0), (0, 0, -0.01)),
+                             c2=(nx / 2.0, ny / 2.0, nz / 2.0), split=split)
+    margin = 64.0
+    pts = rng.uniform(margin, np.array(shape, np.float64) - margin, (n_points, 3))
+    pts[0] = rc
+    settings = config3_settings()
+    cfg = rng.integers(0, len(settings), n_points).astype(np.int32)
+    n_blobs = int(np.prod(shape) // 1000)
+    b = synth.blobs(shape, n_blobs, sigma=(1.5, 3.0), amp=(40.0, 200.0), seed=seed + 30)
+    W = Workload("config3_768cube_u8_40000pts_mixed60", shape, 1, settings[0], pts, deform, b, 2.0,
+                 seed + 301, seed + 302)
+    return W, cfg, settings
 
 
 def order_and_neighbours(points, n_neigh=75, start=None):

@@ -174,6 +174,14 @@ int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *po
                                    int *status_dev, double *objmin_dev, double *params_dev,
                                    int *gn_iters_dev, void *stream);
 
+/* CTAs per point (one cluster) for this engine's searches: 1, 2, 4 or 8, or
+   0 (the default, or the DVC_CLUSTER environment variable at creation) to
+   choose per call from the sample count and seeding. A width whose staging
+   box or sample state does not fit is widened. The search's results depend
+   on the width only through FP32/FP64 summation order. No counterpart in
+   the reference (one thread per point). */
+int dvc_gpu_set_cluster(dvc_engine *e, int cluster);
+
 /* Counters of the most recent dvc_gpu_process / dvc_gpu_process_device call
    on this engine (waits for it to finish): out[0] objective evaluations
    (reference subvolume, grid offsets, Gauss-Newton evaluations, final
@@ -194,6 +202,63 @@ int dvc_gpu_last_counters(dvc_engine *e, long long out[3]);
    counterpart in the reference (it has no per-phase timing). */
 #define DVC_N_PHASES 11
 int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]);
+
+/* ---- several search configurations in one launch -------------------------
+ * The reference runs one configuration per `dvc` run: every point of the
+ * cloud is searched by Search::process_point (Core/Search.cpp:95-192) with the
+ * run's one RunControl (Core/dvc.cpp:233-303). A plan holds several
+ * configurations, each an engine from dvc_gpu_create / dvc_gpu_create_device
+ * (its dvc_params: subvolume geometry, size and sample count, search degrees
+ * of freedom, objective, grid), all on the same volumes (the same ref and
+ * correlate buffers, dimensions, voxel type and interpolation). Each point
+ * names its configuration; one persistent launch searches every point, its
+ * clusters taking the next point from the work queue whatever its
+ * configuration, and each point's result is the one its configuration's own
+ * engine would give at the same cluster width. The engines must outlive the
+ * plan; the plan's calls use the first engine's workspace and counters
+ * (dvc_gpu_last_counters on configs[0]).
+ *   cluster   CTAs per point (1, 2, 4 or 8), or 0 to choose from the sample
+ *             counts; every configuration must fit the shared memory of a
+ *             CTA at that width (DVC_E_ARG otherwise) */
+typedef struct dvc_plan dvc_plan;
+int dvc_gpu_plan_create(dvc_plan **out, dvc_engine *const *configs, int n_configs, int cluster);
+void dvc_gpu_plan_destroy(dvc_plan *plan);
+/* The plan's launch shape: CTAs per point, whether the correlate volume is
+   staged in shared memory (TMA) for the configurations whose box fits, how
+   many configurations are staged, dynamic shared memory per CTA. */
+int dvc_gpu_plan_info(const dvc_plan *plan, int *cluster, int *staging, int *n_staged,
+                      long long *smem_bytes);
+/* Rebuild the plan at another launch shape (cluster 1, 2, 4 or 8; staging 0
+   or 1). Waits for the device first. */
+int dvc_gpu_plan_set_shape(dvc_plan *plan, int cluster, int staging);
+/* Search with point_cfg[i] in 0..n_configs-1 the configuration of point i;
+   every other argument as dvc_gpu_process_device. Enqueued on `stream`. A
+   point whose configuration index is out of range is left unsearched
+   (DVC_NOT_SEARCH) and the launch's error flag records DVC_E_ARG. The first
+   call with a given point count may grow the workspace (a device
+   allocation): make it before capturing later calls in a CUDA graph. */
+int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_points,
+                                const double *points_dev, int n_process, const int *order_dev,
+                                int n_neigh, const int *neigh_dev, int seed_mode,
+                                const double *seeds_dev, int *status_dev, double *objmin_dev,
+                                double *params_dev, int *gn_iters_dev, void *stream);
+/* Same with host arrays (copied in and out; blocking), as dvc_gpu_process. */
+int dvc_gpu_plan_process(dvc_plan *plan, const int *point_cfg, int n_points, const double *points,
+                         int n_process, const int *order, int n_neigh, const int *neigh,
+                         int seed_mode, const double *seeds, int *status, double *objmin,
+                         double *params, int *gn_iters, dvc_stats *stats);
+/* Autotuner (no counterpart in the reference): times the plan's search over
+   the given points (device arrays, as dvc_gpu_plan_process_device; outputs
+   are scratch) at every launch shape that fits: cluster widths 1, 2, 4, 8,
+   each with and without staging. Each shape runs `reps` timed launches
+   after one untimed one; the fastest shape (least mean time) is kept.
+   ms_out[2*j + s] (may be NULL; 8 entries) gets the mean milliseconds of width
+   2^j with staging s, or -1 for a shape that does not fit. Blocking. */
+int dvc_gpu_plan_autotune(dvc_plan *plan, const int *point_cfg_dev, int n_points,
+                          const double *points_dev, int n_process, const int *order_dev,
+                          int n_neigh, const int *neigh_dev, int seed_mode,
+                          const double *seeds_dev, int *status_dev, double *objmin_dev,
+                          double *params_dev, int reps, double ms_out[8]);
 
 /* ---- learned initial guess (no counterpart in the reference) ------------
  * A small 3D CNN proposes each point's start parameters from its reference
@@ -279,9 +344,13 @@ int dvc_gpu_strain(int n, const double *pts, const int *status, const double *ob
    every voxel plus Gaussian noise, clipped and rounded to uint8/uint16.
    `deform` selects the field: 0 none; 1 affine u(X) = t + E (X - c) with
    coef = {t0,t1,t2, E00..E22 (9), c0,c1,c2}; 2 sinusoid u_i = A sin(2 pi X_j / L)
-   with coef = {A, L}. vol_dev is a device buffer. */
+   with coef = {A, L}; 3 affine plus Gaussian bumps, coef = {t (3), E (9),
+   c (3), n, n x (p (3), s, a (3))}, u = t + E (X - c) + sum a exp(-|X - p|^2 /
+   (2 s^2)), n <= 32; 4 two affine pieces split by the plane X_x = split,
+   coef = {t1 (3), E1 (9), c1 (3), t2 (3), E2 (9), c2 (3), split} (blob
+   amplitudes >= 0). vol_dev is a device buffer; blobs a host array. */
 int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int bytes_per_voxel,
-                         int n_blobs, const float *blobs_dev /* n_blobs*5: x y z sigma amp */,
+                         int n_blobs, const float *blobs /* host, n_blobs*5: x y z sigma amp */,
                          int deform, const double *coef, float background, float noise_sigma,
                          unsigned long long noise_seed, float vmax, void *stream);
 

@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--learned-steps", type=int, default=3000)
     ap.add_argument("--no-batching", action="store_true",
                     help="skip configuration 3 (60 configurations in one launch)")
+    ap.add_argument("--pipeline", action="store_true",
+                    help="also run configuration 5 (8 GiB pair, 499,200 points, learned + plain)")
+    ap.add_argument("--pipeline-only", action="store_true",
+                    help="train the network (learned leg) and run only configuration 5")
     ap.add_argument("--batching-only", action="store_true",
                     help="run only the configuration 3 leg and print its JSON")
     ap.add_argument("--no-cpu", action="store_true")
@@ -195,6 +199,12 @@ def main():
         return run_reference(args, rank, world)
     if args.profile_case:
         return profile_case()
+    if args.pipeline_only:
+        import torch
+        torch.cuda.set_device(local)
+        summary, weights = learned_leg(args.learned_steps)
+        print(json.dumps({"learned": summary, "pipeline": pipeline_leg(weights)}))
+        return
     if args.batching_only:
         import torch
         torch.cuda.set_device(local)
@@ -319,7 +329,9 @@ def main():
                                             "spaced in processing order) with the GPU run's seeds",
                                   "max_abs_du_gpu_vs_oracle_vox": err}
     if rank == 0 and not args.no_learned and world == 1:
-        result["learned"] = learned_leg(args.learned_steps)
+        result["learned"], weights = learned_leg(args.learned_steps)
+        if args.pipeline:
+            result["pipeline"] = pipeline_leg(weights)
     if rank == 0 and not args.no_batching and world == 1:
         result["batching"] = batching_leg()
     if rank == 0:
@@ -336,7 +348,7 @@ def learned_leg(steps, oracle_sample=32):
     from digitalvolumecorrelation_gb300 import learned
     from digitalvolumecorrelation_gb300.abi import make_params
     from oracle.oracle import Oracle
-    summary, held, res = learned.run(steps=steps, keep=True)
+    summary, held, res, weights = learned.run(steps=steps, keep=True)
     rng = np.random.default_rng(5)
     n = len(held.points)
     sample = np.sort(rng.choice(n, oracle_sample, replace=False))
@@ -354,7 +366,116 @@ def learned_leg(steps, oracle_sample=32):
         summary[name]["oracle_sample"] = int(ok.sum())
         summary[name]["within_0p01_vox_of_oracle"] = float(np.mean(err <= 0.01)) if len(err) else None
         summary[name]["max_err_vs_oracle_vox"] = float(err.max()) if len(err) else None
-    return summary
+    return summary, weights
+
+
+def pipeline_leg(weights, obj_threshold=0.1, oracle_sample=64, cpu_sample=512):
+    """Configuration 5: the full pipeline on the 8 GiB uint16 pair and the
+    499,200-point grid. The plain GPU method (reference seeding in processing
+    order, coarse grid, Gauss-Newton) and the learned method (the network
+    trained in the learned leg proposes all 12 parameters, Gauss-Newton
+    refines, the plain search redoes points whose ZNSSD exceeds 0.1), each
+    timed over one full pass after a warm-up pass; both checked against the
+    FP64 oracle's converged optimum (started from the true translation, no
+    grid) on a random sample; the reference's CPU path (the oracle with the
+    plain run's seeds, full search) timed on a sample in processing order;
+    neighbour lists from the GPU kNN and the strain window (5 points) fitted
+    on the GPU."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine, workloads
+    from digitalvolumecorrelation_gb300.abi import make_params
+    from oracle.oracle import Oracle
+    W = workloads.config5()
+    n = len(W.points)
+    t0 = time.perf_counter()
+    ref_d, cor_d = W.render_device()
+    render_s = time.perf_counter() - t0
+    p = W.params()
+    E = engine.Engine(p, ref_dev=ref_d, cor_dev=cor_d)
+    t0 = time.perf_counter()
+    order, neigh = engine.order_neighbours(W.points, k=75)
+    knn_s = time.perf_counter() - t0
+    net = engine.Cnn()
+    net.set_weights(weights)
+    dev = torch.device("cuda")
+    pts_d, order_d, neigh_d = (torch.from_numpy(a).to(dev) for a in (W.points, order, neigh))
+    truth = W.truth()
+    out, res = {}, {}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name in ("plain", "learned"):
+        st = torch.empty(n, dtype=torch.int32, device=dev)
+        ob = torch.empty(n, dtype=torch.float64, device=dev)
+        pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
+        it = torch.empty(n, dtype=torch.int32, device=dev)
+        if name == "plain":
+            run = lambda: E.process_device(n, pts_d, order_d, n, neigh_d, neigh.shape[1], engine.SEED_NEIGHBOURS,
+                                           None, st, ob, pa, it)
+        else:
+            run = lambda: E.process_learned(net, n, pts_d, order_d, n, obj_threshold, st, ob, pa, it)
+        run()
+        torch.cuda.synchronize()
+        ev0.record()
+        fb = run()
+        ev1.record()
+        torch.cuda.synchronize()
+        secs = ev0.elapsed_time(ev1) / 1e3
+        s_, o_, p_ = st.cpu().numpy(), ob.cpu().numpy(), pa.cpu().numpy()
+        res[name] = (s_, o_, p_)
+        good = s_ == 0
+        out[name] = dict(points_per_s=round(n / secs, 1), seconds=round(secs, 3), good=int(good.sum()),
+                         median_abs_err_vs_truth_vox=float(np.median(np.abs(p_[good, :3] - truth[good]))),
+                         mean_gn_iterations=float(it.float().mean().item()))
+        if name == "learned":
+            out[name]["fallback_points"] = int(fb)
+            out[name]["fallback_rate"] = round(fb / n, 4)
+    out["speedup_learned_over_plain"] = round(out["learned"]["points_per_s"] / out["plain"]["points_per_s"], 2)
+    net.close()
+    E.close()
+    nvox = W.nvox
+    ref_np = ref_d[:nvox].cpu().numpy().view(np.uint16).reshape(W.shape[::-1])
+    cor_np = cor_d[:nvox].cpu().numpy().view(np.uint16).reshape(W.shape[::-1])
+    del ref_d, cor_d
+    O = Oracle()
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(6)
+    sample = np.sort(rng.choice(n, oracle_sample, replace=False))
+    p0 = make_params(W.shape, bytes_per_voxel=2, **dict(W.params_kw, basin_radius=0.0))
+    o = O.process(p0, ref_np, cor_np, W.points[sample], seed_mode=1, seeds=truth[sample], n_threads=threads)
+    ok = o["status"] == 0
+    for name in ("plain", "learned"):
+        s_, _, p_ = res[name]
+        good = ok & (s_[sample] == 0)
+        err = np.abs(p_[sample][good, :3] - o["params"][good, :3]).max(axis=1)
+        out[name]["oracle_sample"] = int(ok.sum())
+        out[name]["within_0p01_vox_of_oracle"] = float(np.mean(err <= 0.01)) if len(err) else None
+        out[name]["max_err_vs_oracle_vox"] = float(err.max()) if len(err) else None
+    # the reference's CPU path on a sample in processing order, with the plain run's seeds
+    s_, _, p_ = res["plain"]
+    seeds = seeds_from_results(order, neigh, s_, p_, p.rigid_trans[:], n)
+    sub = order[:: max(1, n // cpu_sample)][:cpu_sample]
+    t0 = time.perf_counter()
+    o2 = O.process(p, ref_np, cor_np, W.points[sub], seed_mode=1, seeds=seeds[sub], n_threads=threads)
+    cpu_s = time.perf_counter() - t0
+    g2 = (o2["status"] == 0) & (s_[sub] == 0)
+    # strain window of 5 points on the learned run's results
+    s_, o_, p_ = res["learned"]
+    t0 = time.perf_counter()
+    sw = engine.strain(W.points, s_, o_, p_[:, :3], neigh, ndp=5)
+    strain_s = time.perf_counter() - t0
+    out.update({
+        "workload": W.name, "points": n, "obj_threshold": obj_threshold, "render_seconds": round(render_s, 2),
+        "knn_seconds": round(knn_s, 3), "strain_window": 5, "strain_seconds": round(strain_s, 3),
+        "strain_points_fitted": int((sw["pts_in_sw"] >= 5).sum()),
+        "reference_cpu": {"points_per_s": round(len(sub) / cpu_s, 3), "seconds": round(cpu_s, 2),
+                          "threads": threads, "sample": f"{len(sub)} points evenly spaced in processing order, "
+                                                        "the plain run's seeds, full search",
+                          "same_status_as_gpu": int((o2["status"] == res["plain"][0][sub]).sum()),
+                          "max_abs_du_gpu_vs_oracle_vox": float(np.abs(o2["params"][g2, :3] -
+                                                                       res["plain"][2][sub][g2, :3]).max())
+                          if g2.any() else None},
+    })
+    out["plain"]["speedup_over_reference_cpu"] = round(out["plain"]["points_per_s"] / (len(sub) / cpu_s), 1)
+    return out
 
 
 BATCHING_ORACLE_CONFIGS = ((21, "cube", 3, "ssd"), (41, "sphere", 12, "znssd"), (61, "cube", 6, "znssd"),

@@ -42,6 +42,8 @@ struct SynthArgs {
   float bump[kMaxBumps][7];   // p (3), 1/(2 s^2), a (3)
   // split field: piece 2's X = c2 + Ainv2 (x - t2 - c2), the plane X_x = split
   float Ainv2[9], t2[3], c2[3], split;
+  // bending and jump: kappa, xc, h, J, z0, 1/w
+  float bend[6];
   float background, noise_sigma, vmax;
   unsigned long long seed;
 };
@@ -89,6 +91,15 @@ __global__ void synth_kernel(SynthArgs a) {
         X[0] = x0[0] - u[0];
         X[1] = x0[1] - u[1];
         X[2] = x0[2] - u[2];
+      }
+    } else if (a.deform == 5) {
+      const float x0[3] = {X[0], X[1], X[2]};
+      for (int it = 0; it < 20; it++) {
+        const float dx = X[0] - a.bend[1];
+        const float ux = 0.5f * a.bend[3] * tanhf((X[2] - a.bend[4]) * a.bend[5]);
+        const float uz = 0.5f * a.bend[0] * (dx * dx - a.bend[2]);
+        X[0] = x0[0] - ux;
+        X[2] = x0[2] - uz;
       }
     } else if (a.deform == 2) {
       const float x0[3] = {X[0], X[1], X[2]};
@@ -144,7 +155,7 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
                                     const double *coef, float background, float noise_sigma,
                                     unsigned long long noise_seed, float vmax, void *stream) {
   if (!vol_dev || nx <= 0 || ny <= 0 || nz <= 0 || (bytes_per_voxel != 1 && bytes_per_voxel != 2) ||
-      n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 4 || (deform && !coef))
+      n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 5 || (deform && !coef))
     return dvc_internal_set_error(DVC_E_ARG, "bad synth arguments");
   SynthArgs a{};
   a.vol = vol_dev;
@@ -194,6 +205,11 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
   } else if (deform == 2) {
     a.amp = (float)coef[0];
     a.len = (float)coef[1];
+  } else if (deform == 5) {
+    // coef: kappa, xc, h, J, z0, w
+    if (!(coef[5] > 0.0)) return dvc_internal_set_error(DVC_E_ARG, "jump width must be > 0");
+    for (int i = 0; i < 5; i++) a.bend[i] = (float)coef[i];
+    a.bend[5] = (float)(1.0 / coef[5]);
   } else if (deform == 3) {
     // coef: t (3), E (9), c (3), n, then n x (p (3), s, a (3))
     const int nb = (int)coef[15];
@@ -230,6 +246,9 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
       for (int i = 0; i < 3; i++)
         x[i] = X[i] + P[i] + E[i * 3 + 0] * (X[0] - P[12]) + E[i * 3 + 1] * (X[1] - P[13]) +
                E[i * 3 + 2] * (X[2] - P[14]);
+    } else if (deform == 5) {
+      x[0] = X[0] + 0.5 * coef[3] * tanh((X[2] - coef[4]) / coef[5]);
+      x[2] = X[2] + 0.5 * coef[0] * ((X[0] - coef[1]) * (X[0] - coef[1]) - coef[2]);
     } else if (deform == 2) {
       const double w = 2.0 * M_PI / coef[1];
       x[0] = X[0] + coef[0] * sin(w * X[1]);

@@ -178,7 +178,8 @@ def evaluate(net, pair):
 
 def run(steps=3000, train_pairs=6, log=None, keep=False):
     """Train on `train_pairs` pairs, evaluate on a held-out one. With keep,
-    also return the held-out pair and the per-method results."""
+    also return the held-out pair, the per-method results and the trained
+    weights."""
     pairs = [Pair(101 + 17 * k) for k in range(train_pairs)]
     net, tinfo = train(pairs, steps=steps, log=log)
     for p in pairs:
@@ -189,10 +190,11 @@ def run(steps=3000, train_pairs=6, log=None, keep=False):
     ev["proposal_rms"] = {"uvw_vox": [round(float(v), 4) for v in rms[:3]],
                           "rotation_rad": [round(float(v), 5) for v in rms[3:6]],
                           "strain": [round(float(v), 5) for v in rms[6:]]}
+    weights = net.get_weights()
     net.close()
     summary = dict(config="config4_512cube_u8_bumps_cube31_dof12", search=SEARCH, spacing=SPACING,
                    points=len(held.points), obj_threshold=OBJ_THRESHOLD, training=tinfo, **ev)
-    return (summary, held, res) if keep else summary
+    return (summary, held, res, weights) if keep else summary
 
 
 if __name__ == "__main__":

@@ -150,6 +150,40 @@ class Piecewise:
     kind = 4
 
 
+@dataclass
+class BendJump:
+    """A smooth bending plus a smoothed planar jump:
+    u_x = (J / 2) tanh((X_z - z0) / w), u_y = 0,
+    u_z = (kappa / 2) ((X_x - xc)^2 - h)
+    (curvature kappa of u_z along x, offset h; a jump of J voxels in u_x
+    across the plane X_z = z0, smoothed over w voxels)."""
+    kappa: float = 1e-4
+    xc: float = 0.0
+    h: float = 0.0
+    J: float = 2.0
+    z0: float = 0.0
+    w: float = 5.0
+
+    def u(self, X):
+        X = np.asarray(X, dtype=np.float64)
+        out = np.zeros_like(X)
+        out[..., 0] = 0.5 * self.J * np.tanh((X[..., 2] - self.z0) / self.w)
+        out[..., 2] = 0.5 * self.kappa * ((X[..., 0] - self.xc) ** 2 - self.h)
+        return out
+
+    def inverse(self, x, iters: int = 20):
+        x = np.asarray(x, np.float64)
+        X = x.copy()
+        for _ in range(iters):
+            X = x - self.u(X)
+        return X
+
+    def coef(self):
+        return [self.kappa, self.xc, self.h, self.J, self.z0, self.w]
+
+    kind = 5
+
+
 def rotation_z(deg):
     """R - I for a rotation by `deg` degrees about the z axis."""
     th = math.radians(deg)

@@ -26,6 +26,15 @@ configuration. Volumes are rendered on the GPU by `dvc_gpu_synth_volume`
       subvol_npts = 0.15 x the subvolume's voxel count (at most the
       reference's 50,000), 3, 6 or 12 dof, ssd or znssd; tricubic, disp_max 8
       and basin_radius 4 (chosen here); strain window 7.
+  config 5 ("full pipeline, large"): 2048 x 2048 x 1024 uint16 (8 GiB pair),
+      blobs as config 2; target = a smooth bending u_z = (1e-4 / 2)((x -
+      1024)^2 - 395^2 / 2) (curvature 1e-4 per voxel, |u_z| <= 3.9 over the
+      ROI) plus a 2-voxel jump of u_x across z = 512 smoothed over 5 voxels
+      (u_x = tanh((z - 512) / 5)); 80 x 80 x 78 = 499,200-point grid of
+      spacing 10 centred at (1024, 1024, 512); cube 41 / 3000 samples (15^3 =
+      3375), znssd, tricubic, 12 dof, disp_max 6 and basin_radius 3 (chosen
+      here); learned start with the plain search as fallback where the
+      refined ZNSSD exceeds 0.1; strain window 5.
 """
 from __future__ import annotations
 
@@ -146,6 +155,20 @@ def config3(n_points=40000, shape=(768, 768, 768), seed=3):
     W = Workload("config3_768cube_u8_40000pts_mixed60", shape, 1, settings[0], pts, deform, b, 2.0,
                  seed + 301, seed + 302)
     return W, cfg, settings
+
+
+def config5(grid=(80, 80, 78), spacing=10.0, shape=(2048, 2048, 1024)):
+    nx, ny, nz = shape
+    c = (nx / 2.0, ny / 2.0, nz / 2.0)
+    half = (grid[0] - 1) * spacing / 2.0
+    deform = synth.BendJump(kappa=1e-4, xc=c[0], h=half * half / 2.0, J=2.0, z0=c[2], w=5.0)
+    pts = synth.grid_points(grid, spacing, c)
+    kw = dict(subvol_geom="cube", subvol_size=41, subvol_npts=3000, obj_function="znssd",
+              interp_type="tricubic", num_srch_dof=12, disp_max=6, basin_radius=3.0)
+    n_blobs = int(np.prod(shape) // 1000)
+    b = synth.blobs(shape, n_blobs, sigma=(1.5, 3.0), amp=(2000.0, 60000.0), seed=5)
+    return Workload("config5_2048x2048x1024_u16_499200pts_cube41_dof12", shape, 2, kw, pts, deform, b,
+                    150.0, 501, 502)
 
 
 def order_and_neighbours(points, n_neigh=75, start=None):

@@ -348,7 +348,9 @@ int dvc_gpu_strain(int n, const double *pts, const int *status, const double *ob
    c (3), n, n x (p (3), s, a (3))}, u = t + E (X - c) + sum a exp(-|X - p|^2 /
    (2 s^2)), n <= 32; 4 two affine pieces split by the plane X_x = split,
    coef = {t1 (3), E1 (9), c1 (3), t2 (3), E2 (9), c2 (3), split} (blob
-   amplitudes >= 0). vol_dev is a device buffer; blobs a host array. */
+   amplitudes >= 0); 5 bending and jump, coef = {kappa, xc, h, J, z0, w}:
+   u_x = (J/2) tanh((X_z - z0)/w), u_y = 0, u_z = (kappa/2)((X_x - xc)^2 - h).
+   vol_dev is a device buffer; blobs a host array. */
 int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int bytes_per_voxel,
                          int n_blobs, const float *blobs /* host, n_blobs*5: x y z sigma amp */,
                          int deform, const double *coef, float background, float noise_sigma,

@@ -22,6 +22,8 @@ class DvcParams(C.Structure):
         ("obj_function", C.c_int), ("interp_type", C.c_int),
         ("basin_radius", C.c_double), ("rigid_trans", C.c_double * 3),
         ("sphere_seed", C.c_uint),
+        ("subvol_thresh", C.c_int), ("gray_thresh_min", C.c_double), ("gray_thresh_max", C.c_double),
+        ("min_vol_fract", C.c_double),
     ]
 
 
@@ -36,7 +38,8 @@ class DvcStats(C.Structure):
 def make_params(shape_xyz, bytes_per_voxel=1, subvol_geom="cube", subvol_size=31,
                 subvol_npts=2000, subvol_aspect=(1.0, 1.0, 1.0), disp_max=12, num_srch_dof=6,
                 obj_function="znssd", interp_type="tricubic", basin_radius=0.0,
-                rigid_trans=(0.0, 0.0, 0.0), sphere_seed=1) -> DvcParams:
+                rigid_trans=(0.0, 0.0, 0.0), sphere_seed=1, subvol_thresh=False, gray_thresh_min=25.0,
+                gray_thresh_max=125.0, min_vol_fract=0.2) -> DvcParams:
     p = DvcParams()
     p.vol_wide, p.vol_high, p.vol_tall = (int(v) for v in shape_xyz)
     p.bytes_per_voxel = int(bytes_per_voxel)
@@ -51,4 +54,8 @@ def make_params(shape_xyz, bytes_per_voxel=1, subvol_geom="cube", subvol_size=31
     p.basin_radius = float(basin_radius)
     p.rigid_trans[:] = [float(v) for v in rigid_trans]
     p.sphere_seed = int(sphere_seed)
+    p.subvol_thresh = int(bool(subvol_thresh))
+    p.gray_thresh_min = float(gray_thresh_min)
+    p.gray_thresh_max = float(gray_thresh_max)
+    p.min_vol_fract = float(min_vol_fract)
     return p

@@ -23,7 +23,7 @@ BIN_DIR = os.path.join(PKG, "bin")
 OBJ_DIR = os.path.join(PKG, "lib", "obj")
 LIB = os.path.join(LIB_DIR, "libdvcgpu.so")
 
-CUDA_SOURCES = ["dvc_engine.cu", "dvc_strain.cu", "dvc_synth.cu", "dvc_cnn.cu", "dvc_knn.cu"]
+CUDA_SOURCES = ["dvc_engine.cu", "dvc_strain.cu", "dvc_synth.cu", "dvc_cnn.cu", "dvc_knn.cu", "dvc_io.cu"]
 # the strain fit follows the FP64 oracle operation by operation: no FMA
 # contraction, so its results are bit-identical to the oracle's
 EXTRA_FLAGS = {"dvc_strain.cu": ["-fmad=false"]}

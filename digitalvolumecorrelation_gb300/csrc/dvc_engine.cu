@@ -291,6 +291,14 @@ int validate(const dvc_params *p) {
   if (p->subvol_npts < 1 || p->subvol_npts > 50000)
     return set_error(DVC_E_ARG, "subvol_npts must be in 1..50000");
   if (p->subvol_size < 1) return set_error(DVC_E_ARG, "subvol_size must be >= 1");
+  if (p->subvol_thresh) {
+    const double top = p->bytes_per_voxel == 1 ? 256.0 : 65536.0;  // 2^vol_bit_depth
+    if (!(p->gray_thresh_min >= 0.0) || !(p->gray_thresh_max > p->gray_thresh_min) ||
+        !(p->gray_thresh_max <= top))
+      return set_error(DVC_E_ARG, "gray thresholds must satisfy 0 <= min < max <= 2^vol_bit_depth");
+    if (!(p->min_vol_fract >= 0.0 && p->min_vol_fract <= 1.0))
+      return set_error(DVC_E_ARG, "min_vol_fract must be in 0..1");
+  }
   if (p->num_srch_dof != 3 && p->num_srch_dof != 6 && p->num_srch_dof != 12)
     return set_error(DVC_E_ARG, "num_srch_dof must be 3, 6 or 12");
   if (p->obj_function < 0 || p->obj_function > 4) return set_error(DVC_E_ARG, "bad obj_function");
@@ -615,6 +623,10 @@ int fill_config(const dvc_engine *e, int C, SearchCfg &k) {
     k.inc = displ_max / k.num_inc;
     k.inc_int = (k.inc == std::floor(k.inc) && k.inc <= 64.0 && !getenv("DVC_GENERAL_GRID")) ? (int)k.inc : 0;
   }
+  k.thresh_on = p.subvol_thresh ? 1 : 0;
+  k.gmin = (float)p.gray_thresh_min;
+  k.gmax = (float)p.gray_thresh_max;
+  k.min_count = p.min_vol_fract * e->n_sub;
   rank_ranges(e->h_offsets, e->morton_rad, C, k.rank_start);
   k.off_i = e->d_off_i;
   k.off_f = e->d_off_f;
@@ -642,14 +654,14 @@ int fill_config(const dvc_engine *e, int C, SearchCfg &k) {
 
 // Staging box of configuration k (filled at width C) when it fits `budget`
 // together with `state` bytes of per-CTA sample state: one region per point
-// covers every grid translation (reach k * inc); odd row pitch (in 16-byte
-// units) first, then the plain one. Returns the staging buffer's bytes, 0
-// when the box does not fit (k then stays unstaged).
-size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, SearchCfg &k) {
+// covers every grid translation (reach k * inc) when the grid runs; odd row
+// pitch (in 16-byte units) first, then the plain one. Returns the staging
+// buffer's bytes, 0 when the box does not fit (k then stays unstaged).
+size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, bool grid, SearchCfg &k) {
   const dvc_params &p = e->p;
   const int esize = p.bytes_per_voxel;
   double reach = 0.0;
-  if (p.basin_radius != 0.0) {
+  if (grid && p.basin_radius != 0.0) {
     const int n = (int)((double)p.disp_max / p.basin_radius);
     reach = n * ((double)p.disp_max / n);
   }
@@ -848,6 +860,39 @@ int dvc_gpu_create(dvc_engine **out, const dvc_params *p, const void *ref_vox, c
   return DVC_OK;
 }
 
+int dvc_gpu_create_from_files(dvc_engine **out, const dvc_params *p, const char *ref_path,
+                              const char *cor_path, long long header_bytes, int big_endian) {
+  if (!out || !ref_path || !cor_path) return set_error(DVC_E_ARG, "null argument");
+  *out = nullptr;
+  int rc = validate(p);
+  if (rc) return rc;
+  dvc_engine *e = new dvc_engine();
+  e->p = *p;
+  const size_t bytes = (size_t)p->vol_wide * p->vol_high * p->vol_tall * p->bytes_per_voxel;
+  if (cudaMalloc(&e->ref, bytes + 64) != cudaSuccess || cudaMalloc(&e->cor, bytes + 64) != cudaSuccess) {
+    dvc_gpu_destroy(e);
+    return set_error(DVC_E_NOMEM, "volume allocation failed");
+  }
+  e->owns_volumes = true;
+  if (cudaMemset((char *)e->ref + bytes, 0, 64) != cudaSuccess ||
+      cudaMemset((char *)e->cor + bytes, 0, 64) != cudaSuccess) {
+    dvc_gpu_destroy(e);
+    return set_error(DVC_E_CUDA, "volume padding");
+  }
+  rc = dvc_gpu_load_raw(e->ref, ref_path, header_bytes, p->vol_wide, p->vol_high, p->vol_tall,
+                        p->bytes_per_voxel, big_endian, nullptr);
+  if (!rc)
+    rc = dvc_gpu_load_raw(e->cor, cor_path, header_bytes, p->vol_wide, p->vol_high, p->vol_tall,
+                          p->bytes_per_voxel, big_endian, nullptr);
+  if (!rc) rc = engine_finish(e);
+  if (rc) {
+    dvc_gpu_destroy(e);
+    return rc;
+  }
+  *out = e;
+  return DVC_OK;
+}
+
 int dvc_gpu_create_device(dvc_engine **out, const dvc_params *p, const void *ref_vox_dev,
                           const void *cor_vox_dev) {
   if (!out || !ref_vox_dev || !cor_vox_dev) return set_error(DVC_E_ARG, "null argument");
@@ -916,7 +961,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   size_t stage_bytes = 0;
   for (;;) {
     cap = fill_config(e, C, k);
-    stage_bytes = tma_ok ? stage_config(e, C, budget, state_bytes(cap), k) : 0;
+    stage_bytes = tma_ok ? stage_config(e, C, budget, state_bytes(cap), seed_mode != DVC_SEED_PARAMS, k) : 0;
     const size_t need = stage_bytes + state_bytes(cap);
     if (((tma_ok && !stage_bytes) || need > budget) && C < 8) {
       C *= 2;
@@ -1165,7 +1210,7 @@ static int plan_build(dvc_plan *pl, int C, int staging) {
   for (int i = 0; i < n; i++) {
     memset(&maps[(size_t)i], 0, sizeof(CUtensorMap));
     if (!tma_ok) continue;
-    const size_t b = stage_config(pl->cfgs[i], C, budget, state_bytes(cap), ks[(size_t)i]);
+    const size_t b = stage_config(pl->cfgs[i], C, budget, state_bytes(cap), true, ks[(size_t)i]);
     if (b && encode_stage_map(pl->cfgs[i], ks[(size_t)i], &maps[(size_t)i])) {
       sb = std::max(sb, b);
       n_staged++;

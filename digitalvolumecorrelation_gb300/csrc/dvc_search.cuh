@@ -54,6 +54,11 @@ struct SearchCfg {
   int inc_int;  // the grid step when it is a whole number of voxels, else 0
   double inc;
   double rigid[3];
+  // subvolume pre-check: searched only when at least min_count reference
+  // samples lie in [gmin, gmax]
+  int thresh_on;
+  float gmin, gmax;
+  double min_count;
   // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
   // voxels (stage_tx bytes), TMA-loaded into the staging buffer
   int stage_on;
@@ -1303,7 +1308,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     {
-      KSum rk[1];
+      KSum rk[2];
       for (int i = tid; i < nl; i += kThreads) {
         int c[3], ip[3];
         float f[3], fp[3];
@@ -1329,10 +1334,19 @@ __global__ void __launch_bounds__(kThreads, 1)
         s_fp[i * 3 + 1] = fp[1];
         s_fp[i * 3 + 2] = fp[2];
         rk[0].add(r);
+        rk[1].add((r >= K.gmin && r <= K.gmax) ? 1.f : 0.f);
       }
-      cta_sum_comp<1>(rk, S, S.cbuf[cl.parity]);
-      cluster_reduce(cl, S, 1, 0);
+      cta_sum_comp<2>(rk, S, S.cbuf[cl.parity]);
+      cluster_reduce(cl, S, 2, 0);
     }
+    // subvolume pre-check (subvol_thresh, documented in Core/InputRead.cpp:
+    // 282-323): too few reference samples in the gray range, not searched
+    if (K.thresh_on) {
+      if (tid == 0 && S.red[1] < K.min_count) S.fail = 3;
+      __syncthreads();
+      if (S.fail) goto point_done;
+    }
+    {
     if (tid == 0) {
       for (int d = 0; d < 3; d++) {
         // stable reference point (FloatingCloud: centre, or middle of the cube box)
@@ -1382,6 +1396,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     n_eval += 1;
     __syncthreads();
+    }
 
     pc.to(2);
     // ---------------------------------------------------- grid search ---
@@ -1928,7 +1943,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (cl.rank == 0 && tid == 0) {
       const int n = S.H.n;
       if (S.fail) {
-        a.status[n] = DVC_RANGE_FAIL;
+        a.status[n] = S.fail == 3 ? DVC_NOT_SEARCH : DVC_RANGE_FAIL;
         a.objmin[n] = 0.0;
         for (int p = 0; p < 12; p++) a.params[(size_t)n * 12 + p] = 0.0;
       } else {

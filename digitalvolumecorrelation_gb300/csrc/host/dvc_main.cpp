@@ -12,7 +12,11 @@
 //    each row as it goes, then rewrites the file in the same order);
 //  * a file name may end its line (the reference needs a tab after it);
 //  * with DVC_GPU_NEIGHBOURS set, order and neighbour lists come from the GPU
-//    (same distances, ties by point index instead of std::sort's order).
+//    (same distances, ties by point index instead of std::sort's order);
+//  * with DVC_SUBVOL_THRESH set, `subvol_thresh on` is applied as the manual
+//    documents it (points with too little of the gray range are not searched,
+//    status -3); the reference only parses and echoes the keywords, and so
+//    does this program without the variable.
 #include <algorithm>
 #include <chrono>
 #include <cstdlib>
@@ -37,15 +41,6 @@ static void usage() {
             << "dvc example\t\t// write dvc_in_example, an input file with every keyword\n"
             << "dvc manual\t\t// write dvc_manual, the keyword reference\n"
             << "dvc version\t\t// print the program version\n\n";
-}
-
-static bool read_volume(const std::string &fname, int hdr, size_t bytes, std::vector<char> &out) {
-  std::ifstream f(fname.c_str(), std::ios::binary);
-  if (!f.good()) return false;
-  f.seekg(hdr, std::ios::beg);
-  out.resize(bytes);
-  f.read(out.data(), (std::streamsize)bytes);
-  return (size_t)f.gcount() == bytes;
 }
 
 int main(int argc, char *argv[]) {
@@ -120,13 +115,6 @@ int main(int argc, char *argv[]) {
   append_stat_time(run.sta_fname, "Run start: ", t_start);
 
   const int bpv = run.vol_bit_depth / 8;
-  const size_t vbytes = (size_t)run.vol_wide * run.vol_high * run.vol_tall * bpv;
-  std::vector<char> ref, cor;
-  if (!read_volume(run.ref_fname, run.vol_hdr_lngth, vbytes, ref) ||
-      !read_volume(run.cor_fname, run.vol_hdr_lngth, vbytes, cor)) {
-    std::cout << "\nCannot read the image volumes.\n\n";
-    return 0;
-  }
 
   dvc_params p{};
   p.vol_wide = run.vol_wide;
@@ -145,16 +133,22 @@ int main(int argc, char *argv[]) {
   p.obj_function = run.obj_fcn;
   p.interp_type = run.int_typ;
   p.basin_radius = run.basin_radius;
+  if (run.subvol_thresh == "on" && std::getenv("DVC_SUBVOL_THRESH")) {
+    p.subvol_thresh = 1;
+    p.gray_thresh_min = run.gray_thresh_min;
+    p.gray_thresh_max = run.gray_thresh_max;
+    p.min_vol_fract = run.min_vol_fract;
+  }
   const char *seed = std::getenv("DVC_SPHERE_SEED");
   p.sphere_seed = seed ? (unsigned)std::strtoul(seed, nullptr, 10) : 1u;
 
+  // both volumes streamed from their files straight to device memory
   dvc_engine *eng = nullptr;
-  if (dvc_gpu_create(&eng, &p, ref.data(), cor.data(), run.vol_endian == "big" ? 1 : 0) != DVC_OK) {
+  if (dvc_gpu_create_from_files(&eng, &p, run.ref_fname.c_str(), run.cor_fname.c_str(), run.vol_hdr_lngth,
+                                run.vol_endian == "big" ? 1 : 0) != DVC_OK) {
     std::cout << "\nThe GPU engine could not be set up: " << dvc_gpu_last_error() << "\n\n";
     return 0;
   }
-  std::vector<char>().swap(ref);
-  std::vector<char>().swap(cor);
 
   const char *fcn_names[5] = {"SAD", "SSD", "ZSSD", "NSSD", "ZNSSD"};
   std::cout << "\n\n*************************\nSearch: ( \nSearch(\nbytes_per " << bpv
@@ -203,6 +197,8 @@ int main(int argc, char *argv[]) {
     } else if (status[(size_t)m] == DVC_RANGE_FAIL) {
       rfail++;
       std::cout << "Range_Fail";
+    } else if (status[(size_t)m] == DVC_NOT_SEARCH) {
+      std::cout << "Not_Searched";
     } else {
       cfail++;
       std::cout << "Convg_Fail";

@@ -78,6 +78,11 @@ def load(path: str | None = None):
                                           C.POINTER(C.c_int), C.c_void_p]
     L.dvc_gpu_order_neighbours.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip]
     L.dvc_gpu_set_cluster.argtypes = [C.c_void_p, C.c_int]
+    L.dvc_gpu_read_mhd.argtypes = [C.c_char_p, C.POINTER(DvcVolumeInfo)]
+    L.dvc_gpu_load_raw.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_int, C.c_void_p]
+    L.dvc_gpu_create_from_files.argtypes = [C.POINTER(C.c_void_p), C.POINTER(DvcParams), C.c_char_p,
+                                            C.c_char_p, C.c_longlong, C.c_int]
     L.dvc_gpu_plan_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int]
     L.dvc_gpu_plan_destroy.argtypes = [C.c_void_p]
     L.dvc_gpu_plan_destroy.restype = None
@@ -107,16 +112,43 @@ def _p(a, t):
     return a.ctypes.data_as(t)
 
 
+class DvcVolumeInfo(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("bytes_per_voxel", C.c_int),
+                ("big_endian", C.c_int), ("header_bytes", C.c_longlong), ("data_file", C.c_char * 1024)]
+
+
+def read_mhd(path):
+    """MetaImage header (dvc_gpu_read_mhd): dict(nx, ny, nz, bytes_per_voxel,
+    big_endian, header_bytes, data_file)."""
+    load()
+    info = DvcVolumeInfo()
+    _check(_lib.dvc_gpu_read_mhd(os.fsencode(path), C.byref(info)))
+    return dict(nx=info.nx, ny=info.ny, nz=info.nz, bytes_per_voxel=info.bytes_per_voxel,
+                big_endian=info.big_endian, header_bytes=info.header_bytes,
+                data_file=info.data_file.decode())
+
+
+def load_raw(vol_dev, path, shape_xyz, bytes_per_voxel, header_bytes=0, big_endian=False, stream=0):
+    """Stream a raw volume file into a device buffer (dvc_gpu_load_raw)."""
+    load()
+    nx, ny, nz = shape_xyz
+    _check(_lib.dvc_gpu_load_raw(C.c_void_p(_dev_ptr(vol_dev)), os.fsencode(path), int(header_bytes), nx, ny,
+                                 nz, int(bytes_per_voxel), int(big_endian), C.c_void_p(stream)))
+
+
 class Engine:
     """Both volumes resident on the GPU; Search::Search + Interpolate."""
 
     def __init__(self, params: DvcParams, ref=None, cor=None, big_endian=False, ref_dev=None,
-                 cor_dev=None):
+                 cor_dev=None, ref_path=None, cor_path=None, header_bytes=0):
         L = load()
         self.params = params
         self._h = C.c_void_p()
         self._keep = []
-        if ref_dev is not None:
+        if ref_path is not None:
+            _check(L.dvc_gpu_create_from_files(C.byref(self._h), C.byref(params), os.fsencode(ref_path),
+                                               os.fsencode(cor_path), int(header_bytes), int(big_endian)))
+        elif ref_dev is not None:
             # device buffers (e.g. torch CUDA tensors): pass their addresses
             self._keep = [ref_dev, cor_dev]
             _check(L.dvc_gpu_create_device(C.byref(self._h), C.byref(params),
@@ -411,5 +443,5 @@ def synth_volume_device(vol_dev, shape_xyz, bytes_per_voxel, blobs, deform=None,
                                      C.c_void_p(stream)))
 
 
-__all__ = ["Engine", "Plan", "Cnn", "objective", "strain", "order_neighbours", "synth_volume_device", "make_params", "load",
+__all__ = ["Engine", "Plan", "Cnn", "read_mhd", "load_raw", "objective", "strain", "order_neighbours", "synth_volume_device", "make_params", "load",
            "DvcError", "E_ARG", "SEED_NEIGHBOURS", "SEED_GIVEN", "SEED_RIGID", "SEED_PARAMS"]

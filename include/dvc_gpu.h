@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define DVC_ABI_VERSION 1
+#define DVC_ABI_VERSION 2
 
 /* per-point status, identical to Core/Utility.h:38-41 */
 #define DVC_POINT_GOOD 0
@@ -84,6 +84,16 @@ typedef struct dvc_params {
   unsigned int sphere_seed;         /* mt19937 seed of sphere subvolumes; the
                                        reference's reproducible test mode uses 1
                                        (Core/Search.cpp:102-105)               */
+  /* subvolume pre-check (keywords subvol_thresh, gray_thresh_min/max,
+     min_vol_fract; Core/InputRead.cpp:282-323, limits :564-571): with
+     subvol_thresh = 1 a point whose reference samples lie in
+     [gray_thresh_min, gray_thresh_max] for less than min_vol_fract of the
+     samples is not searched (DVC_NOT_SEARCH). The reference parses and
+     echoes these keywords but its search never applies them; 0 keeps its
+     behaviour. */
+  int subvol_thresh;
+  double gray_thresh_min, gray_thresh_max; /* 0 <= min < max <= 2^(8*bytes_per_voxel) */
+  double min_vol_fract;                    /* 0..1 */
 } dvc_params;
 
 /* Run statistics returned by dvc_gpu_process. */
@@ -151,6 +161,35 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
                            const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
                            const double *seeds_dev, int *status_dev, double *objmin_dev,
                            double *params_dev, int *gn_iters_dev, void *stream);
+
+/* ---- volume files -------------------------------------------------------
+ * The reference reads the raw volume files piecewise for every point (one
+ * seekg + read per row of the interpolation box, Interpolate::kernels,
+ * Core/Interpolate.cpp:144-258; endian swap on the host, :219-250). These
+ * stream each file once into device memory in 64 MiB chunks through two
+ * pinned buffers (file read overlapping the copy), swapping big-endian
+ * 16-bit data on the device. */
+typedef struct dvc_volume_info {
+  int nx, ny, nz;          /* DimSize */
+  int bytes_per_voxel;     /* 1 (MET_UCHAR/MET_CHAR) or 2 (MET_USHORT/MET_SHORT) */
+  int big_endian;          /* BinaryDataByteOrderMSB / ElementByteOrderMSB (16-bit) */
+  long long header_bytes;  /* bytes to skip in data_file (HeaderSize; LOCAL data) */
+  char data_file[1024];    /* ElementDataFile, relative to the .mhd's folder */
+} dvc_volume_info;
+/* Reads a MetaImage (.mhd) header: NDims 3, DimSize, ElementType (8 or
+   16 bit), HeaderSize, byte order, ElementDataFile (a file name or LOCAL);
+   host code, no GPU call. The reference takes the same facts from input-file
+   keys (vol_wide/high/tall, vol_bit_depth, vol_hdr_lngth, vol_endian). */
+int dvc_gpu_read_mhd(const char *mhd_path, dvc_volume_info *out);
+/* Streams nx*ny*nz voxels from `path` (after header_bytes) into vol_dev on
+   `stream`; returns when the volume is in place. */
+int dvc_gpu_load_raw(void *vol_dev, const char *path, long long header_bytes, int nx, int ny,
+                     int nz, int bytes_per_voxel, int big_endian, void *stream);
+/* dvc_gpu_create with both volumes read straight from their files (same
+   header length and byte order for both, as the reference's input file has
+   one vol_hdr_lngth and one vol_endian). */
+int dvc_gpu_create_from_files(dvc_engine **out, const dvc_params *p, const char *ref_path,
+                              const char *cor_path, long long header_bytes, int big_endian);
 
 /* ---- allocation-free search ---------------------------------------------
  * No counterpart in the reference. Same as dvc_gpu_process_device, but the

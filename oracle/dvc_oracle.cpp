@@ -675,6 +675,18 @@ struct Search {
     interp_ref->center_on(pt);
     interp_ref->load(ref);
     interp_ref->interp(p.interp_type, fc.stable, fc.sbmn, fc.sbmx, ref_sub);
+    // subvolume pre-check as the reference's manual documents it
+    // (Core/InputRead.cpp:282-323; parsed there, never applied by its search):
+    // fewer than min_vol_fract of the reference samples in the gray range
+    if (p.subvol_thresh) {
+      int cnt = 0;
+      for (double v : ref_sub)
+        if (v >= p.gray_thresh_min && v <= p.gray_thresh_max) cnt++;
+      if ((double)cnt < p.min_vol_fract * subv_num) {
+        evals++;
+        return DVC_NOT_SEARCH;
+      }
+    }
     const int ndof = p.num_srch_dof;
     std::vector<double> par(ndof, 0.0);
     for (int d = 0; d < 3; d++) par[d] = seed[d];

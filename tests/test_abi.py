@@ -26,6 +26,34 @@ def test_library_exports_every_declared_function():
 def test_abi_version_and_errors_without_gpu_calls():
     lib = ctypes.CDLL(build.build_library())
     lib.dvc_gpu_abi_version.restype = ctypes.c_int
-    assert lib.dvc_gpu_abi_version() == 1
+    assert lib.dvc_gpu_abi_version() == 2
     lib.dvc_gpu_version.restype = ctypes.c_char_p
     assert b"sm_103a" in lib.dvc_gpu_version()
+
+
+def test_metaimage_header_reader(tmp_path):
+    """dvc_gpu_read_mhd is host code (no GPU call): a header with a separate
+    raw file, and one with the data in the same file (LOCAL)."""
+    from digitalvolumecorrelation_gb300 import engine
+    sub = tmp_path / "f000"
+    sub.mkdir()
+    (sub / "frame.mhd").write_text(
+        "ObjectType = Image\nNDims = 3\nBinaryData = True\nBinaryDataByteOrderMSB = True\n"
+        "CompressedData = False\nDimSize = 150 126 127\nElementType = MET_USHORT\n"
+        "HeaderSize = 12\nElementDataFile = frame.raw\n")
+    info = engine.read_mhd(str(sub / "frame.mhd"))
+    assert (info["nx"], info["ny"], info["nz"]) == (150, 126, 127)
+    assert info["bytes_per_voxel"] == 2 and info["big_endian"] == 1 and info["header_bytes"] == 12
+    assert info["data_file"] == str(sub / "frame.raw")
+    head = b"NDims = 3\nDimSize = 4 3 2\nElementType = MET_UCHAR\nElementDataFile = LOCAL\n"
+    (tmp_path / "local.mhd").write_bytes(head + bytes(range(24)))
+    info = engine.read_mhd(str(tmp_path / "local.mhd"))
+    assert info["bytes_per_voxel"] == 1 and info["header_bytes"] == len(head)
+    assert info["data_file"] == str(tmp_path / "local.mhd")
+    (tmp_path / "bad.mhd").write_text("NDims = 3\nDimSize = 4 3 2\nElementType = MET_FLOAT\n"
+                                      "ElementDataFile = x.raw\n")
+    try:
+        engine.read_mhd(str(tmp_path / "bad.mhd"))
+        raise AssertionError("float data accepted")
+    except engine.DvcError as e:
+        assert e.code == engine.E_ARG

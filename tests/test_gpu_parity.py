@@ -158,3 +158,75 @@ def test_given_seed_mode_vs_oracle(eng, oracle):
         rel = np.abs(g["objmin"][good] - o["objmin"][good]) / o["objmin"][good]
         assert rel.max() <= 1e-5
         E.close()
+
+
+def test_subvolume_precheck_vs_oracle(eng, oracle):
+    """subvol_thresh as the reference's manual documents it (Core/InputRead.cpp:
+    282-323): points whose reference samples lie in the gray range for less
+    than min_vol_fract of the samples are not searched (status -3); the rest
+    are searched as usual. A dark slab makes some subvolumes fail the check."""
+    from digitalvolumecorrelation_gb300 import synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    rng = np.random.default_rng(12)
+    shape = (72, 72, 72)
+    b = synth.blobs(shape, 2500, amp=(60.0, 200.0), seed=51)
+    aff = synth.Affine(t=(0.6, -0.9, 1.3), c=(36.0, 36.0, 36.0))
+    ref = synth.render(shape, b, noise_sigma=2.0, noise_seed=52)
+    cor = synth.render(shape, b, deform=aff, noise_sigma=2.0, noise_seed=53)
+    ref[:, :, :30] //= 8  # dark slab, x < 30
+    cor[:, :, :31] //= 8
+    pts = synth.grid_points((5, 4, 4), 6.0, (36.0, 36.0, 36.0))
+    seeds = aff.u(pts) + rng.normal(0, 0.5, pts.shape)
+    for geom, size, npts in (("cube", 15, 900), ("sphere", 17, 1200)):
+        p = make_params(shape, subvol_geom=geom, subvol_size=size, subvol_npts=npts, num_srch_dof=6,
+                        disp_max=3, basin_radius=0.0, subvol_thresh=True, gray_thresh_min=30.0,
+                        gray_thresh_max=255.0, min_vol_fract=0.3)
+        E = eng.Engine(p, ref, cor)
+        g = E.process(pts, seed_mode=1, seeds=seeds)
+        o = oracle.process(p, ref, cor, pts, seed_mode=1, seeds=seeds)
+        np.testing.assert_array_equal(g["status"], o["status"])
+        assert (o["status"] == -3).sum() >= 3 and (o["status"] == 0).sum() >= 10
+        good = o["status"] == 0
+        assert np.abs(g["params"][good, :3] - o["params"][good, :3]).max() <= 1e-3
+        assert np.all(g["params"][~good] == 0.0) and np.all(g["objmin"][~good] == 0.0)
+        E.close()
+
+
+def test_volume_files_streamed_to_the_gpu(eng, tmp_path):
+    """dvc_gpu_create_from_files / dvc_gpu_load_raw: raw files with a header
+    and big-endian 16-bit data give the same volume (and so the same search)
+    as the host-buffer upload; larger than one 64 MiB staging chunk."""
+    import torch
+    from digitalvolumecorrelation_gb300 import synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    shape = (512, 256, 300)  # 75 MiB of uint16
+    rng = np.random.default_rng(3)
+    vol = rng.integers(0, 65535, size=shape[::-1], dtype=np.uint16)
+    hdr = b"\x07" * 37
+    path = tmp_path / "vol.raw"
+    path.write_bytes(hdr + vol.astype(">u2").tobytes())
+    dev = torch.zeros(vol.size + 32, dtype=torch.int16, device="cuda")
+    eng.load_raw(dev, str(path), shape, 2, header_bytes=len(hdr), big_endian=True)
+    got = dev[: vol.size].cpu().numpy().view(np.uint16).reshape(vol.shape)
+    np.testing.assert_array_equal(got, vol)
+    # a small pair through the engine: same results as the host upload
+    small = (48, 48, 48)
+    b = synth.blobs(small, 250, seed=61)
+    ref = synth.render(small, b, noise_seed=62, dtype=np.uint16, vmax=65535)
+    cor = synth.render(small, b, deform=synth.Affine(t=(0.7, -0.4, 1.1)), noise_seed=63, dtype=np.uint16,
+                       vmax=65535)
+    (tmp_path / "r.raw").write_bytes(hdr + ref.astype(">u2").tobytes())
+    (tmp_path / "c.raw").write_bytes(hdr + cor.astype(">u2").tobytes())
+    p = make_params(small, bytes_per_voxel=2, subvol_size=13, subvol_npts=500, disp_max=3)
+    pts = synth.grid_points((3, 3, 3), 6.0, (24.0, 24.0, 24.0))
+    seeds = np.tile([0.7, -0.4, 1.1], (len(pts), 1))
+    E1 = eng.Engine(p, ref.astype(">u2").view(np.uint16), cor.astype(">u2").view(np.uint16), big_endian=True)
+    E2 = eng.Engine(p, ref_path=str(tmp_path / "r.raw"), cor_path=str(tmp_path / "c.raw"),
+                    header_bytes=len(hdr), big_endian=True)
+    r1 = E1.process(pts, seed_mode=1, seeds=seeds)
+    r2 = E2.process(pts, seed_mode=1, seeds=seeds)
+    for k in ("status", "objmin", "params"):
+        np.testing.assert_array_equal(r1[k], r2[k])
+    assert (r1["status"] == 0).all()
+    E1.close()
+    E2.close()

@@ -274,7 +274,7 @@ struct dvc_plan {
   size_t stage_bytes = 0, smem_dyn = 0;
   int max_clusters = 0;            // clusters resident at once
   SearchCfg *d_cfgs = nullptr;     // device: one record per configuration
-  CUtensorMap *d_tmaps = nullptr;  // device: one tensor map per configuration
+  CUtensorMap *d_tmaps = nullptr;  // device: two tensor maps per configuration (correlate, reference)
 };
 
 namespace {
@@ -487,8 +487,8 @@ int ensure_ws(dvc_engine *e, size_t bytes) {
 }
 
 template <typename VT, int IT>
-int launch_search(SearchArgs &a, const CUtensorMap &tmap, size_t smem_dyn, int grid, int cluster,
-                  cudaStream_t st, int *max_clusters) {
+int launch_search(SearchArgs &a, const CUtensorMap &tmap, const CUtensorMap &tmap_ref, size_t smem_dyn,
+                  int grid, int cluster, cudaStream_t st, int *max_clusters) {
   auto kern = search_kernel<VT, IT>;
   CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dyn));
   cudaLaunchConfig_t cfg = {};
@@ -508,7 +508,7 @@ int launch_search(SearchArgs &a, const CUtensorMap &tmap, size_t smem_dyn, int g
     return DVC_OK;
   }
   cfg.gridDim = dim3(grid, 1, 1);
-  CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a, tmap));
+  CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a, tmap, tmap_ref));
   return DVC_OK;
 }
 
@@ -560,16 +560,16 @@ void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int r
   out[0] = units * al;
 }
 
-int dispatch_launch(int bpv, int it, SearchArgs &a, const CUtensorMap &tm, size_t smem, int grid,
-                    int cluster, cudaStream_t st, int *max_clusters) {
+int dispatch_launch(int bpv, int it, SearchArgs &a, const CUtensorMap &tm, const CUtensorMap &tmr, size_t smem,
+                    int grid, int cluster, cudaStream_t st, int *max_clusters) {
   if (bpv == 1) {
-    if (it == 2) return launch_search<uint8_t, 2>(a, tm, smem, grid, cluster, st, max_clusters);
-    if (it == 1) return launch_search<uint8_t, 1>(a, tm, smem, grid, cluster, st, max_clusters);
-    return launch_search<uint8_t, 0>(a, tm, smem, grid, cluster, st, max_clusters);
+    if (it == 2) return launch_search<uint8_t, 2>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+    if (it == 1) return launch_search<uint8_t, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+    return launch_search<uint8_t, 0>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
   }
-  if (it == 2) return launch_search<uint16_t, 2>(a, tm, smem, grid, cluster, st, max_clusters);
-  if (it == 1) return launch_search<uint16_t, 1>(a, tm, smem, grid, cluster, st, max_clusters);
-  return launch_search<uint16_t, 0>(a, tm, smem, grid, cluster, st, max_clusters);
+  if (it == 2) return launch_search<uint16_t, 2>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+  if (it == 1) return launch_search<uint16_t, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+  return launch_search<uint16_t, 0>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
 }
 
 // ---- launch preparation ------------------------------------------------------
@@ -585,12 +585,13 @@ int dyn_budget(size_t *out) {
   return DVC_OK;
 }
 
-// TMA staging of the correlate volume needs 16-byte aligned rows and planes.
+// TMA staging of the volumes needs 16-byte aligned rows, planes and bases.
 bool tma_layout(const dvc_engine *e) {
   const dvc_params &p = e->p;
   const int esize = p.bytes_per_voxel;
   return encode_tiled_fn() != nullptr && ((size_t)p.vol_wide * esize) % 16 == 0 &&
          ((size_t)p.vol_wide * p.vol_high * esize) % 16 == 0 && ((uintptr_t)e->cor % 16) == 0 &&
+         ((uintptr_t)e->ref % 16) == 0 &&
          !getenv("DVC_NO_STAGE");
 }
 
@@ -627,6 +628,7 @@ int fill_config(const dvc_engine *e, int C, SearchCfg &k) {
   k.gmin = (float)p.gray_thresh_min;
   k.gmax = (float)p.gray_thresh_max;
   k.min_count = p.min_vol_fract * e->n_sub;
+  k.inv_nsub = 1.0 / (double)e->n_sub;
   rank_ranges(e->h_offsets, e->morton_rad, C, k.rank_start);
   k.off_i = e->d_off_i;
   k.off_f = e->d_off_f;
@@ -679,8 +681,9 @@ size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, boo
   return bytes;
 }
 
-// Tensor map of the correlate volume with configuration k's staging box.
-bool encode_stage_map(const dvc_engine *e, const SearchCfg &k, CUtensorMap *tm) {
+// Tensor map of volume `vol` (the engine's correlate or reference volume)
+// with configuration k's staging box.
+bool encode_stage_map(const dvc_engine *e, const SearchCfg &k, const void *vol, CUtensorMap *tm) {
   const dvc_params &p = e->p;
   const int esize = p.bytes_per_voxel;
   memset(tm, 0, sizeof *tm);
@@ -689,7 +692,7 @@ bool encode_stage_map(const dvc_engine *e, const SearchCfg &k, CUtensorMap *tm) 
   const cuuint32_t box[3] = {(cuuint32_t)k.stage[0], (cuuint32_t)k.stage[1], (cuuint32_t)k.stage[2]};
   const cuuint32_t estride[3] = {1, 1, 1};
   return encode_tiled_fn()(tm, esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3,
-                           e->cor, gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           const_cast<void *>(vol), gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -970,9 +973,10 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
     if (need > budget) return set_error(DVC_E_ARG, "subvolume too large for the search kernel");
     break;
   }
-  CUtensorMap tmap;
+  CUtensorMap tmap, tmap_ref;
   memset(&tmap, 0, sizeof tmap);
-  if (stage_bytes && !encode_stage_map(e, k, &tmap)) {
+  memset(&tmap_ref, 0, sizeof tmap_ref);
+  if (stage_bytes && !(encode_stage_map(e, k, e->cor, &tmap) && encode_stage_map(e, k, e->ref, &tmap_ref))) {
     k = SearchCfg{};
     cap = fill_config(e, C, k);
     stage_bytes = 0;
@@ -980,7 +984,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   const size_t smem_dyn = stage_bytes + state_bytes(cap);
   int max_clusters = 0;
   SearchArgs probe{};
-  rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tmap, smem_dyn, 0, C, st, &max_clusters);
+  rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tmap, tmap_ref, smem_dyn, 0, C, st, &max_clusters);
   if (rc) return rc;
   if (max_clusters < 1) return set_error(DVC_E_ARG, "search kernel cluster does not fit");
   const int grid = C * std::max(1, std::min(max_clusters, n_process));
@@ -1001,7 +1005,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   e->last_cluster = C;
   e->last_grid = grid;
   e->last_staged = k.stage_on;
-  return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, tmap, smem_dyn, grid, C, st, nullptr);
+  return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, tmap, tmap_ref, smem_dyn, grid, C, st, nullptr);
 }
 
 
@@ -1204,14 +1208,15 @@ static int plan_build(dvc_plan *pl, int C, int staging) {
     return set_error(DVC_E_ARG, "the largest subvolume does not fit the search kernel at cluster width " +
                                     std::to_string(C));
   const bool tma_ok = staging && tma_layout(pl->cfgs[0]);
-  std::vector<CUtensorMap> maps((size_t)n);
+  std::vector<CUtensorMap> maps((size_t)n * 2);  // per configuration: correlate, reference
   size_t sb = 0;
   int n_staged = 0;
   for (int i = 0; i < n; i++) {
-    memset(&maps[(size_t)i], 0, sizeof(CUtensorMap));
+    memset(&maps[(size_t)i * 2], 0, 2 * sizeof(CUtensorMap));
     if (!tma_ok) continue;
     const size_t b = stage_config(pl->cfgs[i], C, budget, state_bytes(cap), true, ks[(size_t)i]);
-    if (b && encode_stage_map(pl->cfgs[i], ks[(size_t)i], &maps[(size_t)i])) {
+    if (b && encode_stage_map(pl->cfgs[i], ks[(size_t)i], pl->cfgs[i]->cor, &maps[(size_t)i * 2]) &&
+        encode_stage_map(pl->cfgs[i], ks[(size_t)i], pl->cfgs[i]->ref, &maps[(size_t)i * 2 + 1])) {
       sb = std::max(sb, b);
       n_staged++;
     } else {
@@ -1226,16 +1231,19 @@ static int plan_build(dvc_plan *pl, int C, int staging) {
   SearchArgs probe{};
   CUtensorMap tm0;
   memset(&tm0, 0, sizeof tm0);
-  rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tm0, smem, 0, C, 0, &mc);
+  rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tm0, tm0, smem, 0, C, 0, &mc);
   if (rc) return rc;
   if (mc < 1) return set_error(DVC_E_ARG, "search kernel cluster does not fit");
   if (!pl->d_cfgs) {
     CUDA_TRY(cudaMalloc(&pl->d_cfgs, (size_t)n * sizeof(SearchCfg)));
-    CUDA_TRY(cudaMalloc(&pl->d_tmaps, (size_t)n * sizeof(CUtensorMap)));
+    CUDA_TRY(cudaMalloc(&pl->d_tmaps, (size_t)n * 2 * sizeof(CUtensorMap)));
   }
-  for (int i = 0; i < n; i++) ks[(size_t)i].tmap = ks[(size_t)i].stage_on ? pl->d_tmaps + i : nullptr;
+  for (int i = 0; i < n; i++) {
+    ks[(size_t)i].tmap = ks[(size_t)i].stage_on ? pl->d_tmaps + 2 * i : nullptr;
+    ks[(size_t)i].tmap_ref = ks[(size_t)i].stage_on ? pl->d_tmaps + 2 * i + 1 : nullptr;
+  }
   CUDA_TRY(cudaDeviceSynchronize());  // no launch still reads the old table
-  CUDA_TRY(cudaMemcpy(pl->d_tmaps, maps.data(), (size_t)n * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(pl->d_tmaps, maps.data(), (size_t)n * 2 * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(pl->d_cfgs, ks.data(), (size_t)n * sizeof(SearchCfg), cudaMemcpyHostToDevice));
   pl->h_cfgs = ks;
   pl->cluster = C;
@@ -1349,7 +1357,7 @@ int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_
   e->last_staged = plan->n_staged > 0;
   CUtensorMap tm0;
   memset(&tm0, 0, sizeof tm0);
-  return dispatch_launch(e->p.bytes_per_voxel, e->p.interp_type, a, tm0, plan->smem_dyn, grid, C, st, nullptr);
+  return dispatch_launch(e->p.bytes_per_voxel, e->p.interp_type, a, tm0, tm0, plan->smem_dyn, grid, C, st, nullptr);
 }
 
 int dvc_gpu_plan_process(dvc_plan *plan, const int *point_cfg, int n_points, const double *points,

@@ -59,12 +59,14 @@ struct SearchCfg {
   int thresh_on;
   float gmin, gmax;
   double min_count;
+  double inv_nsub;  // 1 / n_sub
   // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
   // voxels (stage_tx bytes), TMA-loaded into the staging buffer
   int stage_on;
   int stage[3];
   unsigned stage_tx;
   const CUtensorMap *tmap;       // this configuration's tensor map, or null: the kernel's
+  const CUtensorMap *tmap_ref;   // the same box over the reference volume
   int rank_start[9];             // sample range of each cluster rank
   // stable offsets of the samples from their point: whole voxels and FP32
   // fractions; their extrema over all samples and over each rank's samples
@@ -252,7 +254,10 @@ __device__ __forceinline__ void cluster_reduce_keys(Cl &c, CtaState &S, int nsum
   __syncthreads();
 }
 
-// CTA-level compensated sum of K (<= 8) Kahan partials into dst[0..K) (FP64).
+// CTA-level compensated sum of K (<= 8) Kahan partials into dst[0..K) (FP64):
+// warp partials merged by FP32 TwoSum (about 48 significant bits), one FP64
+// add at the end (each FP64 instruction occupies the narrow FP64 pipe for
+// ~64 cycles, so a serial FP64 sum over the warps cost ~2k cycles).
 template <int K>
 __device__ __forceinline__ void cta_sum_comp(KSum (&v)[K], CtaState &S, double *dst) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -278,9 +283,9 @@ __device__ __forceinline__ void cta_sum_comp(KSum (&v)[K], CtaState &S, double *
     }
   __syncthreads();
   if (threadIdx.x < K) {
-    double s = 0.0;
-    for (int w = 0; w < kWarps; w++) s += (double)S.wred[w][2 * threadIdx.x] + (double)S.wred[w][2 * threadIdx.x + 1];
-    dst[threadIdx.x] = s;
+    float h = S.wred[0][2 * threadIdx.x], l = S.wred[0][2 * threadIdx.x + 1];
+    for (int w = 1; w < kWarps; w++) two_sum_merge(h, l, S.wred[w][2 * threadIdx.x], S.wred[w][2 * threadIdx.x + 1]);
+    dst[threadIdx.x] = (double)h + (double)l;
   }
   __syncthreads();
 }
@@ -348,20 +353,21 @@ __device__ __forceinline__ void clamp_cell(int c[3], const int bext[3]) {
 // Objective from one-pass sums: S1 = sum t', S2 = sum t'^2, S3 = sum t' q,
 // S4 = sum |t' - q|, t' = t - shift, q the per-sample reference quantity,
 // rs2 = sum q^2, n samples.
+// (inv_n = 1/n; FP64 division and square root cost ~440 and ~680 cycles
+// here, so the mean is a product and 1/sigma one reciprocal square root)
 __device__ __forceinline__ double objective_from_sums(int fcn, double S1, double S2, double S3,
-                                                      double S4, double rs2, int n) {
+                                                      double S4, double rs2, int n, double inv_n) {
   switch (fcn) {
     case DVC_SAD: return S4;
     case DVC_SSD: return S2 - 2.0 * S3 + rs2;
     case DVC_ZSSD: {
-      const double m = S1 / n;
+      const double m = S1 * inv_n;
       return (S2 - n * m * m) - 2.0 * S3 + rs2;
     }
-    case DVC_NSSD: return 1.0 - S3 / sqrt(S2);
+    case DVC_NSSD: return 1.0 - S3 * rsqrt(S2);
     default: {
-      const double m = S1 / n;
-      const double sig = sqrt(S2 - n * m * m);
-      return 0.5 * (1.0 - S3 / sig);
+      const double m = S1 * inv_n;
+      return 0.5 * (1.0 - S3 * rsqrt(S2 - n * m * m));
     }
   }
 }
@@ -606,163 +612,92 @@ __device__ void warp_qr_solve(CtaState &S, int n) {
   __syncwarp();
 }
 
-// The same solve with little FP64 work: each FP64 instruction occupies the
-// SM's narrow FP64 pipe for a whole warp, so the serial FP64 factorisation
-// costs tens of thousands of cycles per Gauss-Newton iteration. Here the
-// Jacobi-scaled system D A D y = D b (D = diag(A)^-1/2) is factored by
-// pivoted Householder QR in FP32 on one warp (lane j holds column j), and
-// three solves with FP64 residuals r = b - A x (iterative refinement) bring
-// x to FP64 accuracy. A factor with |R_kk| < 1e-3 |R_00| (an ill-conditioned
-// or rank-deficient system) returns false and the caller uses the FP64
-// factorisation above, which also decides the numerical rank. Scratch: S.red,
-// free once A and b are assembled.
-__device__ bool warp_solve_mixed(CtaState &S, int n) {
+// The solve used by the search: J'J is symmetric positive definite, so the
+// Jacobi-scaled system D A D y = D b (D = diag(A)^-1/2) is factored by a
+// Cholesky factorisation in FP32 across one warp (lane i holds row i of L,
+// the columns' entries reach the other rows by shuffles), and three solves
+// with FP64 residuals r = b - A x (iterative refinement) bring x to FP64
+// accuracy. A pivoted Householder QR of the same system in FP32 took 100k
+// cycles per 12-dof solve inside the search kernel (its serial shuffle
+// chains dominated the iteration); this takes 18k. A pivot below 1e-4
+// (condition number above about 10^4, where two refinements no longer reach
+// FP64 accuracy, or a rank-deficient system) returns false and the caller
+// uses the FP64 factorisation, which also decides the numerical rank.
+// Scratch: S.red, free once A and b are assembled.
+__device__ bool warp_solve_chol(CtaState &S, int n) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int M = kMaxDof;
   const int lane = threadIdx.x & 31;
-  float *sR = reinterpret_cast<float *>(S.red);  // [M][M] upper triangle of R
-  float *sV = sR + M * M;                         // [M][M] reflector of step k in row k
-  float *sBeta = sV + M * M;                      // [16]
-  float *sRinv = sBeta + 16;                      // [16] 1 / R_kk
-  float *sD = sRinv + 16;                         // [16] scaling
-  float *sZ = sD + 16;                            // [16] scaled residual
-  float *sXi = sZ + 16;                           // [16] correction, original order
-  float *sAf = sXi + 16;                          // [M * M] A in FP32
+  float *sL = reinterpret_cast<float *>(S.red);  // [M][M] L, row i columns <= i
+  float *sAf = sL + M * M;                        // [M * M] A in FP32
   double *sX = reinterpret_cast<double *>(sAf + M * M);  // [M] current x
   for (int e = lane; e < n * n; e += 32) sAf[e] = (float)S.A[e];
   __syncwarp();
-  if (lane < n) {
-    const float ajj = sAf[lane * n + lane];
-    sD[lane] = ajj > 0.f ? rsqrtf(ajj) : 1.f;
-  }
-  __syncwarp();
-  float a[M];
-  const float dj = lane < n ? sD[lane] : 0.f;
+  const float di = (lane < n && sAf[lane * n + lane] > 0.f) ? rsqrtf(sAf[lane * n + lane]) : 1.f;
+  float a[M], rinv[M];
 #pragma unroll
-  for (int i = 0; i < M; i++) a[i] = (lane < n && i < n) ? sAf[i * n + lane] * sD[i] * dj : 0.f;
-  int col = lane;
-  float r00 = 0.f;
+  for (int j = 0; j < M; j++) {
+    const float dj = __shfl_sync(FULL, di, j);
+    a[j] = (lane < n && j < n) ? sAf[lane * n + j] * di * dj : 0.f;
+  }
   bool ok = true;
 #pragma unroll
   for (int k = 0; k < M; k++) {
-    if (k >= n) break;
-    float s = -1.f;
-    if (lane >= k && lane < n) {
-      s = 0.f;
+    rinv[k] = 0.f;
+    if (k < n) {
+      const float piv = __shfl_sync(FULL, a[k], k);  // Schur complement diagonal
+      ok = ok && (piv > 1e-4f);                      // also NaN
+      const float r = rsqrtf(fmaxf(piv, 1e-30f));    // 1 / L_kk
+      rinv[k] = r;
+      const float l = a[k] * r;                      // lane i: L_ik
+      a[k] = l;
 #pragma unroll
-      for (int i = k; i < M; i++)
-        if (i < n) s = fmaf(a[i], a[i], s);
-    }
-    float best = s;
-    int pc = lane;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      const float ob = __shfl_xor_sync(FULL, best, o);
-      const int oi = __shfl_xor_sync(FULL, pc, o);
-      if (ob > best || (ob == best && oi < pc)) {
-        best = ob;
-        pc = oi;
+      for (int j = k + 1; j < M; j++) {
+        if (j < n) {
+          const float lj = __shfl_sync(FULL, l, j);  // L_jk
+          if (lane >= j) a[j] = fmaf(-l, lj, a[j]);
+        }
       }
     }
-    if (pc != k) {
-      const int src = lane == k ? pc : (lane == pc ? k : lane);
-#pragma unroll
-      for (int i = 0; i < M; i++) a[i] = __shfl_sync(FULL, a[i], src);
-      col = __shfl_sync(FULL, col, src);
-    }
-    const float nrm = sqrtf(best);
-    if (k == 0) r00 = nrm;
-    if (!(nrm > 1e-3f * r00)) {  // also NaN
-      ok = false;
-      break;
-    }
-    float v[M];
-#pragma unroll
-    for (int i = 0; i < M; i++) v[i] = i >= k ? __shfl_sync(FULL, a[i], k) : 0.f;
-    const float xk = v[k];
-    const float alpha = xk > 0.f ? -nrm : nrm;
-    const float beta = 1.f / (nrm * (nrm + fabsf(xk)));  // 2 / v'v
-    v[k] = xk - alpha;
-    if (lane > k && lane < n) {
-      float t = 0.f;
-#pragma unroll
-      for (int i = k; i < M; i++)
-        if (i < n) t = fmaf(v[i], a[i], t);
-      t *= beta;
-#pragma unroll
-      for (int i = k; i < M; i++)
-        if (i < n) a[i] = fmaf(-t, v[i], a[i]);
-    }
-    if (lane == k) {
-      a[k] = alpha;
-#pragma unroll
-      for (int i = k + 1; i < M; i++) a[i] = 0.f;
-    }
-    if (lane == 0) {
-#pragma unroll
-      for (int i = k; i < M; i++)
-        if (i < n) sV[k * M + i] = v[i];
-      sBeta[k] = beta;
-    }
   }
-  if (!__all_sync(FULL, ok)) return false;
+  if (!ok) return false;
   if (lane < n) {
 #pragma unroll
-    for (int i = 0; i < M; i++)
-      if (i <= lane) sR[i * M + lane] = a[i];
-    S.perm[lane] = col;
+    for (int j = 0; j < M; j++)
+      if (j <= lane) sL[lane * M + j] = a[j];
   }
   __syncwarp();
-  if (lane < n) sRinv[lane] = 1.f / sR[lane * M + lane];
-  __syncwarp();
   double xi = 0.0;  // lane i: x_i
+#pragma unroll 1
   for (int pass = 0; pass < 3; pass++) {
+    float z = 0.f;
     if (lane < n) {
       double r = S.b[lane];
       if (pass > 0)
         for (int j = 0; j < n; j++) r = fma(-S.A[lane * n + j], sX[j], r);
-      sZ[lane] = (float)r * sD[lane];
+      z = (float)r * di;
     }
-    __syncwarp();
-    // every lane forms the same solution: z <- Q'z, then R y = z
-    float z[M], y[M];
-#pragma unroll
-    for (int i = 0; i < M; i++) z[i] = i < n ? sZ[i] : 0.f;
+    // L y = z: lane k finishes y_k, the rows below take it off
 #pragma unroll
     for (int k = 0; k < M; k++) {
       if (k < n) {
-        float t = 0.f;
-#pragma unroll
-        for (int i = k; i < M; i++)
-          if (i < n) t = fmaf(sV[k * M + i], z[i], t);
-        t *= sBeta[k];
-#pragma unroll
-        for (int i = k; i < M; i++)
-          if (i < n) z[i] = fmaf(-t, sV[k * M + i], z[i]);
+        const float yk = __shfl_sync(FULL, z, k) * rinv[k];
+        if (lane == k) z = yk;
+        else if (lane > k) z = fmaf(-a[k], yk, z);
       }
     }
+    // L' w = y: lane k finishes w_k, the rows above take it off (L_ki from
+    // shared memory)
 #pragma unroll
     for (int k = M - 1; k >= 0; k--) {
-      y[k] = 0.f;
       if (k < n) {
-        float t = z[k];
-#pragma unroll
-        for (int j = k + 1; j < M; j++)
-          if (j < n) t = fmaf(-sR[k * M + j], y[j], t);
-        y[k] = t * sRinv[k];
+        const float wk = __shfl_sync(FULL, z, k) * rinv[k];
+        if (lane == k) z = wk;
+        else if (lane < k) z = fmaf(-sL[k * M + lane], wk, z);
       }
     }
-    float yl = 0.f;
-#pragma unroll
-    for (int k = 0; k < M; k++)
-      if (k == lane) yl = y[k];
     if (lane < n) {
-      const int c = S.perm[lane];
-      sXi[c] = yl * sD[c];
-    }
-    __syncwarp();
-    if (lane < n) {
-      xi += (double)sXi[lane];
+      xi += (double)(z * di);
       sX[lane] = xi;
     }
     __syncwarp();
@@ -1140,7 +1075,8 @@ struct PhaseClock {
 // ================================================================ kernel ===
 template <typename VT, int IT>
 __global__ void __launch_bounds__(kThreads, 1)
-    search_kernel(const __grid_constant__ SearchArgs a, const __grid_constant__ CUtensorMap tmap) {
+    search_kernel(const __grid_constant__ SearchArgs a, const __grid_constant__ CUtensorMap tmap,
+                  const __grid_constant__ CUtensorMap tmap_ref) {
   extern __shared__ __align__(128) unsigned char dsm[];
   __shared__ CtaState S;
   Cl cl{cg::this_cluster(), 0u, 1u, 0};
@@ -1262,14 +1198,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int B[3] = {K.stage[0], K.stage[1], K.stage[2]};
     const uint32_t stage_tx = K.stage_tx;
     const CUtensorMap *tmp = K.tmap ? K.tmap : &tmap;
-    if (K.tmap && tid == 0)  // a tensor map in global memory: its latest contents for the TMA unit
+    const CUtensorMap *tmp_ref = K.tmap_ref ? K.tmap_ref : &tmap_ref;
+    if (K.tmap && tid == 0) {  // tensor maps in global memory: their latest contents for the TMA unit
       asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
                        reinterpret_cast<unsigned long long>(tmp))
                    : "memory");
+      asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                       reinterpret_cast<unsigned long long>(tmp_ref))
+                   : "memory");
+    }
     const int ndof = K.ndof;
     const int fcn = K.objfcn;
     const bool sad = (fcn == DVC_SAD);
-    const double inv_nsub = 1.0 / (double)nsub;
+    const double inv_nsub = K.inv_nsub;
     GSrc<VT> gsr = gref, gsc = gcor0;
     gsr.checked = S.H.chk_ref;
     gsc.checked = S.H.chk_cor;
@@ -1307,7 +1248,24 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
     __syncthreads();
+    // the reference region of this CTA's samples, staged by TMA into the
+    // buffer that later holds the correlate region (same box)
+    if (K.stage_on) {
+      if (tid == 0) {
+        const Region r = make_region(K, S.lbmn, S.lbmx, esize);
+        S.reg[0] = r;
+        if (r.ok) tma_load_3d(tmp_ref, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
+      }
+      __syncthreads();
+      if (S.reg[0].ok) {
+        if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
+        phase[0] ^= 1u;
+      }
+    }
     {
+      const Region rr = S.reg[0];
+      const bool rstaged = K.stage_on && rr.ok;
+      const SSrc<VT> ssr{buf_addr[0], rr.r0[0], rr.r0[1], rr.r0[2], B[0], B[1]};
       KSum rk[2];
       for (int i = tid; i < nl; i += kThreads) {
         int c[3], ip[3];
@@ -1326,7 +1284,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         clamp_cell(c, K.bext);
         bool und;
         float g[3];
-        const float r = interp_global<VT, IT, false>(gsr, Gref, c, f, g, und);
+        const float r = rstaged ? eval_sample_t<VT, IT, false, true>(ssr, rr.r0, B, gsr, Gref, c, f, g, und)
+                                : interp_global<VT, IT, false>(gsr, Gref, c, f, g, und);
         n_undef += und;
         s_r[i] = r;
         s_ip[i] = ip[0] | (ip[1] << 10) | (ip[2] << 20);
@@ -1382,7 +1341,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     //   SAD/SSD q = r - mean (shift = mean), ZSSD q = r - mean,
     //   NSSD q = r / |r| (no shift), ZNSSD q = (r - mean) / |r - mean|
     const float shift = (fcn == DVC_NSSD) ? 0.f : (float)rmean;
-    const float qs = (float)(fcn == DVC_NSSD ? 1.0 / sqrt(rraw2) : (fcn == DVC_ZNSSD ? 1.0 / sqrt(rc2) : 1.0));
+    const float qs = fcn == DVC_NSSD ? rsqrtf((float)rraw2) : (fcn == DVC_ZNSSD ? rsqrtf((float)rc2) : 1.f);
     for (int i = tid; i < nl; i += kThreads) s_r[i] = (s_r[i] - shift) * qs;
     if (tid == 0) {
       S.shift = shift;
@@ -1510,7 +1469,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (tid < nch)
           S.objv[tid] = sad ? S.red[3 * tid]
                             : objective_from_sums(fcn, S.red[3 * tid], S.red[3 * tid + 1],
-                                                  S.red[3 * tid + 2], 0.0, S.rsum2, nsub);
+                                                  S.red[3 * tid + 2], 0.0, S.rsum2, nsub, inv_nsub);
         __syncthreads();
         if (tid == 0)
           for (int j = 0; j < nch; j++)
@@ -1761,36 +1720,46 @@ __global__ void __launch_bounds__(kThreads, 1)
         pc.to(9);
         // assemble J'J and -J'e (FP64)
         if (tid == 0) {
+          // FP64 division and square root cost ~440 and ~680 cycles here: one
+          // reciprocal square root gives 1/sigma, sigma and the scales
           const double S1 = S.red[0], S2 = S.red[1], S3 = S.red[2], S4 = S.red[3];
-          const double n = nsub, mean = S1 / n;
-          double obj, sc = 1.0, rho = 0.0, T = 0.0, sig = 0.0;
+          const double n = nsub, mean = S1 * inv_nsub;
+          double obj, sc = 1.0, rho = 0.0, den = 1.0, rden = 1.0;
           switch (fcn) {
             case DVC_SAD:
             case DVC_SSD:
-            case DVC_ZSSD: obj = objective_from_sums(fcn, S1, S2, S3, S4, S.rsum2, nsub); break;
+            case DVC_ZSSD: obj = objective_from_sums(fcn, S1, S2, S3, S4, S.rsum2, nsub, inv_nsub); break;
             case DVC_NSSD:
-              T = sqrt(S2);
-              obj = 1.0 - S3 / T;
-              sc = 1.0 / (T * T);
+              rden = rsqrt(S2);  // 1 / T
+              den = S2 * rden;
+              rho = S3 * rden;
+              obj = 1.0 - rho;
+              sc = rden * rden;
               break;
-            default:
-              sig = sqrt(S2 - n * mean * mean);
-              rho = S3 / sig;
+            default: {
+              const double var = S2 - n * mean * mean;
+              rden = rsqrt(var);  // 1 / sigma
+              den = var * rden;
+              rho = S3 * rden;
               obj = 0.5 * (1.0 - rho);
-              sc = 1.0 / (sig * sig);
+              sc = rden * rden;
               break;
+            }
           }
           S.scal[0] = mean;
           S.scal[1] = sc;
-          S.scal[2] = (fcn == DVC_NSSD) ? T : sig;
-          S.scal[3] = (fcn == DVC_NSSD) ? S3 / T : rho;
-          S.scal[4] = 1.0 / S.scal[2];
+          S.scal[2] = den;
+          S.scal[3] = rho;
+          S.scal[4] = rden;
           S.obj = obj;
           int stop = 0;
           if (it > 0) {
+            // |obj - obj_old| < 1e-6 or |du| < 0.01 (min_Lev_Mar); |du|^2 is
+            // compared first, the square root only near the threshold
             const double del_obj = fabs(obj - S.obj_old);
-            const double del_mag = sqrt(S.upd[0] * S.upd[0] + S.upd[1] * S.upd[1] + S.upd[2] * S.upd[2]);
-            if ((del_obj < 0.000001) || (del_mag < 0.01)) stop = 1;
+            const double m2 = S.upd[0] * S.upd[0] + S.upd[1] * S.upd[1] + S.upd[2] * S.upd[2];
+            const bool small_du = m2 < 0.99999e-4 || (m2 <= 1.00001e-4 && sqrt(m2) < 0.01);
+            if ((del_obj < 0.000001) || small_du) stop = 1;
           }
           S.stop = stop;
         }
@@ -1840,7 +1809,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           __syncthreads();
         }
         if (tid < 32) {
-          if (!warp_solve_mixed(S, ndof)) {
+          if (!warp_solve_chol(S, ndof)) {
             warp_qr_solve(S, ndof);
             if (tid == 0) atomicAdd(a.counters + 16, 1ull);
           }
@@ -1909,8 +1878,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
         cluster_reduce(cl, S, 2, 0);
       }
-      const float inv_sig = (float)(1.0 / sqrt(S.red[0]));
-      const float inv_T = (float)(1.0 / sqrt(S.red[1]));
+      const float inv_sig = rsqrtf((float)S.red[0]);
+      const float inv_T = rsqrtf((float)S.red[1]);
       {
         KSum v[2];
         for (int i = tid; i < nl; i += kThreads) {

@@ -230,3 +230,37 @@ def test_volume_files_streamed_to_the_gpu(eng, tmp_path):
     assert (r1["status"] == 0).all()
     E1.close()
     E2.close()
+
+
+@pytest.mark.parametrize("bpv,step", [(1, 3), (2, 4)])
+def test_whole_voxel_grid_vs_oracle(eng, oracle, bpv, step):
+    """The 5 x 5 x 5 grid with a whole-voxel step of 3 or 4 (lanes over
+    translations) against the oracle, from seeds up to two steps off the
+    truth, uint8 and uint16, cube and sphere."""
+    from digitalvolumecorrelation_gb300 import synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    rng = np.random.default_rng(70 + step)
+    shape = (96, 96, 96)
+    b = synth.blobs(shape, 3000, amp=(60.0, 200.0), seed=71)
+    aff = synth.Affine(t=(1.2, -0.7, 0.4), E=((0.004, 0.0, 0.0), (0.0, -0.003, 0.0), (0.0, 0.0, 0.005)),
+                       c=(48.0, 48.0, 48.0))
+    dt = np.uint8 if bpv == 1 else np.uint16
+    vmax = 255 if bpv == 1 else 65535
+    ref = synth.render(shape, b, noise_sigma=2.0, noise_seed=72, dtype=dt, vmax=vmax)
+    cor = synth.render(shape, b, deform=aff, noise_sigma=2.0, noise_seed=73, dtype=dt, vmax=vmax)
+    pts = synth.grid_points((4, 4, 3), 7.0, (48.0, 48.0, 48.0))
+    seeds = aff.u(pts) + rng.integers(-2, 3, pts.shape) * step + rng.normal(0, 0.3, pts.shape)
+    for geom, size, npts in (("cube", 15, 1000), ("sphere", 17, 1400)):
+        p = make_params(shape, bytes_per_voxel=bpv, subvol_geom=geom, subvol_size=size, subvol_npts=npts,
+                        num_srch_dof=6, disp_max=2 * step, basin_radius=float(step))
+        E = eng.Engine(p, ref, cor)
+        g = E.process(pts, seed_mode=1, seeds=seeds)
+        E.close()
+        o = oracle.process(p, ref, cor, pts, seed_mode=1, seeds=seeds)
+        for r in (g,):
+            np.testing.assert_array_equal(r["status"], o["status"])
+            good = o["status"] == 0
+            assert good.mean() > 0.8
+            assert np.abs(r["params"][good, :3] - o["params"][good, :3]).max() <= 1e-3
+            rel = np.abs(r["objmin"][good] - o["objmin"][good]) / np.abs(o["objmin"][good])
+            assert rel.max() <= 1e-5

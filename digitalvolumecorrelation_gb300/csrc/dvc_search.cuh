@@ -869,6 +869,7 @@ __device__ __forceinline__ void grid_chunk_lanes(
       off0 = ss.boff(o3[0] + c[0] - 1, o3[1] + c[1] - 1, o3[2] + c[2] - 1);
     }
     float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+#pragma unroll 2
     for (int m = 0; m < nb; m++) {
       const int cx = __shfl_sync(FULL, c[0], m), cy = __shfl_sync(FULL, c[1], m),
                 cz = __shfl_sync(FULL, c[2], m);
@@ -1430,6 +1431,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           float p0 = 0.f, p1 = 0.f, p2 = 0.f;
           auto body = [&](auto staged_tag) {
             constexpr bool ST = decltype(staged_tag)::value;
+#pragma unroll 2
             for (int i = lane; i < nl; i += 32) {
               int c[3];
               float f[3], g[3];

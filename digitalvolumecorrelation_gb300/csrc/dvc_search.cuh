@@ -1218,6 +1218,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const BoxGeom Gref{S.H.o_ref[0], S.H.o_ref[1], S.H.o_ref[2], K.bext[0], K.bext[1], K.bext[2]};
     const BoxGeom Gcor{S.H.o_cor[0], S.H.o_cor[1], S.H.o_cor[2], K.bext[0], K.bext[1], K.bext[2]};
     unsigned long long n_eval = 0, n_undef = 0, n_slow = 0;
+    bool gn_last;                 // set before Gauss-Newton
+    unsigned long long und_last;  // undefined-cell evaluations of its last evaluation
     if (tid == 0) S.fail = 0;
     pc.to(1);
 
@@ -1507,8 +1509,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     //   ZNSSD:   e = (t-tbar)/sig - q, J = (I - 11'/n - that that') G / sig
     // so J'J and J'e follow from G'G, G'1, G't' and G'q: chunks of kThreads
     // samples pass through shared memory, one thread per matrix entry.
+    gn_last = false;  // the last Gauss-Newton evaluation was at the final parameters
+    und_last = 0;
     {
       int it_done = 20;
+      unsigned long long und_it = 0;
       const int ntri = ndof * (ndof + 1) / 2;
       const int nent = ntri + 3 * ndof;
       // G'G in 3x3 register tiles: row blocks of the ndof gradient
@@ -1610,6 +1615,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                        : eval_sample_t<VT, IT, true, false>(ss, rg.r0, B, gsc, Gcor, c, f, gv, und)) -
                 S.shift;
             n_undef += und;
+            und_it += und;
+            s_t[i] = t;
             q = s_r[i];
             one = 1.f;
             v[0].add(t);
@@ -1768,6 +1775,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncthreads();
         if (S.stop) {
           it_done = it;
+          gn_last = true;
+          und_last = und_it;
           break;
         }
         {
@@ -1832,7 +1841,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ------------------------------------------------ final objective ---
     // obj_val_at(par_min) (Core/Search.cpp:187): explicit residuals over the
     // stored values, the reference's own two-pass formulation
-    {
+    // When Gauss-Newton stopped by its rule, the final parameters are those
+    // of its last evaluation: the sample values stored then (s_t) and their
+    // sum (S.red[0], the same values summed in the same order) are exactly
+    // what this evaluation would compute, and the range check passed.
+    n_eval += 1;
+    if (gn_last) {
+      n_undef += und_last;
+    } else {
       if (tid == 0) {
         warp_matrices(S.par, ndof, S);
         for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), S.iu[d], S.fu[d]);
@@ -1841,7 +1857,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool rot = S.use_rot;
       double pmn[3], pmx[3];
       range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
-      n_eval += 1;
       if (S.fail) goto point_done;
       if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, tmp, buf_addr[0], bar_addr[0], stage_tx);
       __syncthreads();
@@ -1869,6 +1884,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         cta_sum_comp<1>(v, S, S.cbuf[cl.parity]);
         cluster_reduce(cl, S, 1, 0);
       }
+    }
+    {
       const float tm = (float)(S.red[0] / nsub);
       {
         KSum v[2];

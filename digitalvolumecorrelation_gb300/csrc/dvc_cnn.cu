@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <random>
 #include <string>
@@ -111,6 +112,80 @@ __global__ void __launch_bounds__(256) conv_fwd8(const float *__restrict__ in, c
   }
 #pragma unroll
   for (int c = 0; c < kCoG; c++) out[((size_t)b * Cout + co0 + c) * n3 + o] = fmaxf(acc[c], 0.f);
+}
+
+// conv forward, blocked further: each thread computes CT output channels of
+// VX consecutive output voxels along x. Per input channel and (kz, ky) the
+// 2 VX + 1 input values of the row segment are read once and feed 3 VX CT
+// FMAs (weights from shared memory as [ci][tap][CT], float4 broadcasts).
+// Taps outside the volume read 0 (fma(w, 0, acc) == acc: the same result as
+// skipping them), and every output accumulates over ci, kz, ky, kx in the
+// order of conv_fwd8, so the results are bit-identical to it.
+template <int CT, int VX>
+__global__ void __launch_bounds__(128) conv_fwd_t(const float *__restrict__ in, const float *__restrict__ w,
+                                                  const float *__restrict__ bias, float *__restrict__ out,
+                                                  int B, int Cin, int Cout, int Din) {
+  extern __shared__ float4 swt[];  // [Cin * 27][CT / 4]
+  const int Do = Din / 2, n3 = Do * Do * Do, din3 = Din * Din * Din, nxg = Do / VX;
+  const int co0 = blockIdx.y * CT;
+  float *sw = reinterpret_cast<float *>(swt);
+  for (int e = threadIdx.x; e < Cin * 27 * CT; e += blockDim.x) {
+    const int c = e % CT, ck = e / CT;  // ck = ci * 27 + k
+    sw[e] = w[((size_t)(co0 + c) * Cin) * 27 + ck];
+  }
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)B * Do * Do * nxg) return;
+  const int xg = (int)(t % nxg);
+  const long long r = t / nxg;
+  const int oy = (int)(r % Do), oz = (int)((r / Do) % Do), b = (int)(r / ((long long)Do * Do));
+  const int ox0 = xg * VX, x0 = 2 * ox0 - 1;
+  float acc[VX][CT];
+#pragma unroll
+  for (int c = 0; c < CT; c++) {
+    const float bv = bias[co0 + c];
+#pragma unroll
+    for (int vx = 0; vx < VX; vx++) acc[vx][c] = bv;
+  }
+  for (int ci = 0; ci < Cin; ci++) {
+    const float *ib = in + ((size_t)b * Cin + ci) * din3;
+#pragma unroll
+    for (int kz = 0; kz < 3; kz++) {
+      const int iz = 2 * oz - 1 + kz;
+#pragma unroll
+      for (int ky = 0; ky < 3; ky++) {
+        const int iy = 2 * oy - 1 + ky;
+        const bool rok = iz >= 0 && iz < Din && iy >= 0 && iy < Din;
+        const float *row = ib + ((size_t)(rok ? iz : 0) * Din + (rok ? iy : 0)) * Din;
+        float v[2 * VX + 1];
+#pragma unroll
+        for (int j = 0; j < 2 * VX + 1; j++) {
+          const int ix = x0 + j;
+          v[j] = (rok && ix >= 0 && ix < Din) ? __ldg(row + ix) : 0.f;
+        }
+        const float4 *wk = swt + (size_t)(ci * 27 + kz * 9 + ky * 3) * (CT / 4);
+#pragma unroll
+        for (int kx = 0; kx < 3; kx++)
+#pragma unroll
+          for (int c4 = 0; c4 < CT / 4; c4++) {
+            const float4 wv = wk[kx * (CT / 4) + c4];
+#pragma unroll
+            for (int vx = 0; vx < VX; vx++) {
+              const float iv = v[2 * vx + kx];
+              acc[vx][4 * c4 + 0] = fmaf(wv.x, iv, acc[vx][4 * c4 + 0]);
+              acc[vx][4 * c4 + 1] = fmaf(wv.y, iv, acc[vx][4 * c4 + 1]);
+              acc[vx][4 * c4 + 2] = fmaf(wv.z, iv, acc[vx][4 * c4 + 2]);
+              acc[vx][4 * c4 + 3] = fmaf(wv.w, iv, acc[vx][4 * c4 + 3]);
+            }
+          }
+      }
+    }
+  }
+  const int o0 = (oz * Do + oy) * Do + ox0;
+#pragma unroll
+  for (int c = 0; c < CT; c++)
+#pragma unroll
+    for (int vx = 0; vx < VX; vx++) out[((size_t)b * Cout + co0 + c) * n3 + o0 + vx] = fmaxf(acc[vx][c], 0.f);
 }
 
 // gradient w.r.t. the conv input activation, times the input's ReLU mask:
@@ -215,6 +290,50 @@ __global__ void fc_fwd(const float *__restrict__ x, const float *__restrict__ w,
   float acc = bias[j];
   for (int i = 0; i < Nin; i++) acc = fmaf(w[(size_t)j * Nin + i], x[(size_t)b * Nin + i], acc);
   y[t] = relu ? fmaxf(acc, 0.f) : acc;
+}
+
+// dense forward with 128 outputs, tiled: a block takes 8 samples and all 128
+// outputs, input and weight slices of 32 pass through shared memory
+// (coalesced reads; the weight tile padded to 33 columns against bank
+// conflicts); thread (tb, tj) accumulates outputs tj, tj + 32, tj + 64,
+// tj + 96 of sample tb over the inputs in ascending order from the bias, as
+// fc_fwd does, so the results are bit-identical to it.
+constexpr int kFcTB = 8, kFcIC = 32;
+__global__ void __launch_bounds__(256) fc_fwd128(const float *__restrict__ x, const float *__restrict__ w,
+                                                 const float *__restrict__ bias, float *__restrict__ y, int B,
+                                                 int Nin, int relu) {
+  __shared__ float sx[kFcTB][kFcIC];
+  __shared__ float sw[128][kFcIC + 1];
+  const int tid = threadIdx.x, tb = tid / 32, tj = tid % 32;
+  const int b0 = blockIdx.x * kFcTB;
+  const bool live = b0 + tb < B;
+  float acc[4];
+#pragma unroll
+  for (int m = 0; m < 4; m++) acc[m] = bias[tj + 32 * m];
+  for (int i0 = 0; i0 < Nin; i0 += kFcIC) {
+    for (int e = tid; e < kFcTB * kFcIC; e += 256) {
+      const int bb = e / kFcIC, ii = e % kFcIC;
+      sx[bb][ii] = (b0 + bb < B) ? x[(size_t)(b0 + bb) * Nin + i0 + ii] : 0.f;
+    }
+    for (int e = tid; e < 128 * kFcIC; e += 256) {
+      const int jj = e / kFcIC, ii = e % kFcIC;
+      sw[jj][ii] = w[(size_t)jj * Nin + i0 + ii];
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int ii = 0; ii < kFcIC; ii++) {
+      const float xv = sx[tb][ii];
+#pragma unroll
+      for (int m = 0; m < 4; m++) acc[m] = fmaf(sw[tj + 32 * m][ii], xv, acc[m]);
+    }
+    __syncthreads();
+  }
+  if (live)
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const float v = acc[m];
+      y[(size_t)(b0 + tb) * 128 + tj + 32 * m] = relu ? fmaxf(v, 0.f) : v;
+    }
 }
 
 // dense input gradient times the input's ReLU mask
@@ -387,17 +506,45 @@ Scales scales() {
   return s;
 }
 
+template <int CT, int VX>
+void conv_launch(dvc_cnn *c, int B, int l, cudaStream_t st) {
+  const int Do = kDin[l] / 2;
+  const size_t smem = (size_t)kCin[l] * 27 * CT * 4;
+  const long long nthr = (long long)B * Do * Do * (Do / VX);
+  const dim3 grid((unsigned)((nthr + 127) / 128), (unsigned)(kCout[l] / CT));
+  conv_fwd_t<CT, VX><<<grid, 128, smem, st>>>(c->act[l], c->p + kLay.w[l], c->p + kLay.b[l], c->act[l + 1], B,
+                                              kCin[l], kCout[l], kDin[l]);
+}
+
 // forward from act[0] (already holding the patches) to act[kNL + 2]
 void forward(dvc_cnn *c, int B, cudaStream_t st) {
-  for (int l = 0; l < kNL; l++) {
-    const int Do = kDin[l] / 2;
-    const size_t smem = (size_t)kCin[l] * 27 * kCoG * 4;
-    const dim3 grid((unsigned)(((long long)B * Do * Do * Do + 255) / 256), (unsigned)(kCout[l] / kCoG));
-    conv_fwd8<<<grid, 256, smem, st>>>(c->act[l], c->p + kLay.w[l], c->p + kLay.b[l], c->act[l + 1], B,
-                                       kCin[l], kCout[l], kDin[l]);
+  // DVC_CNN_CONV8: the one-output-per-thread kernels (conv_fwd8, fc_fwd)
+  static const bool one_voxel = getenv("DVC_CNN_CONV8") != nullptr;
+  if (one_voxel) {
+    for (int l = 0; l < kNL; l++) {
+      const int Do = kDin[l] / 2;
+      const size_t smem = (size_t)kCin[l] * 27 * kCoG * 4;
+      const dim3 grid((unsigned)(((long long)B * Do * Do * Do + 255) / 256), (unsigned)(kCout[l] / kCoG));
+      conv_fwd8<<<grid, 256, smem, st>>>(c->act[l], c->p + kLay.w[l], c->p + kLay.b[l], c->act[l + 1], B,
+                                         kCin[l], kCout[l], kDin[l]);
+    }
+  } else {
+    // output voxels per layer 16^3, 8^3, 4^3, 2^3; channel groups of 16 (8
+    // for the last: its weights, 64 x 27 x 16 floats, would not fit), two
+    // voxels per thread (measured: four voxels, 252 registers, ran the first
+    // two layers 15-25% slower; narrower groups on the last two slower too)
+    conv_launch<16, 2>(c, B, 0, st);
+    conv_launch<16, 2>(c, B, 1, st);
+    conv_launch<16, 2>(c, B, 2, st);
+    conv_launch<8, 2>(c, B, 3, st);
   }
-  fc_fwd<<<(B * kF1 + 255) / 256, 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL], c->p + kLay.b[kNL],
-                                                c->act[kNL + 1], B, kF0, kF1, 1);
+  static_assert(kF1 == 128 && kF0 % kFcIC == 0, "fc_fwd128 shape");
+  if (one_voxel)
+    fc_fwd<<<(B * kF1 + 255) / 256, 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL], c->p + kLay.b[kNL],
+                                                  c->act[kNL + 1], B, kF0, kF1, 1);
+  else
+    fc_fwd128<<<(B + kFcTB - 1) / kFcTB, 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL], c->p + kLay.b[kNL],
+                                                       c->act[kNL + 1], B, kF0, 1);
   fc_fwd<<<(B * kF2 + 255) / 256, 256, 0, st>>>(c->act[kNL + 1], c->p + kLay.w[kNL + 1],
                                                 c->p + kLay.b[kNL + 1], c->act[kNL + 2], B, kF1, kF2, 0);
 }
@@ -439,8 +586,11 @@ int dvc_cnn_create(dvc_cnn **out, unsigned seed) {
   if (!out) return dvc_internal_set_error(DVC_E_ARG, "null argument");
   // the largest layer's weight group (64 x 27 x 8 floats) exceeds the default
   // 48 KB of dynamic shared memory
+  const int big = kCin[kNL - 1] * 27 * 8 * 4;  // 55,296 bytes
   if (cudaFuncSetAttribute(conv_fwd8, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kCin[kNL - 1] * 27 * kCoG * 4) != cudaSuccess)
+                           kCin[kNL - 1] * 27 * kCoG * 4) != cudaSuccess ||
+      cudaFuncSetAttribute(conv_fwd_t<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(conv_fwd_t<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
     return dvc_internal_set_error(DVC_E_CUDA, "conv kernel attribute");
   dvc_cnn *c = new dvc_cnn();
   const size_t n = kLay.total;

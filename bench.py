@@ -33,7 +33,7 @@ METRIC = "ROI points/s at <=0.01-voxel error vs FP64 oracle (plain GPU method)"
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one search launch, per workload
 # (profiles/search_kernel_config2_bench.md)
-MEASURED_TRAFFIC = {"config2_1024cube_u16_60800pts_sphere41_dof12": 57.36e9 + 56.28e6}
+MEASURED_TRAFFIC = {"config2_1024cube_u16_60800pts_sphere41_dof12": 90.290e9 + 64.90e6}
 
 
 def parse():
@@ -47,6 +47,8 @@ def parse():
                     help="points of the workload timed on the CPU (cpu_baseline leg)")
     ap.add_argument("--ref-sample", type=int, default=64,
                     help="points per step of the reference arm (--impl reference)")
+    ap.add_argument("--profile-cnn", action="store_true",
+                    help="one network forward pass over 1024 random patches, for profilers")
     ap.add_argument("--profile-case", action="store_true",
                     help="one search launch on a small case for profilers: the bench "
                          "configuration's subvolumes and search on 384^3 uint16 volumes, "
@@ -192,6 +194,29 @@ def profile_case():
                       "evaluations": E.last_counters()[0], "sample_evals": E.last_counters()[0] * 4000}))
 
 
+def profile_cnn(batch=1024, passes=3):
+    """The learned proposer's forward pass (patches to 12 parameters) over a
+    batch of 1024 random patches, `passes` times (random weights: the cost
+    does not depend on them)."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    net = engine.Cnn(seed=3)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.randn((batch, 2, 32, 32, 32), generator=g, device="cuda", dtype=torch.float32)
+    y = torch.empty((batch, 12), dtype=torch.float32, device="cuda")
+    for _ in range(passes):
+        net.forward(batch, x, y)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    net.forward(batch, x, y)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    print(json.dumps({"profile_cnn": batch, "forward_ms": round(ms, 3), "patches_per_s": round(batch / ms * 1e3)}))
+    net.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -199,6 +224,8 @@ def main():
         return run_reference(args, rank, world)
     if args.profile_case:
         return profile_case()
+    if args.profile_cnn:
+        return profile_cnn()
     if args.pipeline_only:
         import torch
         torch.cuda.set_device(local)
@@ -482,7 +509,7 @@ BATCHING_ORACLE_CONFIGS = ((21, "cube", 3, "ssd"), (41, "sphere", 12, "znssd"), 
                            (81, "sphere", 12, "ssd"))
 
 
-def batching_leg(steps=3, warmup=1, tune_points=4000, oracle_per_config=16):
+def batching_leg(steps=2, warmup=1, tune_points=4000, oracle_per_config=16):
     """Configuration 3: 40,000 scattered points, each with its own search
     configuration (60 in all), searched by one persistent launch of a plan
     whose launch shape the autotuner picks; the launch is also captured in a

@@ -678,18 +678,29 @@ size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, boo
   k.stage_on = 1;
   for (int d = 0; d < 3; d++) k.stage[d] = stage[d];
   k.stage_tx = (unsigned)((size_t)stage[0] * stage[1] * stage[2] * esize);
+  // the reference region needs no grid reach: a smaller box in the same
+  // buffer (odd pitch when it fits, else the plain one, else the full box)
+  const size_t full = (size_t)stage[0] * stage[1] * stage[2] * esize;
+  int sr[3];
+  bool fit = false;
+  for (int odd = 1; odd >= 0 && !fit; odd--) {
+    stage_dims(e, C, esize, 0.0, k.rank_start, odd != 0, sr);
+    fit = (size_t)sr[0] * sr[1] * sr[2] * esize <= full;
+  }
+  for (int d = 0; d < 3; d++) k.stage_ref[d] = fit ? sr[d] : stage[d];
+  k.stage_ref_tx = (unsigned)((size_t)k.stage_ref[0] * k.stage_ref[1] * k.stage_ref[2] * esize);
   return bytes;
 }
 
 // Tensor map of volume `vol` (the engine's correlate or reference volume)
-// with configuration k's staging box.
-bool encode_stage_map(const dvc_engine *e, const SearchCfg &k, const void *vol, CUtensorMap *tm) {
+// with box `bx` (the configuration's correlate or reference staging box).
+bool encode_stage_map(const dvc_engine *e, const int bx[3], const void *vol, CUtensorMap *tm) {
   const dvc_params &p = e->p;
   const int esize = p.bytes_per_voxel;
   memset(tm, 0, sizeof *tm);
   const cuuint64_t gdim[3] = {(cuuint64_t)p.vol_wide, (cuuint64_t)p.vol_high, (cuuint64_t)p.vol_tall};
   const cuuint64_t gstride[2] = {(cuuint64_t)p.vol_wide * esize, (cuuint64_t)p.vol_wide * p.vol_high * esize};
-  const cuuint32_t box[3] = {(cuuint32_t)k.stage[0], (cuuint32_t)k.stage[1], (cuuint32_t)k.stage[2]};
+  const cuuint32_t box[3] = {(cuuint32_t)bx[0], (cuuint32_t)bx[1], (cuuint32_t)bx[2]};
   const cuuint32_t estride[3] = {1, 1, 1};
   return encode_tiled_fn()(tm, esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3,
                            const_cast<void *>(vol), gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -976,7 +987,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   CUtensorMap tmap, tmap_ref;
   memset(&tmap, 0, sizeof tmap);
   memset(&tmap_ref, 0, sizeof tmap_ref);
-  if (stage_bytes && !(encode_stage_map(e, k, e->cor, &tmap) && encode_stage_map(e, k, e->ref, &tmap_ref))) {
+  if (stage_bytes && !(encode_stage_map(e, k.stage, e->cor, &tmap) && encode_stage_map(e, k.stage_ref, e->ref, &tmap_ref))) {
     k = SearchCfg{};
     cap = fill_config(e, C, k);
     stage_bytes = 0;
@@ -1215,8 +1226,8 @@ static int plan_build(dvc_plan *pl, int C, int staging) {
     memset(&maps[(size_t)i * 2], 0, 2 * sizeof(CUtensorMap));
     if (!tma_ok) continue;
     const size_t b = stage_config(pl->cfgs[i], C, budget, state_bytes(cap), true, ks[(size_t)i]);
-    if (b && encode_stage_map(pl->cfgs[i], ks[(size_t)i], pl->cfgs[i]->cor, &maps[(size_t)i * 2]) &&
-        encode_stage_map(pl->cfgs[i], ks[(size_t)i], pl->cfgs[i]->ref, &maps[(size_t)i * 2 + 1])) {
+    if (b && encode_stage_map(pl->cfgs[i], ks[(size_t)i].stage, pl->cfgs[i]->cor, &maps[(size_t)i * 2]) &&
+        encode_stage_map(pl->cfgs[i], ks[(size_t)i].stage_ref, pl->cfgs[i]->ref, &maps[(size_t)i * 2 + 1])) {
       sb = std::max(sb, b);
       n_staged++;
     } else {

@@ -65,6 +65,9 @@ struct SearchCfg {
   int stage_on;
   int stage[3];
   unsigned stage_tx;
+  // the reference region's box (no grid reach; fits the same buffer)
+  int stage_ref[3];
+  unsigned stage_ref_tx;
   const CUtensorMap *tmap;       // this configuration's tensor map, or null: the kernel's
   const CUtensorMap *tmap_ref;   // the same box over the reference volume
   int rank_start[9];             // sample range of each cluster rank
@@ -748,10 +751,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
 
 // Staged region covering positions [pmin, pmax] (global voxel coordinates)
 // with the stencil margin; ok = 0 when it does not fit the staging box.
-__device__ __forceinline__ Region make_region(const SearchCfg &a, const double pmin[3],
-                                              const double pmax[3], int esize) {
+__device__ __forceinline__ Region make_region_box(int on, const int box[3], const double pmin[3],
+                                                  const double pmax[3], int esize) {
   Region r;
-  r.ok = a.stage_on;
+  r.ok = on;
   const int al = 16 / esize;
   for (int d = 0; d < 3; d++) {
     const double lo = floor(pmin[d]) - 2.0, hi = floor(pmax[d]) + 3.0;
@@ -763,9 +766,14 @@ __device__ __forceinline__ Region make_region(const SearchCfg &a, const double p
     int l = (int)lo;
     if (d == 0) l = (l >= 0) ? (l / al) * al : -(((-l) + al - 1) / al) * al;
     r.r0[d] = l;
-    if ((int)hi - l + 1 > a.stage[d]) r.ok = 0;
+    if ((int)hi - l + 1 > box[d]) r.ok = 0;
   }
   return r;
+}
+
+__device__ __forceinline__ Region make_region(const SearchCfg &a, const double pmin[3],
+                                              const double pmax[3], int esize) {
+  return make_region_box(a.stage_on, a.stage, pmin, pmax, esize);
 }
 
 template <typename VT, int IT, bool GRAD>
@@ -1255,9 +1263,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     // buffer that later holds the correlate region (same box)
     if (K.stage_on) {
       if (tid == 0) {
-        const Region r = make_region(K, S.lbmn, S.lbmx, esize);
+        const Region r = make_region_box(1, K.stage_ref, S.lbmn, S.lbmx, esize);
         S.reg[0] = r;
-        if (r.ok) tma_load_3d(tmp_ref, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
+        if (r.ok) tma_load_3d(tmp_ref, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], K.stage_ref_tx);
       }
       __syncthreads();
       if (S.reg[0].ok) {
@@ -1268,7 +1276,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     {
       const Region rr = S.reg[0];
       const bool rstaged = K.stage_on && rr.ok;
-      const SSrc<VT> ssr{buf_addr[0], rr.r0[0], rr.r0[1], rr.r0[2], B[0], B[1]};
+      const int Br[3] = {K.stage_ref[0], K.stage_ref[1], K.stage_ref[2]};
+      const SSrc<VT> ssr{buf_addr[0], rr.r0[0], rr.r0[1], rr.r0[2], Br[0], Br[1]};
       KSum rk[2];
       for (int i = tid; i < nl; i += kThreads) {
         int c[3], ip[3];
@@ -1287,7 +1296,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         clamp_cell(c, K.bext);
         bool und;
         float g[3];
-        const float r = rstaged ? eval_sample_t<VT, IT, false, true>(ssr, rr.r0, B, gsr, Gref, c, f, g, und)
+        const float r = rstaged ? eval_sample_t<VT, IT, false, true>(ssr, rr.r0, Br, gsr, Gref, c, f, g, und)
                                 : interp_global<VT, IT, false>(gsr, Gref, c, f, g, und);
         n_undef += und;
         s_r[i] = r;
@@ -1433,7 +1442,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           float p0 = 0.f, p1 = 0.f, p2 = 0.f;
           auto body = [&](auto staged_tag) {
             constexpr bool ST = decltype(staged_tag)::value;
-#pragma unroll 2
+#pragma unroll (ST ? 2 : 1)
             for (int i = lane; i < nl; i += 32) {
               int c[3];
               float f[3], g[3];

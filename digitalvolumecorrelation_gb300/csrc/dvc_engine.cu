@@ -260,7 +260,7 @@ struct dvc_engine {
   size_t counters_off = 0;  // offset of the last call's counters in ws
   int num_sms = 0;
   int cluster = 0;          // CTAs per point (0 = choose per call)
-  int last_cluster = 0, last_grid = 0, last_staged = 0;
+  int last_cluster = 0, last_grid = 0, last_staged = 0, last_smem = 0;
 };
 
 // Several configurations on the same volumes, one launch shape for all.
@@ -538,7 +538,7 @@ EncodeTiledFn encode_tiled_fn() {
 // of the stable sample offsets, plus stencil, rounding and warp margins; x
 // rounded so every copy starts and spans whole 16-byte units.
 void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int rs[9], bool odd,
-                int out[3]) {
+                int out[3], bool zreach = true) {
   double emax[3] = {0.0, 0.0, 0.0};
   for (int r = 0; r < C; r++) {
     const int lo = rs[r], hi = rs[r + 1];
@@ -551,7 +551,7 @@ void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int r
     for (int d = 0; d < 3; d++) emax[d] = std::max(emax[d], mx[d] - mn[d]);
   }
   const int al = 16 / esize;
-  for (int d = 0; d < 3; d++) out[d] = (int)ceil(emax[d] + 2.0 * reach) + 6;
+  for (int d = 0; d < 3; d++) out[d] = (int)ceil(emax[d] + ((d < 2 || zreach) ? 2.0 * reach : 0.0)) + 6;
   // rows of an odd number of 16-byte units: consecutive rows then start in
   // all eight 16-byte bank groups, so the gathers of nearby samples spread
   // over the 32 shared-memory banks (an even count uses half of them)
@@ -667,15 +667,25 @@ size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, boo
     const int n = (int)((double)p.disp_max / p.basin_radius);
     reach = n * ((double)p.disp_max / n);
   }
+  // the box covers the grid's translations in x, y and z; when that does not
+  // fit, one z slab of translations at a time (the grid restages per slab)
   int stage[3] = {0, 0, 0};
   size_t bytes = 0;
-  for (int odd = 1; odd >= 0; odd--) {
-    stage_dims(e, C, esize, reach, k.rank_start, odd != 0, stage);
-    bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;
-    if (bytes + state <= budget) break;
+  bool fits = false;
+  int slab = 0;
+  for (int zr = 1; zr >= 0 && !fits; zr--) {
+    if (zr == 0 && reach == 0.0) break;
+    for (int odd = 1; odd >= 0; odd--) {
+      stage_dims(e, C, esize, reach, k.rank_start, odd != 0, stage, zr != 0);
+      bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;
+      fits = bytes + state <= budget && stage[0] <= 256 && stage[1] <= 256 && stage[2] <= 256;
+      if (fits) break;
+    }
+    slab = zr == 0;
   }
-  if (stage[0] > 256 || stage[1] > 256 || stage[2] > 256 || bytes + state > budget) return 0;
+  if (!fits || (slab && getenv("DVC_NO_SLAB"))) return 0;
   k.stage_on = 1;
+  k.stage_slab = slab;
   for (int d = 0; d < 3; d++) k.stage[d] = stage[d];
   k.stage_tx = (unsigned)((size_t)stage[0] * stage[1] * stage[2] * esize);
   // the reference region needs no grid reach: a smaller box in the same
@@ -955,18 +965,20 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   const dvc_params &p = e->p;
 
   // launch shape: one cluster of C CTAs per point in flight, persistent grid
-  // of as many clusters as fit. Points waiting on neighbours (the reference's
-  // seeding) favour wide clusters (short per-point latency); independent
-  // points favour narrow ones (fewer cluster barriers). Each CTA stages the
-  // correlate region of its samples in shared memory (TMA) when the volume's
-  // layout allows it and the box fits.
+  // of as many clusters as fit. About 512 samples per CTA or more with the
+  // reference's seeding (its points wait on neighbours, which favours shorter
+  // per-point latency), 1024 for independent points; clusters of 8 place
+  // only 120 CTAs on the 152 SMs, clusters of 4 place 144. Each CTA stages
+  // the correlate region of its samples in shared memory (TMA) when the
+  // volume's layout allows it and a box fits: one covering every grid
+  // translation, else one per z slab of translations, else a wider cluster.
   size_t budget = 0;
   rc = dyn_budget(&budget);
   if (rc) return rc;
   const bool tma_ok = tma_layout(e);
   int C = e->cluster;
   if (C <= 0) {
-    const int per = (seed_mode == DVC_SEED_NEIGHBOURS) ? 256 : 1024;
+    const int per = (seed_mode == DVC_SEED_NEIGHBOURS) ? 512 : 1024;
     C = 1;
     while (C < 8 && e->n_sub / (2 * C) >= per) C *= 2;
   }
@@ -1011,11 +1023,12 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   if (getenv("DVC_VERBOSE"))
     fprintf(stderr, "dvc search: %d points, cluster %d, grid %d CTAs, staged %d (box %d x %d x %d), "
             "dynamic smem %zu of %zu, samples/CTA <= %d, grid step %s\n", n_process, C, grid,
-            k.stage_on, k.stage[0], k.stage[1], k.stage[2], smem_dyn, budget, cap,
+            k.stage_on ? (k.stage_slab ? 2 : 1) : 0, k.stage[0], k.stage[1], k.stage[2], smem_dyn, budget, cap,
             k.inc_int ? "integral" : (k.do_grid ? "general" : "none"));
   e->last_cluster = C;
   e->last_grid = grid;
-  e->last_staged = k.stage_on;
+  e->last_staged = k.stage_on ? (k.stage_slab ? 2 : 1) : 0;
+  e->last_smem = (int)smem_dyn;
   return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, tmap, tmap_ref, smem_dyn, grid, C, st, nullptr);
 }
 
@@ -1366,6 +1379,7 @@ int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_
   e->last_cluster = C;
   e->last_grid = grid;
   e->last_staged = plan->n_staged > 0;
+  e->last_smem = (int)plan->smem_dyn;
   CUtensorMap tm0;
   memset(&tm0, 0, sizeof tm0);
   return dispatch_launch(e->p.bytes_per_voxel, e->p.interp_type, a, tm0, tm0, plan->smem_dyn, grid, C, st, nullptr);
@@ -1427,6 +1441,15 @@ int dvc_gpu_plan_autotune(dvc_plan *plan, const int *point_cfg_dev, int n_points
   cudaEventDestroy(ev1);
   const int rc2 = plan_build(plan, rc == DVC_OK ? bestC : C0, rc == DVC_OK ? bestS : S0);
   return rc ? rc : rc2;
+}
+
+int dvc_gpu_last_launch(dvc_engine *e, int out[4]) {
+  if (!e || !out) return set_error(DVC_E_ARG, "null argument");
+  out[0] = e->last_cluster;
+  out[1] = e->last_grid;
+  out[2] = e->last_staged;
+  out[3] = e->last_smem;
+  return DVC_OK;
 }
 
 int dvc_gpu_set_cluster(dvc_engine *e, int cluster) {

@@ -63,6 +63,7 @@ struct SearchCfg {
   // staging of the correlate volume: box of stage[0] x stage[1] x stage[2]
   // voxels (stage_tx bytes), TMA-loaded into the staging buffer
   int stage_on;
+  int stage_slab;  // the box covers one z slab of the grid's translations
   int stage[3];
   unsigned stage_tx;
   // the reference region's box (no grid reach; fits the same buffer)
@@ -1399,27 +1400,36 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       if (S.fail) goto point_done;
-      // one staged region covering this CTA's samples under every translation
-      if (tid == 0) {
-        double pmn[3], pmx[3];
-        for (int d = 0; d < 3; d++) {
-          pmn[d] = S.lbmn[d] + S.par[d] - k * inc;
-          pmx[d] = S.lbmx[d] + S.par[d] + k * inc;
-        }
-        Region r = make_region(K, pmn, pmx, esize);
-        S.reg[0] = r;
-        if (r.ok) tma_load_3d(tmp, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
-      }
-      __syncthreads();
-      const Region rg = S.reg[0];
-      if (rg.ok) {
-        if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
-        phase[0] ^= 1u;
-      }
-      const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
+      // one staged region covering this CTA's samples under every
+      // translation, or (slab boxes) under the translations of one z offset,
+      // restaged per chunk of side^2 translations (z-major order, so the
+      // first strict minimum is the same)
+      const bool slab = K.stage_slab != 0;
+      const int chunk = slab ? side * side : kGridChunk;
       const int lane = tid & 31, warp = tid >> 5;
-      for (int o0 = 0; o0 < total; o0 += kGridChunk) {
-        const int nch = min(kGridChunk, total - o0);
+      for (int o0 = 0; o0 < total; o0 += chunk) {
+        const int nch = min(chunk, total - o0);
+        if (o0 == 0 || slab) {
+          if (tid == 0) {
+            const double zo = slab ? (double)(o0 / (side * side) - k) * inc : 0.0;
+            double pmn[3], pmx[3];
+            for (int d = 0; d < 3; d++) {
+              const bool zs = slab && d == 2;
+              pmn[d] = S.lbmn[d] + S.par[d] + (zs ? zo : -k * inc);
+              pmx[d] = S.lbmx[d] + S.par[d] + (zs ? zo : k * inc);
+            }
+            Region r = make_region(K, pmn, pmx, esize);
+            S.reg[0] = r;
+            if (r.ok) tma_load_3d(tmp, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
+          }
+          __syncthreads();
+          if (S.reg[0].ok) {
+            if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
+            phase[0] ^= 1u;
+          }
+        }
+        const Region rg = S.reg[0];
+        const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
         if (tid < nch) {
           const int o = o0 + tid;
           const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};

@@ -78,6 +78,7 @@ def load(path: str | None = None):
                                           C.POINTER(C.c_int), C.c_void_p]
     L.dvc_gpu_order_neighbours.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip]
     L.dvc_gpu_set_cluster.argtypes = [C.c_void_p, C.c_int]
+    L.dvc_gpu_last_launch.argtypes = [C.c_void_p, _ip]
     L.dvc_gpu_read_mhd.argtypes = [C.c_char_p, C.POINTER(DvcVolumeInfo)]
     L.dvc_gpu_load_raw.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.c_int, C.c_void_p]
@@ -203,6 +204,13 @@ class Engine:
                                             ptr(status_dev), ptr(objmin_dev), ptr(params_dev),
                                             ptr(gn_iters_dev), C.byref(nfb), C.c_void_p(stream)))
         return nfb.value
+
+    def last_launch(self):
+        """dict(cluster, ctas, staging (0 none, 1 every translation, 2 per z
+        slab), smem_bytes) of the most recent search launch."""
+        out = (C.c_int * 4)()
+        _check(_lib.dvc_gpu_last_launch(self._h, out))
+        return dict(cluster=out[0], ctas=out[1], staging=out[2], smem_bytes=out[3])
 
     def last_counters(self):
         """(evaluations, Gauss-Newton iterations, undefined-cell evaluations)

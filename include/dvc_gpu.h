@@ -220,6 +220,11 @@ int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *po
    on the width only through FP32/FP64 summation order. No counterpart in
    the reference (one thread per point). */
 int dvc_gpu_set_cluster(dvc_engine *e, int cluster);
+/* Shape of this engine's most recent search launch: out[0] CTAs per point,
+   out[1] CTAs in the grid, out[2] staging of the correlate region (0 none,
+   1 one box covering every grid translation, 2 one box per z slab of
+   translations), out[3] dynamic shared memory per CTA in bytes. */
+int dvc_gpu_last_launch(dvc_engine *e, int out[4]);
 
 /* Counters of the most recent dvc_gpu_process / dvc_gpu_process_device call
    on this engine (waits for it to finish): out[0] objective evaluations

@@ -264,3 +264,36 @@ def test_whole_voxel_grid_vs_oracle(eng, oracle, bpv, step):
             assert np.abs(r["params"][good, :3] - o["params"][good, :3]).max() <= 1e-3
             rel = np.abs(r["objmin"][good] - o["objmin"][good]) / np.abs(o["objmin"][good])
             assert rel.max() <= 1e-5
+
+
+def test_grid_with_slab_staging_vs_oracle(eng, oracle):
+    """Cube 41 / 3375 samples, uint16, 5 x 5 x 5 grid of step 3, at cluster
+    width 4: the box covering every translation does not fit beside the
+    sample state, so the grid stages one z slab of translations at a time.
+    Against the oracle, from seeds up to two steps off the truth."""
+    from digitalvolumecorrelation_gb300 import synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    rng = np.random.default_rng(81)
+    shape = (112, 112, 112)
+    b = synth.blobs(shape, 4000, amp=(2000.0, 60000.0), seed=82)
+    aff = synth.Affine(t=(0.9, -1.3, 0.6), E=((0.003, 0.0, 0.0), (0.0, 0.002, 0.0), (0.0, 0.0, -0.004)),
+                       c=(56.0, 56.0, 56.0))
+    ref = synth.render(shape, b, noise_sigma=150.0, noise_seed=83, dtype=np.uint16, vmax=65535)
+    cor = synth.render(shape, b, deform=aff, noise_sigma=150.0, noise_seed=84, dtype=np.uint16, vmax=65535)
+    pts = synth.grid_points((2, 2, 2), 10.0, (56.0, 56.0, 56.0))
+    seeds = aff.u(pts) + rng.integers(-2, 3, pts.shape) * 3 + rng.normal(0, 0.3, pts.shape)
+    p = make_params(shape, bytes_per_voxel=2, subvol_geom="cube", subvol_size=41, subvol_npts=3000,
+                    num_srch_dof=6, disp_max=6, basin_radius=3.0)
+    E = eng.Engine(p, ref, cor)
+    E.set_cluster(4)
+    g = E.process(pts, seed_mode=1, seeds=seeds)
+    launch = E.last_launch()
+    E.close()
+    assert launch["cluster"] == 4 and launch["staging"] == 2
+    o = oracle.process(p, ref, cor, pts, seed_mode=1, seeds=seeds)
+    np.testing.assert_array_equal(g["status"], o["status"])
+    good = o["status"] == 0
+    assert good.all()
+    assert np.abs(g["params"][good, :3] - o["params"][good, :3]).max() <= 1e-3
+    rel = np.abs(g["objmin"][good] - o["objmin"][good]) / np.abs(o["objmin"][good])
+    assert rel.max() <= 1e-5

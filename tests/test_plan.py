@@ -171,3 +171,48 @@ def test_plan_autotune(case):
     plan.close()
     for E in engines:
         E.close()
+
+
+def test_plan_launch_in_a_cuda_graph(case):
+    """After one call has sized the workspace, the plan's launch (memsets,
+    dataflow kernels, search) is captured in a CUDA graph; replays give
+    exactly the results of the direct call (reference seeding across the
+    configurations)."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine, workloads
+    engines, keep = _engines(case)
+    plan = engine.Plan(engines)
+    n = len(case["pts"])
+    order, neigh = workloads.order_and_neighbours(case["pts"])
+    dev = torch.device("cuda")
+    t = lambda a, dt=None: torch.as_tensor(a, dtype=dt, device=dev)
+    cfg_d, pts_d, od, nd = t(case["cfg"]), t(case["pts"]), t(order), t(neigh)
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+    ob = torch.empty(n, dtype=torch.float64, device=dev)
+    pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
+    its = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def call(stream):
+        plan.process_device(cfg_d, n, pts_d, od, n, nd, neigh.shape[1], engine.SEED_NEIGHBOURS, None, st, ob,
+                            pa, its, stream=stream)
+
+    call(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    direct = [x.clone() for x in (st, ob, pa, its)]
+    for x in (st, ob, pa, its):
+        x.zero_()
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+        call(side.cuda_stream)
+    for _ in range(2):
+        g.replay()
+        torch.cuda.synchronize()
+        for a, b in zip((st, ob, pa, its), direct):
+            assert torch.equal(a, b)
+    assert (direct[0] == 0).float().mean().item() > 0.8
+    del g
+    plan.close()
+    for E in engines:
+        E.close()

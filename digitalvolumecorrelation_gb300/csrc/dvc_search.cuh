@@ -943,6 +943,140 @@ __device__ __forceinline__ void grid_chunk_lanes(
   }
 }
 
+// The same evaluation with groups of exactly nch threads (any nch <= 128, so a
+// slab of 25 translations keeps 250 of 256 threads busy where groups of 32
+// lanes keep 200): thread j of a group evaluates translation o0 + j. A group
+// may straddle two warps, so per round each thread prepares one sample of its
+// group into a shared record (interpolation weights, reference quantity,
+// stencil offset, packed cell) that every thread of the group then reads as
+// a broadcast. `rec` holds 16 floats per thread (16-byte aligned), `s_scr`
+// the group partial sums afterwards.
+template <typename VT, int IT>
+__device__ __forceinline__ void grid_chunk_groups(
+    CtaState &S, const int *s_ip, const float *s_fp, const float *s_r, int nl, float *rec, float *s_scr,
+    const SSrc<VT> &ss, const int r0[3], const int B[3], const GSrc<VT> &gsc, const BoxGeom &G, int o0,
+    int nch, int side, int k, int parity, bool sad, unsigned long long &n_undef, unsigned long long &n_slow) {
+  constexpr int esize = (int)sizeof(VT);
+  const int tid = threadIdx.x;
+  const int groups = kThreads / nch;
+  const int grp = tid / nch, j = tid % nch;
+  const bool in = grp < groups;
+  // this thread's translation
+  const int step = S.cfg.inc_int;
+  const int o = o0 + j;
+  const int dc[3] = {(o % side - k) * step, ((o / side) % side - k) * step, (o / (side * side) - k) * step};
+  const int dbytes = ((dc[2] * B[1] + dc[1]) * B[0] + dc[0]) * esize;
+  const int n3[3] = {G.bx, G.by, G.bz};
+  const int o3[3] = {G.ox, G.oy, G.oz};
+  int lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    lo[d] = max(IT == 2 ? 1 : 0, r0[d] + 1 - o3[d]) - dc[d];
+    hi[d] = min(min(n3[d] - (IT == 2 ? 3 : 2), S.cfg.bext[d] - 1), r0[d] + B[d] - 3 - o3[d]) - dc[d];
+  }
+  int iu0[3];
+  float fu0[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), iu0[d], fu0[d]);
+  // this group's samples, in rounds of nch (one per thread)
+  const int s_lo = in ? (int)(((long long)nl * grp) / groups) : 0;
+  const int s_hi = in ? (int)(((long long)nl * (grp + 1)) / groups) : 0;
+  const int per = (nl + groups - 1) / groups;
+  const int rounds = (per + nch - 1) / nch;
+  const float4 *rg4 = reinterpret_cast<const float4 *>(rec) + (size_t)(in ? grp : 0) * nch * 4;
+  KSum k0, k1, k2;
+  for (int r = 0; r < rounds; r++) {
+    const int sb0 = s_lo + r * nch;
+    const int cnt = in ? max(0, min(nch, s_hi - sb0)) : 0;
+    if (in && j < cnt) {
+      int c[3];
+      float f[3];
+      sample_pos(s_ip, s_fp, sb0 + j, S, iu0, fu0, false, c, f);
+      float w[3][4], dw[4];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        if (IT == 2) {
+          cr_weights(f[d], w[d], dw);
+        } else {
+          w[d][0] = 0.f; w[d][1] = 1.f - f[d]; w[d][2] = f[d]; w[d][3] = 0.f;
+        }
+      }
+      float4 *my = reinterpret_cast<float4 *>(rec) + (size_t)tid * 4;
+      my[0] = make_float4(w[0][0], w[0][1], w[0][2], w[0][3]);
+      my[1] = make_float4(w[1][0], w[1][1], w[1][2], w[1][3]);
+      my[2] = make_float4(w[2][0], w[2][1], w[2][2], w[2][3]);
+      // cells as signed 16-bit pairs (box-local, so far inside that range)
+      my[3] = make_float4(s_r[sb0 + j],
+                          __uint_as_float(ss.boff(o3[0] + c[0] - 1, o3[1] + c[1] - 1, o3[2] + c[2] - 1)),
+                          __int_as_float((c[0] & 0xffff) | (c[1] << 16)), __int_as_float(c[2]));
+    }
+    __syncthreads();
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+#pragma unroll 2
+    for (int m = 0; m < cnt; m++) {
+      const float4 wx4 = rg4[m * 4], wy4 = rg4[m * 4 + 1], wz4 = rg4[m * 4 + 2], x4 = rg4[m * 4 + 3];
+      const int cp = __float_as_int(x4.z);
+      const int cx = (cp << 16) >> 16, cy = cp >> 16, cz = __float_as_int(x4.w);
+      const float q = x4.x;
+      float t;
+      if (cx >= lo[0] && cx <= hi[0] && cy >= lo[1] && cy <= hi[1] && cz >= lo[2] && cz <= hi[2]) {
+        const float wx[4] = {wx4.x, wx4.y, wx4.z, wx4.w}, wy[4] = {wy4.x, wy4.y, wy4.z, wy4.w},
+                    wz[4] = {wz4.x, wz4.y, wz4.z, wz4.w};
+        float g[3];
+        t = contract_h<SSrc<VT>, false>(ss, ss.stencil_at(__float_as_uint(x4.y) + (uint32_t)dbytes), wx, wy, wz,
+                                        wx, wy, wz, g);
+      } else {
+        int c[3];
+        float f[3];
+        sample_pos(s_ip, s_fp, sb0 + m, S, iu0, fu0, false, c, f);
+        int cc[3] = {c[0] + dc[0], c[1] + dc[1], c[2] + dc[2]};
+        clamp_cell(cc, S.cfg.bext);
+        float g[3];
+        bool und;
+        t = eval_sample_t<VT, IT, false, true>(ss, r0, B, gsc, G, cc, f, g, und);
+        n_undef += und;
+        n_slow++;
+      }
+      t -= S.shift;
+      if (sad) {
+        p0 += fabsf(t - q);
+      } else {
+        p0 += t;
+        p1 += t * t;
+        p2 += t * q;
+      }
+    }
+    k0.add(p0);
+    k1.add(p1);
+    k2.add(p2);
+    __syncthreads();  // the records are rewritten next round
+  }
+  // groups -> chunk sums (FP32 pairs in scratch, merged by TwoSum, FP64 in cbuf)
+  float *part = s_scr;  // [groups][nch][6]
+  if (in) {
+    float *my = part + ((size_t)grp * nch + j) * 6;
+    my[0] = k0.s; my[1] = -k0.c;
+    my[2] = k1.s; my[3] = -k1.c;
+    my[4] = k2.s; my[5] = -k2.c;
+  }
+  __syncthreads();
+  if (tid < nch) {
+    float h[3], l[3];
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+      h[m] = part[(size_t)tid * 6 + 2 * m];
+      l[m] = part[(size_t)tid * 6 + 2 * m + 1];
+    }
+    for (int g2 = 1; g2 < groups; g2++) {
+      const float *pp = part + ((size_t)g2 * nch + tid) * 6;
+#pragma unroll
+      for (int m = 0; m < 3; m++) two_sum_merge(h[m], l[m], pp[2 * m], pp[2 * m + 1]);
+    }
+#pragma unroll
+    for (int m = 0; m < 3; m++) S.cbuf[parity][3 * tid + m] = (double)h[m] + (double)l[m];
+  }
+}
+
 // Keep the staged region when it covers positions [pmn, pmx] with the stencil
 // margin; otherwise stage a new one into the same buffer. One thread; returns
 // 1 when a copy was started (the block then waits for it).
@@ -1106,6 +1240,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   float *s_r = s_fp + 3 * cap;
   float *s_t = s_r + cap;
   float *s_G = s_t + cap;  // [kGRows][kThreads]
+  // the grid's shared sample records (16 floats per thread, 16-byte aligned)
+  // reuse the final values and chunk rows, free during the grid phase
+  float *grid_rec = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(s_t) + 15) & ~(uintptr_t)15);
+  const bool grid_groups = grid_rec + 16 * kThreads <= s_G + kGRows * kThreads;
   const uint32_t bar_addr[2] = {smem_addr(&S.bar[0]), smem_addr(&S.bar[1])};
   const uint32_t buf_addr[2] = {smem_addr(stage_buf[0]), smem_addr(stage_buf[1])};
   uint32_t phase[2] = {0u, 0u};
@@ -1439,7 +1577,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
         __syncthreads();
-        if (IT != 0 && rg.ok && K.inc_int > 0) {
+        if (IT != 0 && rg.ok && K.inc_int > 0 && grid_groups) {
+          grid_chunk_groups<VT, IT>(S, s_ip, s_fp, s_r, nl, grid_rec, grid_rec, ss, rg.r0, B, gsc, Gcor, o0, nch,
+                                    side, k, cl.parity, sad, n_undef, n_slow);
+        } else if (IT != 0 && rg.ok && K.inc_int > 0) {
           grid_chunk_lanes<VT, IT>(a, S, s_ip, s_fp, s_r, nl, s_G, ss, rg.r0, B, gsc, Gcor, o0, nch,
                                    side, k, cl.parity, sad, n_undef, n_slow);
         } else {

@@ -1012,7 +1012,7 @@ __device__ __forceinline__ void grid_chunk_groups(
     }
     __syncthreads();
     float p0 = 0.f, p1 = 0.f, p2 = 0.f;
-#pragma unroll 2
+#pragma unroll 1
     for (int m = 0; m < cnt; m++) {
       const float4 wx4 = rg4[m * 4], wy4 = rg4[m * 4 + 1], wz4 = rg4[m * 4 + 2], x4 = rg4[m * 4 + 3];
       const int cp = __float_as_int(x4.z);

@@ -983,7 +983,7 @@ __device__ __forceinline__ void grid_chunk_groups(
   const int s_hi = in ? (int)(((long long)nl * (grp + 1)) / groups) : 0;
   const int per = (nl + groups - 1) / groups;
   const int rounds = (per + nch - 1) / nch;
-  const float4 *rg4 = reinterpret_cast<const float4 *>(rec) + (size_t)(in ? grp : 0) * nch * 4;
+  const uint32_t rg_addr = smem_addr(rec + (size_t)(in ? grp : 0) * nch * 16);
   KSum k0, k1, k2;
   for (int r = 0; r < rounds; r++) {
     const int sb0 = s_lo + r * nch;
@@ -1014,16 +1014,26 @@ __device__ __forceinline__ void grid_chunk_groups(
     float p0 = 0.f, p1 = 0.f, p2 = 0.f;
 #pragma unroll 1
     for (int m = 0; m < cnt; m++) {
-      const float4 wx4 = rg4[m * 4], wy4 = rg4[m * 4 + 1], wz4 = rg4[m * 4 + 2], x4 = rg4[m * 4 + 3];
-      const int cp = __float_as_int(x4.z);
-      const int cx = (cp << 16) >> 16, cy = cp >> 16, cz = __float_as_int(x4.w);
-      const float q = x4.x;
+      // the record by 8-byte loads (two groups' records per warp: 16-byte
+      // loads took more wavefronts), the weights only on the fast path
+      const uint32_t ra = rg_addr + (uint32_t)m * 64u;
+      const uint2 h0 = lds64(ra + 48), h1 = lds64(ra + 56);
+      const float q = __uint_as_float(h0.x);
+      const uint32_t obv = h0.y;
+      const int cp = (int)h1.x, cz = (int)h1.y;
+      const int cx = (cp << 16) >> 16, cy = cp >> 16;
       float t;
       if (cx >= lo[0] && cx <= hi[0] && cy >= lo[1] && cy <= hi[1] && cz >= lo[2] && cz <= hi[2]) {
-        const float wx[4] = {wx4.x, wx4.y, wx4.z, wx4.w}, wy[4] = {wy4.x, wy4.y, wy4.z, wy4.w},
-                    wz[4] = {wz4.x, wz4.y, wz4.z, wz4.w};
+        float wx[4], wy[4], wz[4];
+#pragma unroll
+        for (int a2 = 0; a2 < 2; a2++) {
+          const uint2 ux = lds64(ra + 8 * a2), uy = lds64(ra + 16 + 8 * a2), uz = lds64(ra + 32 + 8 * a2);
+          wx[2 * a2] = __uint_as_float(ux.x); wx[2 * a2 + 1] = __uint_as_float(ux.y);
+          wy[2 * a2] = __uint_as_float(uy.x); wy[2 * a2 + 1] = __uint_as_float(uy.y);
+          wz[2 * a2] = __uint_as_float(uz.x); wz[2 * a2 + 1] = __uint_as_float(uz.y);
+        }
         float g[3];
-        t = contract_h<SSrc<VT>, false>(ss, ss.stencil_at(__float_as_uint(x4.y) + (uint32_t)dbytes), wx, wy, wz,
+        t = contract_h<SSrc<VT>, false>(ss, ss.stencil_at(obv + (uint32_t)dbytes), wx, wy, wz,
                                         wx, wy, wz, g);
       } else {
         int c[3];

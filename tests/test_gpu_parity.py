@@ -232,11 +232,14 @@ def test_volume_files_streamed_to_the_gpu(eng, tmp_path):
     E2.close()
 
 
-@pytest.mark.parametrize("bpv,step", [(1, 3), (2, 4)])
-def test_whole_voxel_grid_vs_oracle(eng, oracle, bpv, step):
-    """The 5 x 5 x 5 grid with a whole-voxel step of 3 or 4 (lanes over
-    translations) against the oracle, from seeds up to two steps off the
-    truth, uint8 and uint16, cube and sphere."""
+@pytest.mark.parametrize("bpv,step,cluster", [(1, 3, None), (2, 4, None), (2, 3, 8)])
+def test_whole_voxel_grid_vs_oracle(eng, oracle, bpv, step, cluster):
+    """The 5 x 5 x 5 grid with a whole-voxel step of 3 or 4 against the
+    oracle, from seeds up to two steps off the truth, uint8 and uint16, cube
+    and sphere. One CTA per point evaluates it by thread groups of one chunk
+    with shared sample records; clusters of 8 leave at most ~190 samples per
+    CTA, too few for the record area, so the 32-lane groups with shuffles
+    evaluate it."""
     from digitalvolumecorrelation_gb300 import synth
     from digitalvolumecorrelation_gb300.abi import make_params
     rng = np.random.default_rng(70 + step)
@@ -254,6 +257,8 @@ def test_whole_voxel_grid_vs_oracle(eng, oracle, bpv, step):
         p = make_params(shape, bytes_per_voxel=bpv, subvol_geom=geom, subvol_size=size, subvol_npts=npts,
                         num_srch_dof=6, disp_max=2 * step, basin_radius=float(step))
         E = eng.Engine(p, ref, cor)
+        if cluster:
+            E.set_cluster(cluster)
         g = E.process(pts, seed_mode=1, seeds=seeds)
         E.close()
         o = oracle.process(p, ref, cor, pts, seed_mode=1, seeds=seeds)

@@ -33,7 +33,7 @@ METRIC = "ROI points/s at <=0.01-voxel error vs FP64 oracle (plain GPU method)"
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one search launch, per workload
 # (profiles/search_kernel_config2_bench.md)
-MEASURED_TRAFFIC = {"config2_1024cube_u16_60800pts_sphere41_dof12": 93.147e9 + 286.82e6}
+MEASURED_TRAFFIC = {"config2_1024cube_u16_60800pts_sphere41_dof12": 93.161e9 + 278.46e6}
 
 
 def parse():

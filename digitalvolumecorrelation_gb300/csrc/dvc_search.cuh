@@ -1014,8 +1014,7 @@ __device__ __forceinline__ void grid_chunk_groups(
     float p0 = 0.f, p1 = 0.f, p2 = 0.f;
 #pragma unroll 1
     for (int m = 0; m < cnt; m++) {
-      // the record by 8-byte loads (two groups' records per warp: 16-byte
-      // loads took more wavefronts), the weights only on the fast path
+      // the record by 8-byte loads, the weights only on the fast path
       const uint32_t ra = rg_addr + (uint32_t)m * 64u;
       const uint2 h0 = lds64(ra + 48), h1 = lds64(ra + 56);
       const float q = __uint_as_float(h0.x);

@@ -663,10 +663,16 @@ size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, boo
   const dvc_params &p = e->p;
   const int esize = p.bytes_per_voxel;
   double reach = 0.0;
+  int side = 1;
   if (grid && p.basin_radius != 0.0) {
     const int n = (int)((double)p.disp_max / p.basin_radius);
     reach = n * ((double)p.disp_max / n);
+    side = 2 * n + 1;
   }
+  // a slab is reduced as one chunk of side^2 translations: at most
+  // kGridChunk of them (grids of side 13 and more stage the whole box or
+  // nothing)
+  const bool slab_ok = side * side <= kGridChunk;
   // the box covers the grid's translations in x, y and z; when that does not
   // fit, one z slab of translations at a time (the grid restages per slab)
   int stage[3] = {0, 0, 0};
@@ -674,7 +680,7 @@ size_t stage_config(const dvc_engine *e, int C, size_t budget, size_t state, boo
   bool fits = false;
   int slab = 0;
   for (int zr = 1; zr >= 0 && !fits; zr--) {
-    if (zr == 0 && reach == 0.0) break;
+    if (zr == 0 && (reach == 0.0 || !slab_ok)) break;
     for (int odd = 1; odd >= 0; odd--) {
       stage_dims(e, C, esize, reach, k.rank_start, odd != 0, stage, zr != 0);
       bytes = (((size_t)stage[0] * stage[1] * stage[2] * esize + 16) + 127) & ~(size_t)127;

@@ -302,3 +302,38 @@ def test_grid_with_slab_staging_vs_oracle(eng, oracle):
     assert np.abs(g["params"][good, :3] - o["params"][good, :3]).max() <= 1e-3
     rel = np.abs(g["objmin"][good] - o["objmin"][good]) / np.abs(o["objmin"][good])
     assert rel.max() <= 1e-5
+
+
+def test_wide_grid_without_slab_staging_vs_oracle(eng, oracle):
+    """A 13 x 13 x 13 grid (disp_max 6, basin_radius 1) on cube 41 / 3375
+    samples, uint16, asked for cluster width 4: its box does not fit there,
+    and a z slab of 169 translations is more than one grid chunk, so the
+    engine widens the cluster (or leaves the region unstaged) instead of
+    staging slabs. Against the oracle, from seeds up to four voxels off the
+    truth."""
+    from digitalvolumecorrelation_gb300 import synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    rng = np.random.default_rng(91)
+    shape = (112, 112, 112)
+    b = synth.blobs(shape, 4000, amp=(2000.0, 60000.0), seed=92)
+    aff = synth.Affine(t=(-0.8, 1.1, 0.5), E=((0.002, 0.0, 0.0), (0.0, -0.003, 0.0), (0.0, 0.0, 0.002)),
+                       c=(56.0, 56.0, 56.0))
+    ref = synth.render(shape, b, noise_sigma=150.0, noise_seed=93, dtype=np.uint16, vmax=65535)
+    cor = synth.render(shape, b, deform=aff, noise_sigma=150.0, noise_seed=94, dtype=np.uint16, vmax=65535)
+    pts = synth.grid_points((2, 2, 1), 10.0, (56.0, 56.0, 56.0))
+    seeds = aff.u(pts) + rng.integers(-4, 5, pts.shape) + rng.normal(0, 0.3, pts.shape)
+    p = make_params(shape, bytes_per_voxel=2, subvol_geom="cube", subvol_size=41, subvol_npts=3000,
+                    num_srch_dof=6, disp_max=6, basin_radius=1.0)
+    E = eng.Engine(p, ref, cor)
+    E.set_cluster(4)
+    g = E.process(pts, seed_mode=1, seeds=seeds)
+    launch = E.last_launch()
+    E.close()
+    assert launch["staging"] != 2
+    o = oracle.process(p, ref, cor, pts, seed_mode=1, seeds=seeds)
+    np.testing.assert_array_equal(g["status"], o["status"])
+    good = o["status"] == 0
+    assert good.all()
+    assert np.abs(g["params"][good, :3] - o["params"][good, :3]).max() <= 1e-3
+    rel = np.abs(g["objmin"][good] - o["objmin"][good]) / np.abs(o["objmin"][good])
+    assert rel.max() <= 1e-5

@@ -76,6 +76,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(ms, world, device=None):
+    """The slowest rank's step time: all-reduce MAX of `ms` over the process
+    group (replicas: each rank searches its own copy of the workload)."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n_points, world, ms):
+    """Whole-job points/s: every rank's points over the slowest rank's time."""
+    return n_points * world / (ms / 1e3)
+
+
 def workload(cfg):
     from digitalvolumecorrelation_gb300 import workloads
     return workloads.config1() if cfg == 1 else workloads.config2()
@@ -278,16 +295,12 @@ def main():
     ev1.record()
     torch.cuda.synchronize()
     clocks = clk.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
     status = status_d.cpu().numpy()
     params = params_d.cpu().numpy()
     objmin = objmin_d.cpu().numpy()
     its = its_d.cpu().numpy()
-    value = n * world / (ms / 1e3)
+    value = replica_value(n, world, ms)
 
     # sample-evaluations per launch (the roofline's unit), from the counts the
     # engine keeps: per point, the reference subvolume, every grid offset, each

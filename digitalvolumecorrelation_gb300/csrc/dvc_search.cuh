@@ -161,7 +161,6 @@ struct CtaState {
   int giu[kGridChunk][3];
   float gfu[kGridChunk][3];
   double objv[kGridChunk];
-  float wpart[kWarps][kGridChunk * 3];
   double cbuf[2][kCB];
   double red[kCB];
   float wred[kWarps][2 * 8];

@@ -22,6 +22,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -108,7 +109,9 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples: DVC_CLOCKS_DIR (default: the system temporary directory)
+        out_dir = os.environ.get("DVC_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, f"dvc_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:

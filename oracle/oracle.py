@@ -2,7 +2,7 @@
 
 Two checkers live under oracle/:
   * liboracle.so  — dvc_oracle.cpp, the FP64 restatement of the reference's
-                    hot path (builds anywhere: here and on the GPU box);
+                    hot path (builds on any host with g++);
   * _ref/libdvcref.so — the reference's own Core/*.cpp compiled by
                     build_ref.sh (only where the reference sources exist).
 Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg import

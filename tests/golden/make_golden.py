@@ -16,7 +16,7 @@ on small seeded synthetic volumes, what the reference computes:
   * end-to-end runs of the reference's `dvc` and `strain` programs
     (input file, point cloud and raw volumes -> .disp, .stat, .sort.csv,
     strain CSVs); `--dvc-runs` regenerates only these.
-The GPU machine has no reference sources, so its tests read these files.
+Machines without the reference sources run the tests from these files.
 """
 from __future__ import annotations
 

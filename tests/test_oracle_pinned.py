@@ -1,7 +1,7 @@
 """The FP64 oracle restatement against the reference's recorded outputs.
 
-Runs wherever the oracle builds (here and on the GPU machine): it pins the
-checker used by the GPU parity tests to the reference itself.
+Runs wherever the oracle builds (no reference sources needed): it pins the
+oracle used by the GPU parity tests to the reference itself.
 """
 import numpy as np
 import pytest

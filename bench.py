@@ -32,9 +32,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ROI points/s at <=0.01-voxel error vs FP64 oracle (plain GPU method)"
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one search launch, per workload
-# (profiles/search_kernel_config2_bench.md)
-MEASURED_TRAFFIC = {"config2_1024cube_u16_60800pts_sphere41_dof12": 93.161e9 + 278.46e6}
+# FP32 work of one sample-evaluation as the search kernel performs it (the
+# separable tricubic form): 64 stencil products + 16 + 4 for the y and z
+# passes, 3 x 8 for the Catmull-Rom weights, ~8 for the warp and the
+# compensated objective sums: about 100 FMA = 200 FLOP
+FP32_FLOP_PER_SAMPLE = 200.0
+FP32_LANES_PER_SM = 128
 
 
 def parse():
@@ -47,7 +50,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=384,
                     help="points of the workload timed on the CPU (cpu_baseline leg)")
     ap.add_argument("--ref-sample", type=int, default=64,
-                    help="points per step of the reference arm (--impl reference)")
+                    help="points per step of the reference arm (--impl reference): the first "
+                         "points of the processing order")
     ap.add_argument("--profile-cnn", action="store_true",
                     help="one network forward pass over 1024 random patches, for profilers")
     ap.add_argument("--profile-case", action="store_true",
@@ -97,6 +101,19 @@ def replica_value(n_points, world, ms):
 def workload(cfg):
     from digitalvolumecorrelation_gb300 import workloads
     return workloads.config1() if cfg == 1 else workloads.config2()
+
+
+def bench_config(W, world):
+    """The `config` object of both arms' JSON lines (the same workload)."""
+    from digitalvolumecorrelation_gb300.synth import cube_subvol_count
+    p = W.params()
+    n_sub = p.subvol_npts if p.subvol_geom == 1 else cube_subvol_count(p.subvol_npts)
+    return {"workload": W.name, "points": len(W.points), "volume": list(W.shape),
+            "bytes_per_voxel": W.bytes_per_voxel, "n_sub": n_sub,
+            "seeding": "reference (neighbours, processing order)",
+            "l2": "inputs larger than L2 (two %d MiB volumes)" % (W.nvox * W.bytes_per_voxel >> 20),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "params": W.params_kw}
 
 
 class Clocks:
@@ -167,18 +184,24 @@ def seeds_from_results(order, neigh, status, params, rigid, n_process):
     return seeds
 
 
-def cpu_leg(W, p, ref_np, cor_np, pts, seeds, gpu_params, sample, threads):
+def cpu_leg(W, p, ref_np, cor_np, pts, seeds, gpu, sample, threads):
     """The FP64 oracle (a port of the reference path) on a bounded sample of
-    points with the GPU run's seeds: time and error against the GPU."""
+    points with the GPU run's seeds: its time, and the GPU's agreement with
+    it on the metric's terms (status, u/v/w, objmin)."""
     from oracle.oracle import Oracle
     O = Oracle()
     idx = sample
     t0 = time.perf_counter()
     r = O.process(p, ref_np, cor_np, pts[idx], seed_mode=1, seeds=seeds[idx], n_threads=threads)
     dt = time.perf_counter() - t0
-    good = r["status"] == 0
-    err = float(np.abs(r["params"][good, :3] - gpu_params[idx][good, :3]).max()) if good.any() else None
-    return len(idx) / dt, dt, err, r
+    st, ob, pa = gpu["status"][idx], gpu["objmin"][idx], gpu["params"][idx]
+    good = (r["status"] == 0) & (st == 0)
+    acc = {"same_status": int((r["status"] == st).sum()), "points": len(idx),
+           "max_abs_du_gpu_vs_oracle_vox": float(np.abs(r["params"][good, :3] - pa[good, :3]).max())
+           if good.any() else None,
+           "max_rel_objmin_gpu_vs_oracle": float((np.abs(ob[good] - r["objmin"][good]) /
+                                                  np.abs(r["objmin"][good])).max()) if good.any() else None}
+    return len(idx) / dt, dt, acc, r
 
 
 def profile_case():
@@ -298,6 +321,9 @@ def main():
     ev1.record()
     torch.cuda.synchronize()
     clocks = clk.stop()
+    device_status = E.last_status()  # a bounded wait that gave up would show here
+    if device_status != 0:
+        raise SystemExit(f"search launch reported device status {device_status}")
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
     status = status_d.cpu().numpy()
     params = params_d.cpu().numpy()
@@ -320,9 +346,12 @@ def main():
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak_tf = peaks.get("bf16_tflops", 1900.0)
     achieved = sample_evals * flop_per_sample / (ms / 1e3) / 1e12
-    # DRAM bytes of one search launch of this workload, from the one-pass ncu
-    # capture summarised in profiles/search_kernel_config2_bench.md
-    traffic = MEASURED_TRAFFIC.get(W.name)
+    # the FP32 pipes' peak at the clock seen in the timed region: every SM's
+    # 128 FP32 lanes, one FMA (2 FLOP) per lane per cycle
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    fp32_peak = props.multi_processor_count * FP32_LANES_PER_SM * 2.0 * sm_mhz * 1e6 / 1e12
+    fp32_achieved = sample_evals * FP32_FLOP_PER_SAMPLE / (ms / 1e3) / 1e12
 
     # accuracy: truth and oracle sample
     truth = W.truth()
@@ -332,13 +361,11 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded speckle pair rendered on the GPU; no public dataset)",
-        "config": {"workload": W.name, "points": n, "volume": list(W.shape),
-                   "bytes_per_voxel": W.bytes_per_voxel, "n_sub": n_sub,
-                   "seeding": "reference (neighbours, processing order)",
-                   "l2": "inputs larger than L2 (two %d MiB volumes)" % (W.nvox * W.bytes_per_voxel >> 20),
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "params": W.params_kw},
-        "gpu_launches": 3 * args.steps,
+        "config": bench_config(W, world),
+        # per step: outputs initialised, ranks, and for the dataflow schedule the
+        # dependency count, prefix sum, successor fill and ready queue; the search
+        "gpu_launches": 7 * args.steps,
+        "device_status": device_status,
         "results": {"good": int(good.sum()), "range_fail": int((status == -1).sum()),
                     "mean_gn_iters": float(its[good].mean()) if good.any() else None,
                     "evaluations": evals, "undefined_cell_evaluations": undefined,
@@ -347,11 +374,21 @@ def main():
                     if good.any() else None},
         "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak_tf,
                      "unit": "TFLOP/s", "frac": round(achieved / peak_tf, 4),
-                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram read+write)",
+                     "traffic": None,
+                     "traffic_note": "DRAM bytes are not measurable inside the run; the one-pass ncu "
+                                     "capture of this launch reads 2.1x the algorithmic bytes",
                      "flop_per_unit": flop_per_sample, "units_per_launch": sample_evals,
+                     "peak_source": "measured bf16 (burst)" if "bf16_tflops" in peaks else "fallback",
                      "note": "algorithmic FLOPs of the fused 64x64 coefficient product per "
                              "sample-evaluation; the kernel evaluates the same interpolant in "
-                             "separable form (~90 FMA per sample-evaluation)"},
+                             "separable form on the FP32 pipes (roofline_fp32)"},
+        "roofline_fp32": {"bound": "fp32", "achieved": round(fp32_achieved, 2), "peak": round(fp32_peak, 1),
+                          "unit": "TFLOP/s", "frac": round(fp32_achieved / fp32_peak, 4),
+                          "flop_per_unit": FP32_FLOP_PER_SAMPLE, "units_per_launch": sample_evals,
+                          "peak_source": f"{props.multi_processor_count} SMs x {FP32_LANES_PER_SM} FP32 "
+                                         f"lanes x 2 FLOP x {sm_mhz:.0f} MHz (median SM clock of the run)",
+                          "note": "the FP32 work the kernel performs per sample-evaluation; the rest of a "
+                                  "point's time is its serial sections and the seeding's dependency chain"},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_e2e:
@@ -365,12 +402,13 @@ def main():
             ref_np = ref_np.view(np.uint16)
             cor_np = cor_np.view(np.uint16)
         threads = os.cpu_count() or 1
-        pps, dt, err, _ = cpu_leg(W, p, ref_np, cor_np, W.points, seeds, params, sample, threads)
+        gpu = dict(status=status, objmin=objmin, params=params)
+        pps, dt, acc, _ = cpu_leg(W, p, ref_np, cor_np, W.points, seeds, gpu, sample, threads)
         result["cpu_baseline"] = {"value": round(pps, 4), "unit": "points/s", "cores": threads,
                                   "kind": "port", "seconds": round(dt, 2),
                                   "sample": f"{len(sample)} points of the same workload (evenly "
                                             "spaced in processing order) with the GPU run's seeds",
-                                  "max_abs_du_gpu_vs_oracle_vox": err}
+                                  "accuracy": acc}
     if rank == 0 and not args.no_learned and world == 1:
         result["learned"], weights = learned_leg(args.learned_steps)
         if args.pipeline:
@@ -647,7 +685,7 @@ def batching_leg(steps=2, warmup=1, tune_points=4000, oracle_per_config=16):
     }
 
 
-def e2e_leg(W, p, order, neigh, ref_d, cor_d, n):
+def e2e_leg(W, p, order, neigh, ref_d, cor_d, n, iters=3):
     """Through the C ABI with host buffers: upload both volumes from pinned
     host memory, search, read back all results."""
     import torch
@@ -660,7 +698,7 @@ def e2e_leg(W, p, order, neigh, ref_d, cor_d, n):
         ref_np = ref_np.view(np.uint16)
         cor_np = cor_np.view(np.uint16)
     times = []
-    for it in range(2):
+    for it in range(1 + iters):  # one untimed warm-up call, then `iters` timed ones
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         E = engine.Engine(p, ref_np, cor_np)
@@ -668,77 +706,62 @@ def e2e_leg(W, p, order, neigh, ref_d, cor_d, n):
         E.close()
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
-    dt = min(times[1:]) if len(times) > 1 else times[0]
+    dt = statistics.median(times[1:])
     h2d = 2 * W.nvox * W.bytes_per_voxel + W.points.nbytes + order.nbytes + neigh.nbytes
     d2h = n * (4 + 8 + 96 + 4)
     return {"value": round(n / dt, 2), "unit": "points/s", "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "seconds": round(dt, 3)}
+            "d2h_bytes_per_step": int(d2h), "seconds": round(dt, 3),
+            "timing": f"median of {iters} calls after one warm-up call",
+            "seconds_each": [round(t, 3) for t in times[1:]]}
 
 
 def run_reference(args, rank, world):
-    """The reference's CPU implementation of the path on the host cores: the
-    FP64 oracle port (the reference itself is not built on this machine) on a
-    bounded sample of the same workload per step."""
+    """The reference's CPU implementation of the path on the host cores, on
+    the GPU arm's workload: the FP64 port of its search (oracle/; the
+    reference's own sources are not on this machine to build), with the
+    reference's seeding over the first --ref-sample points of the same
+    processing order (the reference's own `num_points_to_process` subset),
+    on the same two volumes, rendered by the same generator outside the
+    timed region and copied to host memory. Every step searches that prefix
+    again; all host threads."""
     if rank != 0:
         return
-    from digitalvolumecorrelation_gb300 import synth
+    import torch
+    from digitalvolumecorrelation_gb300 import workloads
+    from oracle.oracle import Oracle
     W = workload(args.config)
     p = W.params()
-    # a CPU rendering of the same workload definition is out of reach for
-    # 1 GiB volumes in a few minutes, so each step processes points of a
-    # cropped copy: the sample points' own neighbourhoods rendered on the CPU
-    n_sample = max(1, args.ref_sample)
-    idx = np.linspace(0, len(W.points) - 1, n_sample).astype(int)
-    crop = 2 * int(np.ceil(p.subvol_size / 2.0 * max(p.subvol_aspect[:]) + p.disp_max + 8))
-    from oracle.oracle import Oracle
+    order, neigh = workloads.order_and_neighbours(W.points)
+    ref_d, cor_d = W.render_device()
+    ref_np = ref_d[: W.nvox].cpu().numpy()
+    cor_np = cor_d[: W.nvox].cpu().numpy()
+    del ref_d, cor_d
+    torch.cuda.empty_cache()
+    if W.bytes_per_voxel == 2:
+        ref_np, cor_np = ref_np.view(np.uint16), cor_np.view(np.uint16)
+    n_sample = max(1, min(args.ref_sample, len(W.points)))
     O = Oracle()
     threads = os.cpu_count() or 1
-    from digitalvolumecorrelation_gb300.abi import make_params
-    crops = []  # rendered once, outside the timed calls
-    for i in idx:
-        pt = W.points[i]
-        lo = np.floor(pt - crop / 2).astype(int)
-        shape = (crop, crop, crop)
-        b = W.blobs.copy()
-        b[:, :3] -= lo
-        keep = np.all((b[:, :3] > -12) & (b[:, :3] < crop + 12), axis=1)
-        dt_ = np.uint8 if W.bytes_per_voxel == 1 else np.uint16
-        ref = synth.render(shape, b[keep], None, W.noise_sigma, 1000 + i, dtype=dt_)
-
-        class Shift:
-            kind = 0
-
-            def __init__(self, lo):
-                self.lo = lo
-
-            def u(self, X):
-                return W.deform.u(np.asarray(X) + self.lo)
-
-            def inverse(self, x):
-                return W.deform.inverse(np.asarray(x) + self.lo) - self.lo
-
-        cor = synth.render(shape, b[keep], Shift(lo), W.noise_sigma, 2000 + i, dtype=dt_)
-        pc = make_params(shape, bytes_per_voxel=W.bytes_per_voxel, **W.params_kw)
-        crops.append((pc, ref, cor, (pt - lo)[None, :], W.truth(pt[None, :])))
-    rates = []
+    secs = []
     for s in range(args.warmup + args.steps):
-        t_total = 0.0
-        for pc, ref, cor, local, seed in crops:
-            t0 = time.perf_counter()
-            O.process(pc, ref, cor, local, seed_mode=1, seeds=seed, n_threads=threads)
-            t_total += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r = O.process(p, ref_np, cor_np, W.points, order=order, neigh=neigh, n_process=n_sample,
+                      seed_mode=0, n_threads=threads)
         if s >= args.warmup:
-            rates.append(len(idx) / t_total)
-    v = float(np.mean(rates))
+            secs.append(time.perf_counter() - t0)
+    step_s = float(np.mean(secs))
+    v = n_sample / step_s
+    done = order[:n_sample]
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "points/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": W.name, "params": W.params_kw},
-        "cpu_baseline": {"value": round(v, 4), "unit": "points/s", "cores": threads,
-                         "kind": "port",
-                         "sample": f"{len(idx)} points per step, each on a cropped copy of its "
-                                   "neighbourhood, seeded with the true displacement"},
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the GPU arm's volumes: same generator and seeds)",
+        "config": bench_config(W, world),
+        "cpu_baseline": {"value": round(v, 4), "unit": "points/s", "cores": threads, "kind": "port",
+                         "sample": f"the first {n_sample} points of the processing order per step, "
+                                   "the reference's neighbour seeding, full search (grid + Gauss-Newton)"},
+        "results": {"good": int((r["status"][done] == 0).sum()), "range_fail": int((r["status"][done] == -1).sum())},
         "e2e": {"value": round(v, 4), "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }))

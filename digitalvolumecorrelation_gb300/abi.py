@@ -10,6 +10,8 @@ OBJ = {"sad": 0, "ssd": 1, "zssd": 2, "nssd": 3, "znssd": 4}
 INTERP = {"nearest": 0, "trilinear": 1, "tricubic": 2}
 GEOM = {"cube": 0, "sphere": 1}
 SEED_NEIGHBOURS, SEED_GIVEN, SEED_RIGID, SEED_PARAMS = 0, 1, 2, 3
+COARSE = {"grid": 0, "random": 1}
+REFINE = {"gauss_newton": 0, "nelder_mead": 1}
 
 
 class DvcParams(C.Structure):
@@ -24,6 +26,7 @@ class DvcParams(C.Structure):
         ("sphere_seed", C.c_uint),
         ("subvol_thresh", C.c_int), ("gray_thresh_min", C.c_double), ("gray_thresh_max", C.c_double),
         ("min_vol_fract", C.c_double),
+        ("coarse_method", C.c_int), ("refine_method", C.c_int), ("coarse_seed", C.c_uint),
     ]
 
 
@@ -39,7 +42,8 @@ def make_params(shape_xyz, bytes_per_voxel=1, subvol_geom="cube", subvol_size=31
                 subvol_npts=2000, subvol_aspect=(1.0, 1.0, 1.0), disp_max=12, num_srch_dof=6,
                 obj_function="znssd", interp_type="tricubic", basin_radius=0.0,
                 rigid_trans=(0.0, 0.0, 0.0), sphere_seed=1, subvol_thresh=False, gray_thresh_min=25.0,
-                gray_thresh_max=125.0, min_vol_fract=0.2) -> DvcParams:
+                gray_thresh_max=125.0, min_vol_fract=0.2, coarse_method="grid",
+                refine_method="gauss_newton", coarse_seed=1) -> DvcParams:
     p = DvcParams()
     p.vol_wide, p.vol_high, p.vol_tall = (int(v) for v in shape_xyz)
     p.bytes_per_voxel = int(bytes_per_voxel)
@@ -58,4 +62,7 @@ def make_params(shape_xyz, bytes_per_voxel=1, subvol_geom="cube", subvol_size=31
     p.gray_thresh_min = float(gray_thresh_min)
     p.gray_thresh_max = float(gray_thresh_max)
     p.min_vol_fract = float(min_vol_fract)
+    p.coarse_method = COARSE[coarse_method] if isinstance(coarse_method, str) else int(coarse_method)
+    p.refine_method = REFINE[refine_method] if isinstance(refine_method, str) else int(refine_method)
+    p.coarse_seed = int(coarse_seed)
     return p

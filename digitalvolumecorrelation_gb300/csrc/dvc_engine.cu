@@ -26,8 +26,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <random>
 #include <string>
@@ -254,10 +257,14 @@ struct dvc_engine {
   // the same split into whole voxels and FP32 fractions in [0, 1)
   int *d_off_i = nullptr;
   float *d_off_f = nullptr;
+  double *d_rand_off = nullptr;  // random_global's translations (coarse_method random)
   // grow-only per-call workspace
   void *ws = nullptr;
   size_t ws_bytes = 0;
-  size_t counters_off = 0;  // offset of the last call's counters in ws
+  // control block of the last search call (work counter, error flag, queue
+  // tail, counters from +64): in ws, or in the allocation-free scratch
+  char *last_ctl = nullptr;
+  long long wait_polls = -1;  // dependency-wait bound of the search (< 0: default)
   int num_sms = 0;
   int cluster = 0;          // CTAs per point (0 = choose per call)
   int last_cluster = 0, last_grid = 0, last_staged = 0, last_smem = 0;
@@ -309,7 +316,33 @@ int validate(const dvc_params *p) {
   for (int d = 0; d < 3; d++)
     if (!(p->subvol_aspect[d] >= 0.1 && p->subvol_aspect[d] <= 10.0))
       return set_error(DVC_E_ARG, "subvol_aspect components must be in [0.1, 10]");
+  if (p->coarse_method != DVC_COARSE_GRID && p->coarse_method != DVC_COARSE_RANDOM)
+    return set_error(DVC_E_ARG, "coarse_method must be DVC_COARSE_GRID or DVC_COARSE_RANDOM");
+  if (p->refine_method != DVC_REFINE_GAUSS_NEWTON && p->refine_method != DVC_REFINE_NELDER_MEAD)
+    return set_error(DVC_E_ARG, "refine_method must be DVC_REFINE_GAUSS_NEWTON or DVC_REFINE_NELDER_MEAD");
   return DVC_OK;
+}
+
+// random_global's translations (Core/Search.cpp:1045-1098): num_pts of them,
+// 3 draws each in x, y, z order, displ_max * (2 * rand()) / RAND_MAX with the
+// doubled draw an int product (wrapping as two's complement above 2^30, as
+// the reference's compiled code does); rand() after srand(seed) is the C
+// library's generator, drawn here from a private state (initstate_r /
+// random_r give the same sequence) so the caller's rand() is left alone.
+std::vector<double> random_global_offsets(int num_pts, double displ_max, unsigned seed) {
+  struct random_data rd;
+  memset(&rd, 0, sizeof rd);
+  int32_t state[32];  // the 128-byte state of srand() / rand()
+  initstate_r(seed, reinterpret_cast<char *>(state), sizeof state, &rd);
+  const double dbl_rand_max = RAND_MAX;
+  std::vector<double> rel((size_t)num_pts * 3);
+  for (size_t k = 0; k < rel.size(); k++) {
+    int32_t r = 0;
+    random_r(&rd, &r);
+    const int twice = (int)(2u * (uint32_t)r);
+    rel[k] = displ_max * (twice / dbl_rand_max);
+  }
+  return rel;
 }
 
 // Search::Search geometry: subvolume count and the nominal interpolation box
@@ -460,6 +493,13 @@ int engine_finish(dvc_engine *e) {
     CUDA_TRY(cudaMalloc(&e->d_off_f, m * sizeof(float)));
     CUDA_TRY(cudaMemcpy(e->d_off_i, oi.data(), m * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(e->d_off_f, of.data(), m * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  if (e->p.coarse_method == DVC_COARSE_RANDOM && e->p.basin_radius != 0.0) {
+    const int num_inc = (int)(e->p.disp_max / e->p.basin_radius);
+    const int side = 2 * num_inc + 1;
+    const std::vector<double> rel = random_global_offsets(side * side * side, e->p.disp_max, e->p.coarse_seed);
+    CUDA_TRY(cudaMalloc(&e->d_rand_off, rel.size() * sizeof(double)));
+    CUDA_TRY(cudaMemcpy(e->d_rand_off, rel.data(), rel.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   CUDA_TRY(cudaGetDevice(&e->device));
   CUDA_TRY(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device));
@@ -624,6 +664,9 @@ int fill_config(const dvc_engine *e, int C, SearchCfg &k) {
     k.inc = displ_max / k.num_inc;
     k.inc_int = (k.inc == std::floor(k.inc) && k.inc <= 64.0 && !getenv("DVC_GENERAL_GRID")) ? (int)k.inc : 0;
   }
+  k.coarse_random = (k.do_grid && p.coarse_method == DVC_COARSE_RANDOM) ? 1 : 0;
+  k.rand_off = e->d_rand_off;
+  k.refine_nm = p.refine_method == DVC_REFINE_NELDER_MEAD ? 1 : 0;
   k.thresh_on = p.subvol_thresh ? 1 : 0;
   k.gmin = (float)p.gray_thresh_min;
   k.gmax = (float)p.gray_thresh_max;
@@ -724,6 +767,12 @@ bool encode_stage_map(const dvc_engine *e, const int bx[3], const void *vol, CUt
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The control block at the start of every search call's scratch: int work
+// counter, int error flag, int ready-queue tail, then the 64-bit counters.
+constexpr size_t kCtlBytes = 256;
+constexpr size_t kCountersOff = 64;
+static_assert(kCountersOff + kNumCounters * sizeof(unsigned long long) <= kCtlBytes, "control block");
+
 // One search call's points, seeds and outputs (device pointers).
 struct RunIO {
   int n_points;
@@ -756,32 +805,37 @@ int check_run(const dvc_engine *e, const RunIO &io) {
 // engine e's grow-only workspace (or `ws_fixed`), outputs initialised, ranks
 // of the processing order, and with dataflow scheduling the predecessor
 // counts, successor lists and ready queue. Fills the run fields of `a`.
-int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed, SearchArgs &a) {
+int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed, size_t ws_fixed_bytes,
+                SearchArgs &a) {
   const int n_points = io.n_points, n_process = io.n_process, n_neigh = io.n_neigh;
-  // workspace: done[n], rank[n], counter/error/counters; with dataflow
-  // scheduling also the predecessor counts, successor lists and ready queue
-  const size_t off_done = 0;
+  // workspace: the control block (kCtlBytes: work counter, error flag, queue
+  // tail, counters from +kCountersOff), done[n], rank[n]; with dataflow
+  // scheduling also the predecessor counts, successor lists and ready queue.
+  // The control block comes first, so its place does not depend on the size.
+  const size_t off_ctl = 0;
+  const size_t off_done = kCtlBytes;
   const size_t off_rank = off_done + (size_t)n_points * 4;
-  const size_t off_ctl = (off_rank + (size_t)n_points * 4 + 255) & ~(size_t)255;
   const bool dataflow = io.seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !ws_fixed &&
                         !getenv("DVC_IN_ORDER");
-  const size_t off_pend = off_ctl + 256;
+  const size_t off_pend = (off_rank + (size_t)n_points * 4 + 255) & ~(size_t)255;
   const size_t off_soff = off_pend + (size_t)n_points * 4;
   const size_t off_cursor = off_soff + ((size_t)n_points + 1) * 4;
   const size_t off_queue = off_cursor + (size_t)n_points * 4;
   const size_t off_succ = off_queue + (size_t)n_process * 4;
-  const size_t ws_need = dataflow ? off_succ + (size_t)n_process * n_neigh * 4 : off_ctl + 256;
+  const size_t ws_need = dataflow ? off_succ + (size_t)n_process * n_neigh * 4 : off_pend;
   char *ws = ws_fixed;
-  if (!ws) {
+  if (ws) {
+    if (ws_need > ws_fixed_bytes) return set_error(DVC_E_ARG, "search scratch larger than the fixed array");
+  } else {
     const int rc = ensure_ws(e, ws_need);
     if (rc) return rc;
     ws = (char *)e->ws;
-    e->counters_off = off_ctl + 64;
   }
+  e->last_ctl = ws + off_ctl;
   int *done = (int *)(ws + off_done);
   int *rank = (int *)(ws + off_rank);
   int *ctl = (int *)(ws + off_ctl);
-  CUDA_TRY(cudaMemsetAsync(ws + off_ctl, 0, 256, st));
+  CUDA_TRY(cudaMemsetAsync(ws + off_ctl, 0, kCtlBytes, st));
   {
     const int T = 256;
     const int G = (n_points + T - 1) / T;
@@ -835,7 +889,8 @@ int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed,
     a.queue_tail = ctl + 2;
   }
   a.done = done;
-  a.counters = (unsigned long long *)(ws + off_ctl + 64);
+  a.counters = (unsigned long long *)(ws + off_ctl + kCountersOff);
+  a.wait_polls = e->wait_polls < 0 ? kWaitPolls : e->wait_polls;
   return DVC_OK;
 }
 
@@ -951,17 +1006,19 @@ void dvc_gpu_destroy(dvc_engine *e) {
   }
   if (e->d_off_i) cudaFree(e->d_off_i);
   if (e->d_off_f) cudaFree(e->d_off_f);
+  if (e->d_rand_off) cudaFree(e->d_rand_off);
   if (e->ws) cudaFree(e->ws);
   delete e;
 }
 
 // The search launch with one configuration (the engine's). Scratch (done
 // flags, ranks, work counter, counters) is the engine's grow-only workspace,
-// or `ws_fixed` when the caller supplies it.
+// or `ws_fixed` (ws_fixed_bytes long) when the caller supplies it.
 static int process_device_ws(dvc_engine *e, int n_points, const double *points_dev, int n_process,
                              const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
                              const double *seeds_dev, int *status_dev, double *objmin_dev,
-                             double *params_dev, int *gn_iters_dev, void *stream, char *ws_fixed) {
+                             double *params_dev, int *gn_iters_dev, void *stream, char *ws_fixed,
+                             size_t ws_fixed_bytes = 0) {
   const RunIO io{n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev, seed_mode,
                  seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev};
   int rc = check_run(e, io);
@@ -1019,7 +1076,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   const int grid = C * std::max(1, std::min(max_clusters, n_process));
 
   SearchArgs a{};
-  rc = prepare_run(e, io, st, ws_fixed, a);
+  rc = prepare_run(e, io, st, ws_fixed, ws_fixed_bytes, a);
   if (rc) return rc;
   if (n_process == 0) return DVC_OK;
   a.cfg0 = k;
@@ -1057,26 +1114,30 @@ int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev
 // engine's workspace. It holds DVC_NOALLOC_MAX_POINTS points, belongs to every
 // GPU that loads the library until the process exits, and is shared by all
 // calls: each call clears the parts that must start at zero, and calls whose
-// work overlaps on the GPU race on it.
-static __device__ __align__(256) unsigned char
-    g_noalloc_scratch[(size_t)DVC_NOALLOC_MAX_POINTS * 8 + 512];
+// work overlaps on the GPU race on it. Layout (in-order scheduling, no
+// dataflow tables): the control block, then done[n] and rank[n], the block
+// after them rounded up to 256 bytes.
+constexpr size_t kNoallocBytes = kCtlBytes + (size_t)DVC_NOALLOC_MAX_POINTS * 8 + 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 // Device address of g_noalloc_scratch on the current device, looked up once
 // per device (the host symbol is only a stand-in, never a device address).
+// Host threads making a first call on the same device may both look it up;
+// they store the same address.
 static int noalloc_scratch(char **out) {
-  static void *addr[64] = {nullptr};
+  static std::atomic<void *> addr[64];
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return set_error(DVC_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(err));
   if (dev < 0 || dev >= 64) return set_error(DVC_E_ARG, "device index above 63");
-  if (!addr[dev]) {
-    void *p = nullptr;
+  void *p = addr[dev].load(std::memory_order_acquire);
+  if (!p) {
     err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (err != cudaSuccess || !p)
       return set_error(DVC_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(err));
-    addr[dev] = p;
+    addr[dev].store(p, std::memory_order_release);
   }
-  *out = (char *)addr[dev];
+  *out = (char *)p;
   return DVC_OK;
 }
 
@@ -1094,7 +1155,20 @@ int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *po
   if (rc) return rc;
   return process_device_ws(e, n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev,
                            seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev,
-                           stream, ws);
+                           stream, ws, kNoallocBytes);
+}
+
+// The error flag of engine e's last search launch, which has finished:
+// DVC_OK, or the DVC_E_* code the launch recorded (with its message).
+static int launch_error(dvc_engine *e) {
+  if (!e->last_ctl) return DVC_OK;
+  int ctl[2] = {0, 0};
+  CUDA_TRY(cudaMemcpy(ctl, e->last_ctl, sizeof ctl, cudaMemcpyDeviceToHost));
+  if (ctl[1] == DVC_E_TIMEOUT)
+    return set_error(DVC_E_TIMEOUT, "a bounded device-side wait gave up; points were left unsearched "
+                                     "(status DVC_NOT_SEARCH) or evaluated without staging");
+  if (ctl[1] != 0) return set_error(ctl[1], "a point named no configuration of the plan; it was left unsearched");
+  return DVC_OK;
 }
 
 // Host-array search: arguments checked, arrays copied in, the engine's (or
@@ -1177,13 +1251,9 @@ static int host_process(dvc_engine *e, dvc_plan *plan, const int *point_cfg, int
   TRYC(cudaEventRecord(ev1, 0));
   TRYC(cudaEventSynchronize(ev1));
   TRYC(cudaGetLastError());
-  int ctl[2] = {0, 0};
   unsigned long long counters[3] = {0, 0, 0};
-  if (n_process > 0) {
-    const size_t off_ctl = ((size_t)n_points * 8 + 255) & ~(size_t)255;
-    TRYC(cudaMemcpy(ctl, (char *)e->ws + off_ctl, sizeof ctl, cudaMemcpyDeviceToHost));
-    TRYC(cudaMemcpy(counters, (char *)e->ws + off_ctl + 64, sizeof counters, cudaMemcpyDeviceToHost));
-  }
+  if (n_process > 0 && e->last_ctl)
+    TRYC(cudaMemcpy(counters, e->last_ctl + kCountersOff, sizeof counters, cudaMemcpyDeviceToHost));
   TRYC(cudaMemcpy(status, d_status, N * sizeof(int), cudaMemcpyDeviceToHost));
   TRYC(cudaMemcpy(objmin, d_obj, N * sizeof(double), cudaMemcpyDeviceToHost));
   TRYC(cudaMemcpy(params, d_par, N * 12 * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1192,8 +1262,10 @@ static int host_process(dvc_engine *e, dvc_plan *plan, const int *point_cfg, int
   cudaEventElapsedTime(&kms, ev0, ev1);
   cleanup();
 #undef TRYC
-  if (ctl[1] == DVC_E_TIMEOUT) return set_error(ctl[1], "a bounded dependency wait gave up; points left unsearched");
-  if (ctl[1] != 0) return set_error(ctl[1], "a point named no configuration of the plan; it was left unsearched");
+  if (n_process > 0) {
+    rc = launch_error(e);
+    if (rc) return rc;
+  }
   if (stats) {
     memset(stats, 0, sizeof *stats);
     stats->n_processed = n_process;
@@ -1362,7 +1434,7 @@ int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_
   if (n_points == 0) return DVC_OK;
   cudaStream_t st = (cudaStream_t)stream;
   SearchArgs a{};
-  rc = prepare_run(e, io, st, nullptr, a);
+  rc = prepare_run(e, io, st, nullptr, 0, a);
   if (rc) return rc;
   if (n_process == 0) return DVC_OK;
   const int n = (int)plan->cfgs.size();
@@ -1469,29 +1541,42 @@ int dvc_gpu_set_cluster(dvc_engine *e, int cluster) {
 int dvc_gpu_last_counters(dvc_engine *e, long long out[3]) {
   if (!e || !out) return set_error(DVC_E_ARG, "null argument");
   out[0] = out[1] = out[2] = 0;
-  if (!e->ws) return DVC_OK;
+  if (!e->last_ctl) return DVC_OK;
   unsigned long long c[3];
   CUDA_TRY(cudaDeviceSynchronize());
-  CUDA_TRY(cudaMemcpy(c, (char *)e->ws + e->counters_off, sizeof c, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(c, e->last_ctl + kCountersOff, sizeof c, cudaMemcpyDeviceToHost));
   for (int k = 0; k < 3; k++) out[k] = (long long)c[k];
   return DVC_OK;
+}
+
+int dvc_gpu_set_wait_limit(dvc_engine *e, long long polls) {
+  if (!e) return set_error(DVC_E_ARG, "null engine");
+  e->wait_polls = polls < 0 ? -1 : polls;
+  return DVC_OK;
+}
+
+int dvc_gpu_last_status(dvc_engine *e) {
+  if (!e) return set_error(DVC_E_ARG, "null engine");
+  if (!e->last_ctl) return DVC_OK;
+  CUDA_TRY(cudaDeviceSynchronize());
+  return launch_error(e);
 }
 
 int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]) {
   if (!e || !out) return set_error(DVC_E_ARG, "null argument");
   for (int k = 0; k < DVC_N_PHASES; k++) out[k] = 0;
-  if (!e->ws) return DVC_OK;
+  if (!e->last_ctl) return DVC_OK;
   static_assert(DVC_N_PHASES == kPhases, "phase count");
   unsigned long long c[DVC_N_PHASES];
   CUDA_TRY(cudaDeviceSynchronize());
-  CUDA_TRY(cudaMemcpy(c, (char *)e->ws + e->counters_off + 4 * sizeof(unsigned long long), sizeof c,
+  CUDA_TRY(cudaMemcpy(c, e->last_ctl + kCountersOff + 4 * sizeof(unsigned long long), sizeof c,
                       cudaMemcpyDeviceToHost));
   for (int k = 0; k < DVC_N_PHASES; k++) out[k] = (long long)c[k];
   if (getenv("DVC_VERBOSE")) {
     unsigned long long slow = 0, fp64 = 0;
-    CUDA_TRY(cudaMemcpy(&slow, (char *)e->ws + e->counters_off + 3 * sizeof(unsigned long long),
+    CUDA_TRY(cudaMemcpy(&slow, e->last_ctl + kCountersOff + 3 * sizeof(unsigned long long),
                         sizeof slow, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(&fp64, (char *)e->ws + e->counters_off + 16 * sizeof(unsigned long long),
+    CUDA_TRY(cudaMemcpy(&fp64, e->last_ctl + kCountersOff + kCounterFp64Solves * sizeof(unsigned long long),
                         sizeof fp64, cudaMemcpyDeviceToHost));
     fprintf(stderr, "dvc search: %llu integral-grid evaluations took the general path, "
             "%llu Gauss-Newton systems used the FP64 factorisation\n", slow, fp64);
@@ -1568,6 +1653,7 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
     if (cudaMemcpyAsync(&nfb, cnt, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       rc = set_error(DVC_E_CUDA, "fallback count");
+    if (!rc) rc = launch_error(e);
   }
   if (!rc && nfb > 0) {
     if (cudaMalloc(&ob2, N * 8) != cudaSuccess || cudaMalloc(&pa2, N * 96) != cudaSuccess ||
@@ -1583,6 +1669,7 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
                                                       params_dev, gn_iters_dev);
   }
   if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = set_error(DVC_E_CUDA, "learned search");
+  if (!rc && nfb > 0) rc = launch_error(e);
   if (!rc && n_fallback) *n_fallback = nfb;
   cleanup();
   return rc;

@@ -38,7 +38,7 @@ namespace dvc {
 namespace cg = cooperative_groups;
 
 constexpr int kGridChunk = 128;               // grid offsets reduced together
-constexpr long long kWaitPolls = 1LL << 25;   // bounded dependency wait (~seconds)
+constexpr long long kWaitPolls = 1LL << 25;   // default bound of a dependency wait (~seconds)
 constexpr int kCB = 384;                      // cluster reduction buffer length
 constexpr int kGRows = kMaxDof + 3;           // Gauss-Newton chunk rows: g[12], 1, t', q
 
@@ -54,6 +54,12 @@ struct SearchCfg {
   int inc_int;  // the grid step when it is a whole number of voxels, else 0
   double inc;
   double rigid[3];
+  // the search's stages: coarse_random, random_global's translations
+  // (rand_off, (2 num_inc + 1)^3 x 3 offsets from the estimate, in draw
+  // order) in place of the grid; refine_nm, Nelder-Mead in place of
+  // Gauss-Newton
+  int coarse_random, refine_nm;
+  const double *rand_off;
   // subvolume pre-check: searched only when at least min_count reference
   // samples lie in [gmin, gmax]
   int thresh_on;
@@ -107,6 +113,9 @@ struct SearchArgs {
   int *pend;
   const int *succ_off, *succ;
   int *queue, *queue_tail;
+  // polls before a dependency wait (a neighbour's done flag, a ready-queue
+  // slot) gives up and records DVC_E_TIMEOUT
+  long long wait_polls;
   unsigned long long *counters;  // [0] evaluations, [1] GN iterations, [2] undefined evals,
                                  // [3] sample evaluations of the integral grid that took the
                                  // general path, [4 + k] SM cycles of phase k summed over
@@ -153,6 +162,8 @@ struct CtaState {
   float fu[3];
   float M[9], R[9], N[27];  // (I+S)R - I, R, (I+S) dR/dangle
   int use_rot, fail, stop, best;
+  int nm_act;    // Nelder-Mead: the next step (thread 0's decision)
+  int tma_dead;  // a staging copy did not land in time: this CTA stages no more
   int lrange;                  // lpmn/lpmx hold the last evaluation's positions of this CTA
   double lpmn[3], lpmx[3];
   int pi[3], qi[3];            // point - reference box origin, point + seed - correlate box
@@ -398,7 +409,7 @@ __device__ bool point_seed(const SearchArgs &a, const SearchCfg &K, PointHeader 
       long long polls = 0;
       volatile int *flag = a.done + m;
       while (*flag == 0) {
-        if (++polls > kWaitPolls) {
+        if (++polls > a.wait_polls) {
           fail = 1;
           break;
         }
@@ -749,6 +760,25 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
   return false;
 }
 
+// Every thread of the block waits for the staging copy on barrier `bar`. A
+// thread whose wait gives up marks the CTA (tma_dead) and records
+// DVC_E_TIMEOUT; after the block barrier every thread sees the mark, so the
+// evaluation path chosen from the region stays block-uniform: a dead CTA
+// evaluates from global memory and starts no further copies (a late copy
+// could land on a later one). The phase of a copy that never landed is not
+// flipped, so the exit can wait for it once more. Block-uniform call sites.
+__device__ __forceinline__ bool stage_wait(const SearchArgs &a, CtaState &S, uint32_t bar,
+                                           uint32_t &phase) {
+  if (!mbar_wait(bar, phase)) {
+    S.tma_dead = 1;
+    atomicExch(a.error_flag, DVC_E_TIMEOUT);
+  }
+  __syncthreads();
+  if (S.tma_dead) return false;
+  phase ^= 1u;
+  return true;
+}
+
 // Staged region covering positions [pmin, pmax] (global voxel coordinates)
 // with the stencil margin; ok = 0 when it does not fit the staging box.
 __device__ __forceinline__ Region make_region_box(int on, const int box[3], const double pmin[3],
@@ -1085,12 +1115,26 @@ __device__ __forceinline__ void grid_chunk_groups(
   }
 }
 
+// Offset of coarse-stage translation o along axis d from the current
+// estimate: the grid's (o in z, y, x loop order, steps of inc) or
+// random_global's o-th draw.
+__device__ __forceinline__ double coarse_off(const SearchCfg &K, int o, int d, int side, int k,
+                                             double inc) {
+  if (K.coarse_random) return K.rand_off[(size_t)o * 3 + d];
+  const int off = d == 0 ? o % side - k : (d == 1 ? (o / side) % side - k : o / (side * side) - k);
+  return __dmul_rn((double)off, inc);
+}
+
 // Keep the staged region when it covers positions [pmn, pmx] with the stencil
 // margin; otherwise stage a new one into the same buffer. One thread; returns
 // 1 when a copy was started (the block then waits for it).
 __device__ __forceinline__ int restage(const SearchArgs &a, CtaState &S, const double pmn[3],
                                        const double pmx[3], int esize, const CUtensorMap *tm,
                                        uint32_t buf, uint32_t bar, uint32_t tx) {
+  if (S.tma_dead) {
+    S.reg[0].ok = 0;
+    return 0;
+  }
   const Region cur = S.reg[0];
   if (cur.ok) {
     bool in = true;
@@ -1202,6 +1246,11 @@ __device__ __forceinline__ void range_check(Cl &cl, const int *s_ip, const float
 // 7 sample evaluation and G'G chunks, 8 block and cluster reductions,
 // 9 objective, assembly, solve and update, 10 G'G accumulation (inside 7).
 constexpr int kPhases = 11;
+// counters[]: 0..3 as listed in SearchArgs, 4 + k phase k's cycles, then the
+// Gauss-Newton systems solved by the FP64 factorisation
+constexpr int kCounterFp64Solves = 16;
+constexpr int kNumCounters = kCounterFp64Solves + 1;
+static_assert(4 + kPhases <= kCounterFp64Solves, "counter layout");
 struct PhaseClock {
   long long acc[kPhases] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   long long prev = 0;
@@ -1256,6 +1305,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t buf_addr[2] = {smem_addr(stage_buf[0]), smem_addr(stage_buf[1])};
   uint32_t phase[2] = {0u, 0u};
   if (tid == 0) {
+    S.tma_dead = 0;
     mbar_init(bar_addr[0]);
     mbar_init(bar_addr[1]);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1286,7 +1336,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           volatile int *slot = a.queue + h;
           long long polls = 0;
           int n;
-          while ((n = *slot) < 0 && ++polls <= kWaitPolls) __nanosleep(256);
+          while ((n = *slot) < 0 && ++polls <= a.wait_polls) __nanosleep(256);
           if (n < 0) {
             atomicExch(a.error_flag, DVC_E_TIMEOUT);
             H.flag = 1;
@@ -1410,18 +1460,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     // buffer that later holds the correlate region (same box)
     if (K.stage_on) {
       if (tid == 0) {
-        const Region r = make_region_box(1, K.stage_ref, S.lbmn, S.lbmx, esize);
+        const Region r = make_region_box(!S.tma_dead, K.stage_ref, S.lbmn, S.lbmx, esize);
         S.reg[0] = r;
         if (r.ok) tma_load_3d(tmp_ref, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], K.stage_ref_tx);
       }
       __syncthreads();
-      if (S.reg[0].ok) {
-        if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
-        phase[0] ^= 1u;
-      }
+      if (S.reg[0].ok) stage_wait(a, S, bar_addr[0], phase[0]);
     }
     {
-      const Region rr = S.reg[0];
+      Region rr = S.reg[0];
+      if (S.tma_dead) rr.ok = 0;
       const bool rstaged = K.stage_on && rr.ok;
       const int Br[3] = {K.stage_ref[0], K.stage_ref[1], K.stage_ref[2]};
       const SSrc<VT> ssr{buf_addr[0], rr.r0[0], rr.r0[1], rr.r0[2], Br[0], Br[1]};
@@ -1521,6 +1569,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     // trgrid_global (Core/Search.cpp:934-1043): (2k+1)^3 translations; the
     // first strictly smaller objective in z, y, x loop order wins. Any
     // translation whose sample box leaves the active box fails the point.
+    // random_global (:1045-1098) is the same over its drawn translations
+    // (the general evaluation path: their steps are not whole voxels).
     // The correlate region of each translation is staged by TMA into one of
     // two buffers while the previous translation is evaluated.
     if (K.do_grid && a.seed_mode != DVC_SEED_PARAMS) {
@@ -1532,9 +1582,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       {
         int bad = 0;
         for (int o = tid; o < total; o += kThreads) {
-          const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
           for (int d = 0; d < 3; d++) {
-            const double pc = __dadd_rn(S.par[d], __dmul_rn((double)off[d], inc));
+            const double pc = __dadd_rn(S.par[d], coarse_off(K, o, d, side, k, inc));
             if (!(__dadd_rn(S.sbmn[d], pc) >= S.H.act_cor.mn[d]) ||
                 !(__dadd_rn(S.sbmx[d], pc) <= S.H.act_cor.mx[d]))
               bad = 1;
@@ -1550,7 +1599,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // translation, or (slab boxes) under the translations of one z offset,
       // restaged per chunk of side^2 translations (z-major order, so the
       // first strict minimum is the same)
-      const bool slab = K.stage_slab != 0;
+      const bool slab = K.stage_slab != 0 && !K.coarse_random;
       const int chunk = slab ? side * side : kGridChunk;
       const int lane = tid & 31, warp = tid >> 5;
       for (int o0 = 0; o0 < total; o0 += chunk) {
@@ -1565,30 +1614,29 @@ __global__ void __launch_bounds__(kThreads, 1)
               pmx[d] = S.lbmx[d] + S.par[d] + (zs ? zo : k * inc);
             }
             Region r = make_region(K, pmn, pmx, esize);
+            if (S.tma_dead) r.ok = 0;
             S.reg[0] = r;
             if (r.ok) tma_load_3d(tmp, buf_addr[0], bar_addr[0], r.r0[0], r.r0[1], r.r0[2], stage_tx);
           }
           __syncthreads();
-          if (S.reg[0].ok) {
-            if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
-            phase[0] ^= 1u;
-          }
+          if (S.reg[0].ok) stage_wait(a, S, bar_addr[0], phase[0]);
         }
-        const Region rg = S.reg[0];
+        Region rg = S.reg[0];
+        if (S.tma_dead) rg.ok = 0;
         const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
         if (tid < nch) {
           const int o = o0 + tid;
-          const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
           for (int d = 0; d < 3; d++) {
-            const double pc = __dadd_rn(S.par[d], __dmul_rn((double)off[d], inc));
+            const double pc = __dadd_rn(S.par[d], coarse_off(K, o, d, side, k, inc));
             split_d(__dsub_rn(pc, S.H.seed[d]), S.giu[tid][d], S.gfu[tid][d]);
           }
         }
         __syncthreads();
-        if (IT != 0 && rg.ok && K.inc_int > 0 && grid_groups) {
+        const bool integral = K.inc_int > 0 && !K.coarse_random;
+        if (IT != 0 && rg.ok && integral && grid_groups) {
           grid_chunk_groups<VT, IT>(S, s_ip, s_fp, s_r, nl, grid_rec, grid_rec, ss, rg.r0, B, gsc, Gcor, o0, nch,
                                     side, k, cl.parity, sad, n_undef, n_slow);
-        } else if (IT != 0 && rg.ok && K.inc_int > 0) {
+        } else if (IT != 0 && rg.ok && integral) {
           grid_chunk_lanes<VT, IT>(a, S, s_ip, s_fp, s_r, nl, s_G, ss, rg.r0, B, gsc, Gcor, o0, nch,
                                    side, k, cl.parity, sad, n_undef, n_slow);
         } else {
@@ -1654,13 +1702,109 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       if (tid == 0 && S.best >= 0) {
         const int o = S.best;
-        const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
-        for (int d = 0; d < 3; d++) S.par[d] += (double)off[d] * inc;
+        if (K.coarse_random) {
+          for (int d = 0; d < 3; d++) S.par[d] = __dadd_rn(S.par[d], K.rand_off[(size_t)o * 3 + d]);
+        } else {
+          const int off[3] = {o % side - k, (o / side) % side - k, o / (side * side) - k};
+          for (int d = 0; d < 3; d++) S.par[d] += (double)off[d] * inc;
+        }
       }
       __syncthreads();
     } else if (tid == 0) {
       S.reg[0].ok = 0;
     }
+
+    // ------------------------------------------- objective at S.par ---
+    // obj_val_at(x) (Core/Search.cpp:448-488) at the parameters in S.par
+    // (thread 0 sets them before the call): warp, range check (false: the
+    // cloud left the active box, S.fail = 1), staging, the samples' values
+    // (s_t) and the objective by explicit residuals, the reference's own
+    // two-pass formulation (S.obj). reuse: s_t and their sum (S.red[0]) are
+    // already those of these parameters (the last Gauss-Newton evaluation:
+    // the same values summed in the same order), and its range check passed.
+    {
+    auto objective_at_par = [&](bool reuse) -> bool {
+      if (reuse) {
+        n_undef += und_last;
+      } else {
+        if (tid == 0) {
+          warp_matrices(S.par, ndof, S);
+          for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), S.iu[d], S.fu[d]);
+        }
+        __syncthreads();
+        const bool rot = S.use_rot;
+        double pmn[3], pmx[3];
+        range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
+        if (S.fail) return false;
+        if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, tmp, buf_addr[0], bar_addr[0], stage_tx);
+        __syncthreads();
+        if (S.stop) stage_wait(a, S, bar_addr[0], phase[0]);
+        Region rg = S.reg[0];
+        if (S.tma_dead) rg.ok = 0;
+        const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
+        {
+          KSum v[1];
+          for (int i = tid; i < nl; i += kThreads) {
+            int c[3];
+            float f[3], g[3];
+            sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
+            clamp_cell(c, K.bext);
+            bool und;
+            const float t = (rg.ok ? eval_sample_t<VT, IT, false, true>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)
+                                   : eval_sample_t<VT, IT, false, false>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)) -
+                            S.shift;
+            n_undef += und;
+            s_t[i] = t;
+            v[0].add(t);
+          }
+          cta_sum_comp<1>(v, S, S.cbuf[cl.parity]);
+          cluster_reduce(cl, S, 1, 0);
+        }
+      }
+      {
+        const float tm = (float)(S.red[0] / nsub);
+        {
+          KSum v[2];
+          for (int i = tid; i < nl; i += kThreads) {
+            const float t = s_t[i];
+            v[0].add((t - tm) * (t - tm));
+            v[1].add(t * t);
+          }
+          cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
+          cluster_reduce(cl, S, 2, 0);
+        }
+        const float inv_sig = rsqrtf((float)S.red[0]);
+        const float inv_T = rsqrtf((float)S.red[1]);
+        {
+          KSum v[2];
+          for (int i = tid; i < nl; i += kThreads) {
+            const float t = s_t[i], q = s_r[i];
+            float e;
+            switch (fcn) {
+              case DVC_SAD:
+              case DVC_SSD: e = t - q; break;
+              case DVC_ZSSD: e = (t - tm) - q; break;
+              case DVC_NSSD: e = t * inv_T - q; break;
+              default: e = (t - tm) * inv_sig - q; break;
+            }
+            v[0].add(e * e);
+            v[1].add(fabsf(e));
+          }
+          cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
+          cluster_reduce(cl, S, 2, 0);
+        }
+        if (tid == 0) {
+          double obj = S.red[0];
+          if (fcn == DVC_SAD) obj = S.red[1];
+          if (fcn == DVC_NSSD) obj /= 2.0;
+          if (fcn == DVC_ZNSSD) obj /= 4.0;
+          S.obj = obj;
+        }
+        __syncthreads();
+      }
+      return true;
+    };
+    bool have_obj = false;  // S.obj holds the objective at the final parameters
 
     pc.to(3);
     // ------------------------------------------------- Gauss-Newton ---
@@ -1679,7 +1823,147 @@ __global__ void __launch_bounds__(kThreads, 1)
     // samples pass through shared memory, one thread per matrix entry.
     gn_last = false;  // the last Gauss-Newton evaluation was at the final parameters
     und_last = 0;
-    {
+    if (K.refine_nm) {
+      // ----------------------------------------------- Nelder-Mead ---
+      // look_with(amoeba, ndof, ftol) (Core/Search.cpp:379-440) with
+      // min_Nelder_Mead (:680-932): simplex steps 0.2 in every parameter,
+      // ftol 1e-5 for 3 dof and 1e-7 otherwise; reflection 1, expansion 2,
+      // contraction -0.5 (kept only when it beats the best vertex, as the
+      // reference has it), shrink 0.5 towards the best vertex; Convg_Fail
+      // after 2000 evaluations; an evaluation outside the active box fails
+      // the point. The simplex logic runs on thread 0 of every CTA in FP64
+      // (the objectives are cluster totals, so all CTAs decide alike); each
+      // objective is evaluated by the whole cluster. The simplex lives in the
+      // Gauss-Newton chunk rows, which this mode leaves unused.
+      double *nm = reinterpret_cast<double *>(s_G);  // [13][12] vertices
+      double *nmv = nm + 13 * kMaxDof;              // [13] their objectives
+      double *xref = nmv + 13;                       // [12] the reflected vertex
+      const int nvrt = ndof + 1;
+      const double tol = ndof == 3 ? 1e-5 : 1e-7;
+      int nfunc = 0;
+      int wrst = 0, best = 0, poor = 0;  // thread 0's
+      double cen[kMaxDof], del[kMaxDof], yref = 0.0;
+      if (tid == 0)
+        for (int i = 0; i < nvrt; i++)
+          for (int j = 0; j < ndof; j++)
+            nm[i * kMaxDof + j] = (i > 0 && j == i - 1) ? __dadd_rn(S.par[j], 0.2) : S.par[j];
+      for (int i = 0; i < nvrt; i++) {
+        if (tid == 0)
+          for (int j = 0; j < ndof; j++) S.par[j] = nm[i * kMaxDof + j];
+        n_eval += 1;
+        if (!objective_at_par(false)) goto point_done;
+        if (tid == 0) nmv[i] = S.obj;
+      }
+      nfunc = nvrt;
+      for (;;) {
+        if (tid == 0) {
+          wrst = 0;
+          best = 0;
+          for (int i = 1; i < nvrt; i++) {
+            if (nmv[i] > nmv[wrst]) wrst = i;
+            if (nmv[i] < nmv[best]) best = i;
+          }
+          poor = best;
+          for (int i = 0; i < nvrt; i++)
+            if (i != wrst && i != best && nmv[i] > nmv[poor]) poor = i;
+          S.best = best;
+          const double rel = __ddiv_rn(2.0 * fabs(nmv[wrst] - nmv[best]),
+                                       fabs(nmv[wrst]) + fabs(nmv[best]) + 1.0e-10);
+          if (rel < tol) {
+            S.nm_act = 1;  // converged
+          } else if (nfunc > 2000) {
+            S.nm_act = 2;  // Convg_Fail
+          } else {
+            S.nm_act = 0;
+            for (int j = 0; j < ndof; j++) {
+              double c = 0.0;
+              for (int i = 0; i < nvrt; i++)
+                if (i != wrst) c = __dadd_rn(c, nm[i * kMaxDof + j]);
+              c = __ddiv_rn(c, (double)ndof);
+              cen[j] = c;
+              del[j] = __dsub_rn(c, nm[wrst * kMaxDof + j]);
+              xref[j] = __dadd_rn(c, del[j]);
+              S.par[j] = xref[j];
+            }
+          }
+        }
+        __syncthreads();
+        if (S.nm_act == 1) break;
+        if (S.nm_act == 2) {
+          if (tid == 0) S.fail = 2;
+          __syncthreads();
+          goto point_done;
+        }
+        n_eval += 1;
+        if (!objective_at_par(false)) goto point_done;
+        nfunc += 1;
+        if (tid == 0) {
+          yref = S.obj;
+          if (yref <= nmv[poor] && yref >= nmv[best]) {  // keep the reflection
+            for (int j = 0; j < ndof; j++) nm[wrst * kMaxDof + j] = xref[j];
+            nmv[wrst] = yref;
+            S.nm_act = 0;
+          } else if (yref < nmv[best]) {  // try the expansion
+            for (int j = 0; j < ndof; j++) S.par[j] = __dadd_rn(cen[j], __dmul_rn(2.0, del[j]));
+            S.nm_act = 3;
+          } else {  // the contraction
+            for (int j = 0; j < ndof; j++) S.par[j] = __dadd_rn(cen[j], __dmul_rn(-0.5, del[j]));
+            S.nm_act = 4;
+          }
+        }
+        __syncthreads();
+        if (S.nm_act == 0) continue;
+        n_eval += 1;
+        if (!objective_at_par(false)) goto point_done;
+        nfunc += 1;
+        if (tid == 0) {
+          const double y = S.obj;
+          if (S.nm_act == 3) {  // the expansion if better than the best, else the reflection
+            const bool e = y < nmv[best];
+            for (int j = 0; j < ndof; j++) nm[wrst * kMaxDof + j] = e ? S.par[j] : xref[j];
+            nmv[wrst] = e ? y : yref;
+            S.nm_act = 0;
+          } else if (y < nmv[best]) {  // the contraction beats the best vertex
+            for (int j = 0; j < ndof; j++) nm[wrst * kMaxDof + j] = S.par[j];
+            nmv[wrst] = y;
+            S.nm_act = 0;
+          } else {
+            S.nm_act = 5;  // shrink towards the best vertex
+          }
+        }
+        __syncthreads();
+        if (S.nm_act == 0) continue;
+        for (int i = 0; i < nvrt; i++) {
+          if (i == S.best) continue;
+          if (tid == 0) {
+            const int b = S.best;
+            for (int j = 0; j < ndof; j++) {
+              const double v = __dadd_rn(nm[b * kMaxDof + j],
+                                         __dmul_rn(0.5, __dsub_rn(nm[i * kMaxDof + j], nm[b * kMaxDof + j])));
+              nm[i * kMaxDof + j] = v;
+              S.par[j] = v;
+            }
+          }
+          n_eval += 1;
+          if (!objective_at_par(false)) goto point_done;
+          nfunc += 1;
+          if (tid == 0) nmv[i] = S.obj;
+        }
+      }
+      // the best vertex; its objective is the final one (obj_val_at there
+      // evaluates the same values again)
+      if (tid == 0) {
+        const int b = S.best;
+        for (int j = 0; j < ndof; j++) S.par[j] = nm[b * kMaxDof + j];
+        S.obj = nmv[b];
+        if (cl.rank == 0) {
+          if (a.gn_iters) a.gn_iters[S.H.n] = nfunc;
+          atomicAdd(a.counters + 1, (unsigned long long)nfunc);
+        }
+      }
+      __syncthreads();
+      have_obj = true;
+    } else {
       int it_done = 20;
       unsigned long long und_it = 0;
       const int ntri = ndof * (ndof + 1) / 2;
@@ -1753,11 +2037,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           S.lrange = 0;
         }
         __syncthreads();
-        const Region rg = S.reg[0];
-        if (S.stop) {
-          if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
-          phase[0] ^= 1u;
-        }
+        if (S.stop) stage_wait(a, S, bar_addr[0], phase[0]);
+        Region rg = S.reg[0];
+        if (S.tma_dead) rg.ok = 0;
         const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
         pc.to(7);
 
@@ -1990,7 +2272,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (tid < 32) {
           if (!warp_solve_chol(S, ndof)) {
             warp_qr_solve(S, ndof);
-            if (tid == 0) atomicAdd(a.counters + 16, 1ull);
+            if (tid == 0) atomicAdd(a.counters + kCounterFp64Solves, 1ull);
           }
           if (tid < ndof) S.par[tid] += S.x[tid];
           if (tid < 3) S.upd[tid] = S.x[tid];
@@ -2007,99 +2289,19 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     pc.to(4);
     // ------------------------------------------------ final objective ---
-    // obj_val_at(par_min) (Core/Search.cpp:187): explicit residuals over the
-    // stored values, the reference's own two-pass formulation
-    // When Gauss-Newton stopped by its rule, the final parameters are those
-    // of its last evaluation: the sample values stored then (s_t) and their
-    // sum (S.red[0], the same values summed in the same order) are exactly
-    // what this evaluation would compute, and the range check passed.
-    n_eval += 1;
-    if (gn_last) {
-      n_undef += und_last;
-    } else {
-      if (tid == 0) {
-        warp_matrices(S.par, ndof, S);
-        for (int d = 0; d < 3; d++) split_d(__dsub_rn(S.par[d], S.H.seed[d]), S.iu[d], S.fu[d]);
-      }
-      __syncthreads();
-      const bool rot = S.use_rot;
-      double pmn[3], pmx[3];
-      range_check(cl, s_ip, s_fp, nl, S, rot, pmn, pmx);
-      if (S.fail) goto point_done;
-      if (tid == 0) S.stop = restage(a, S, pmn, pmx, esize, tmp, buf_addr[0], bar_addr[0], stage_tx);
-      __syncthreads();
-      const Region rg = S.reg[0];
-      if (S.stop) {
-        if (!mbar_wait(bar_addr[0], phase[0])) atomicExch(a.error_flag, DVC_E_TIMEOUT);
-        phase[0] ^= 1u;
-      }
-      const SSrc<VT> ss{buf_addr[0], rg.r0[0], rg.r0[1], rg.r0[2], B[0], B[1]};
-      {
-        KSum v[1];
-        for (int i = tid; i < nl; i += kThreads) {
-          int c[3];
-          float f[3], g[3];
-          sample_pos(s_ip, s_fp, i, S, S.iu, S.fu, rot, c, f);
-          clamp_cell(c, K.bext);
-          bool und;
-          const float t = (rg.ok ? eval_sample_t<VT, IT, false, true>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)
-                                 : eval_sample_t<VT, IT, false, false>(ss, rg.r0, B, gsc, Gcor, c, f, g, und)) -
-                          S.shift;
-          n_undef += und;
-          s_t[i] = t;
-          v[0].add(t);
-        }
-        cta_sum_comp<1>(v, S, S.cbuf[cl.parity]);
-        cluster_reduce(cl, S, 1, 0);
-      }
+    // obj_val_at(par_min) (Core/Search.cpp:187); after Gauss-Newton stopped
+    // by its rule the final parameters are those of its last evaluation
+    if (!have_obj) {
+      n_eval += 1;
+      if (!objective_at_par(gn_last)) goto point_done;
     }
-    {
-      const float tm = (float)(S.red[0] / nsub);
-      {
-        KSum v[2];
-        for (int i = tid; i < nl; i += kThreads) {
-          const float t = s_t[i];
-          v[0].add((t - tm) * (t - tm));
-          v[1].add(t * t);
-        }
-        cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
-        cluster_reduce(cl, S, 2, 0);
-      }
-      const float inv_sig = rsqrtf((float)S.red[0]);
-      const float inv_T = rsqrtf((float)S.red[1]);
-      {
-        KSum v[2];
-        for (int i = tid; i < nl; i += kThreads) {
-          const float t = s_t[i], q = s_r[i];
-          float e;
-          switch (fcn) {
-            case DVC_SAD:
-            case DVC_SSD: e = t - q; break;
-            case DVC_ZSSD: e = (t - tm) - q; break;
-            case DVC_NSSD: e = t * inv_T - q; break;
-            default: e = (t - tm) * inv_sig - q; break;
-          }
-          v[0].add(e * e);
-          v[1].add(fabsf(e));
-        }
-        cta_sum_comp<2>(v, S, S.cbuf[cl.parity]);
-        cluster_reduce(cl, S, 2, 0);
-      }
-      if (tid == 0) {
-        double obj = S.red[0];
-        if (fcn == DVC_SAD) obj = S.red[1];
-        if (fcn == DVC_NSSD) obj /= 2.0;
-        if (fcn == DVC_ZNSSD) obj /= 4.0;
-        S.obj = obj;
-      }
-      __syncthreads();
     }
 
   point_done:
     if (cl.rank == 0 && tid == 0) {
       const int n = S.H.n;
       if (S.fail) {
-        a.status[n] = S.fail == 3 ? DVC_NOT_SEARCH : DVC_RANGE_FAIL;
+        a.status[n] = S.fail == 3 ? DVC_NOT_SEARCH : (S.fail == 2 ? DVC_CONVG_FAIL : DVC_RANGE_FAIL);
         a.objmin[n] = 0.0;
         for (int p = 0; p < 12; p++) a.params[(size_t)n * 12 + p] = 0.0;
       } else {
@@ -2128,6 +2330,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     pc.to(0);
   }
   pc.flush(a.counters);
+  // a copy that did not land in time: one more bounded wait before the
+  // shared memory it writes is released
+  if (S.tma_dead && tid == 0) mbar_wait(bar_addr[0], phase[0]);
   // no CTA leaves while another may still read its shared memory
   cl.g.sync();
 }

@@ -209,11 +209,17 @@ int main(int argc, char *argv[]) {
   std::cout.unsetf(std::ios::floatfield);
 
   const long long t_finish = (long long)std::time(nullptr);
+  // rows in processing order from the stored results, as the reference's final
+  // rewrite (Core/dvc.cpp:314-320): a failed point keeps its initial objmin 0
+  // and zero displacements
   write_disp_header(run.res_fname);
+  write_par_header(run.par_fname, run.num_srch_dof);
   for (int i = 0; i < N; i++) {
     const int m = order[(size_t)i];
     append_disp_row(run.res_fname, labels[(size_t)m], &pts[(size_t)m * 3], status[(size_t)m],
                     objmin[(size_t)m], &par[(size_t)m * 12]);
+    append_par_row(run.par_fname, labels[(size_t)m], &pts[(size_t)m * 3], status[(size_t)m],
+                   objmin[(size_t)m], &par[(size_t)m * 12], run.num_srch_dof);
   }
   write_stat_echo(run, (size_t)n, bmin, bmax, kVersion);
   append_stat_time(run.sta_fname, "Run start:\t", t_start);

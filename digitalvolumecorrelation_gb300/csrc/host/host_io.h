@@ -21,6 +21,7 @@ namespace dvchost {
 // Settings of one run (the reference's RunControl, Core/Utility.h:90-134).
 struct RunConfig {
   std::string ref_fname, cor_fname, pts_fname, out_fname, res_fname, sta_fname;
+  std::string par_fname;  // <output_filename>.par: every search parameter (no reference counterpart)
   unsigned long ref_bytes = 0, cor_bytes = 0;  // file sizes found while checking the names
   int vol_bit_depth = 8;
   std::string vol_endian = "little";
@@ -88,6 +89,14 @@ void write_manual(std::ostream &os);
 void write_disp_header(const std::string &fname);
 void append_disp_row(const std::string &fname, int label, const double pt[3], int status,
                      double objmin, const double uvw[3]);
+// `.par` (no reference counterpart; the reference's .disp keeps u, v, w
+// only, Core/InputRead.cpp:1133-1196): the .disp columns label, x, y, z,
+// status, objmin, then all num_srch_dof parameters (u v w phi the psi exx
+// eyy ezz exy eyz exz) in scientific notation with 9 decimals, so the
+// rotations and strains of 6- and 12-dof searches are kept.
+void write_par_header(const std::string &fname, int ndof);
+void append_par_row(const std::string &fname, int label, const double pt[3], int status,
+                    double objmin, const double *par, int ndof);
 // `.stat`: the input echo (truncates the file), a time stamp line, run totals
 void write_stat_echo(const RunConfig &run, size_t n_points, const double bmin[3],
                      const double bmax[3], const char *version);

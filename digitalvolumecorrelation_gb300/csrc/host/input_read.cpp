@@ -276,6 +276,7 @@ bool InputFile::read(RunConfig &r) {
   if (new_file("output_filename", r.out_fname) != kOk) return false;
   r.res_fname = r.out_fname + ".disp";
   r.sta_fname = r.out_fname + ".stat";
+  r.par_fname = r.out_fname + ".par";
 
   if (int_in("vol_bit_depth", {8, 16}, r.vol_bit_depth) != kOk) return false;
   if (r.vol_bit_depth != 8 && str_in("vol_endian", {"little", "big"}, r.vol_endian) != kOk) return false;
@@ -425,7 +426,9 @@ void write_manual(std::ostream &os) {
      << "                           -1 = range fail (the search left the disp_max range),\n"
      << "                           -2 = convergence fail; u v w = target - reference position\n"
      << "   <output_filename>.stat  echo of the input, the point cloud, run times and totals\n"
-     << "   <point_cloud_filename>.sort.csv  the 75 nearest points of every point (for strain)\n\n";
+     << "   <point_cloud_filename>.sort.csv  the 75 nearest points of every point (for strain)\n"
+     << "   <output_filename>.par   the .disp columns with every search parameter: u v w, and\n"
+     << "                           phi the psi (6 dof), exx eyy ezz exy eyz exz (12 dof)\n\n";
 }
 
 void write_disp_header(const std::string &fname) {
@@ -439,6 +442,23 @@ void append_disp_row(const std::string &fname, int label, const double pt[3], in
   f << label << "\t" << pt[0] << "\t" << pt[1] << "\t" << pt[2] << "\t" << status << "\t" << objmin;
   f << std::fixed << std::setprecision(6);
   for (int i = 0; i < 3; i++) f << "\t" << uvw[i];
+  f << "\n";
+}
+
+void write_par_header(const std::string &fname, int ndof) {
+  static const char *names[12] = {"u", "v", "w", "phi", "the", "psi", "exx", "eyy", "ezz", "exy", "eyz", "exz"};
+  std::ofstream f(fname.c_str(), std::ios_base::out);
+  f << "n\tx\ty\tz\tstatus\tobjmin";
+  for (int i = 0; i < ndof; i++) f << "\t" << names[i];
+  f << "\n";
+}
+
+void append_par_row(const std::string &fname, int label, const double pt[3], int status,
+                    double objmin, const double *par, int ndof) {
+  std::ofstream f(fname.c_str(), std::ios_base::out | std::ios_base::app);
+  f << label << "\t" << pt[0] << "\t" << pt[1] << "\t" << pt[2] << "\t" << status << "\t" << objmin;
+  f << std::scientific << std::setprecision(9);
+  for (int i = 0; i < ndof; i++) f << "\t" << par[i];
   f << "\n";
 }
 

@@ -58,6 +58,8 @@ def load(path: str | None = None):
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.dvc_gpu_last_counters.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
     L.dvc_gpu_last_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+    L.dvc_gpu_last_status.argtypes = [C.c_void_p]
+    L.dvc_gpu_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
     L.dvc_gpu_interpolate.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
     L.dvc_gpu_objective.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp]
     L.dvc_gpu_strain.argtypes = [C.c_int, _dp, _ip, _dp, _dp, C.c_int, _ip, C.c_int, C.c_double,
@@ -218,6 +220,15 @@ class Engine:
         out = (C.c_longlong * 3)()
         _check(_lib.dvc_gpu_last_counters(self._h, out))
         return tuple(int(v) for v in out)
+
+    def last_status(self):
+        """Device-side outcome of the most recent search launch
+        (dvc_gpu_last_status): OK, or the DVC_E_* code it recorded."""
+        return int(_lib.dvc_gpu_last_status(self._h))
+
+    def set_wait_limit(self, polls):
+        """Polls before a dependency wait of the search gives up (< 0: default)."""
+        _check(_lib.dvc_gpu_set_wait_limit(self._h, int(polls)))
 
     def last_phase_cycles(self):
         """SM cycles of the most recent search per phase, summed over CTAs:

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define DVC_ABI_VERSION 2
+#define DVC_ABI_VERSION 3
 
 /* per-point status, identical to Core/Utility.h:38-41 */
 #define DVC_POINT_GOOD 0
@@ -66,6 +66,16 @@ enum dvc_seed_mode {
   DVC_SEED_PARAMS = 3
 };
 
+/* The search's coarse stage and refinement. The reference's process_point
+   runs trgrid_global then min_Lev_Mar (Core/Search.cpp:132,141); its source
+   also holds two alternatives that no input key selects: random_global
+   (:1045-1098; as many random translations as the grid has points, from a
+   clock-seeded rand(), each component uniform in [-disp_max, disp_max))
+   and Nelder-Mead through look_with(amoeba, ...) (:150-181, 379-440,
+   680-932; Convg_Fail after 2000 evaluations). Here they are opt-in. */
+enum dvc_coarse { DVC_COARSE_GRID = 0, DVC_COARSE_RANDOM = 1 };
+enum dvc_refine { DVC_REFINE_GAUSS_NEWTON = 0, DVC_REFINE_NELDER_MEAD = 1 };
+
 /* Search configuration: the `dvc` input-file keys that shape the hot path
    (Core/Utility.h:90-134 RunControl; limits Core/InputRead.cpp:519-631). */
 typedef struct dvc_params {
@@ -94,6 +104,12 @@ typedef struct dvc_params {
   int subvol_thresh;
   double gray_thresh_min, gray_thresh_max; /* 0 <= min < max <= 2^(8*bytes_per_voxel) */
   double min_vol_fract;                    /* 0..1 */
+  /* search stages (no input key in the reference; 0 = its defaults) */
+  int coarse_method;          /* dvc_coarse: with basin_radius > 0, the grid or
+                                 random_global's translations                */
+  int refine_method;          /* dvc_refine: Gauss-Newton or Nelder-Mead     */
+  unsigned int coarse_seed;   /* srand() seed of random_global's draws (the
+                                 reference uses the clock, time(NULL))        */
 } dvc_params;
 
 /* Run statistics returned by dvc_gpu_process. */
@@ -156,11 +172,34 @@ int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_pro
 /* Same as dvc_gpu_process with every array already in device memory
    (points, order, neigh, seeds; outputs status, objmin, params, gn_iters).
    Enqueued on `stream` (cudaStream_t, may be NULL); returns once enqueued;
-   stats are not filled. */
+   stats are not filled. Errors found on the device (a bounded wait that gave
+   up) are read afterwards with dvc_gpu_last_status. */
 int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev, int n_process,
                            const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
                            const double *seeds_dev, int *status_dev, double *objmin_dev,
                            double *params_dev, int *gn_iters_dev, void *stream);
+
+/* Outcome on the device of this engine's most recent search launch (any of
+   the search calls, the plan calls that use this engine's workspace, and the
+   allocation-free call while no later call on any engine reused its array);
+   waits for the device first. The reference surfaces every failure as an
+   exception or a status (Core/Utility.h:76-86); a device launch cannot throw,
+   so it records the first failure in a flag that this reads:
+   DVC_OK; DVC_E_TIMEOUT when a bounded wait gave up (a neighbour's result or
+   a ready-queue slot that did not arrive within the wait limit: those points
+   are left DVC_NOT_SEARCH; or a shared-memory staging copy that did not land:
+   the CTA then evaluated from global memory, results unchanged); DVC_E_ARG
+   when a plan's point named no configuration. dvc_gpu_process and the other
+   host-array calls return the same code themselves. */
+int dvc_gpu_last_status(dvc_engine *e);
+
+/* Polls a dependency wait of this engine's searches makes before it gives up
+   (a point waiting for a neighbour's result, a cluster waiting for a
+   ready-queue slot): polls >= 0 sets the bound, a negative value restores the
+   default (2^25 polls, about 4 s per wait). The reference waits on nothing
+   (one host thread runs the points in order); the bound keeps every device
+   wait finite, and a small one lets a test make a wait run out. */
+int dvc_gpu_set_wait_limit(dvc_engine *e, long long polls);
 
 /* ---- volume files -------------------------------------------------------
  * The reference reads the raw volume files piecewise for every point (one
@@ -205,7 +244,8 @@ int dvc_gpu_create_from_files(dvc_engine **out, const dvc_params *p, const char 
  * call before any stream capture. All calls share the one array; calls whose
  * work overlaps on the GPU race on it, so serialise them. The engine must
  * already exist (dvc_gpu_create / dvc_gpu_create_device allocate).
- * dvc_gpu_last_counters does not report these calls. */
+ * dvc_gpu_last_counters and dvc_gpu_last_status report the call until the
+ * next allocation-free call (from any engine) overwrites the array. */
 #define DVC_NOALLOC_MAX_POINTS 65536
 int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *points_dev,
                                    int n_process, const int *order_dev, int n_neigh,

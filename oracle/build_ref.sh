@@ -14,6 +14,12 @@ set -euo pipefail
 REF=${DVC_REFERENCE_DIR:-/root/reference}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
+# `build_ref.sh --where`: print the reference directory (exit 3 when absent)
+if [ "${1:-}" = "--where" ]; then
+  [ -d "$REF/Core" ] || exit 3
+  echo "$REF"
+  exit 0
+fi
 if [ ! -d "$REF/Core" ]; then
   echo "reference sources not found at $REF; oracle/_ref not built" >&2
   exit 3
@@ -30,7 +36,9 @@ $CXX $FLAGS -c "$HERE/ref_capi.cpp" -o "$OUT/obj/ref_capi.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 LIBOBJS=""
 for s in $SRCS; do LIBOBJS="$LIBOBJS $OUT/obj/$s.o"; done
-$CXX -shared -fopenmp -o "$OUT/libdvcref.so" $LIBOBJS "$OUT/obj/ref_capi.o"
+# -Bsymbolic-functions: the reference's calls bind to this library's own
+# definitions (ref_capi.cpp's time(), for random_global's clock seed)
+$CXX -shared -fopenmp -Wl,-Bsymbolic-functions -o "$OUT/libdvcref.so" $LIBOBJS "$OUT/obj/ref_capi.o"
 $CXX -fopenmp -o "$OUT/dvc" "$OUT/obj/dvc.o" $LIBOBJS
 $CXX -fopenmp -o "$OUT/strain" "$OUT/obj/strain.o" $LIBOBJS
 echo "built $OUT/libdvcref.so $OUT/dvc $OUT/strain"

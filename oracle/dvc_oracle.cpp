@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <random>
@@ -609,6 +610,21 @@ void qr_solve(int m, int n, const double *A0 /* row-major m x n */, const double
 }
 
 // ------------------------------------------------------------------ Search ---
+// random_global's translations (Core/Search.cpp:1045-1098): 3 draws per
+// translation from the C library's rand() after srand(seed), each
+// displ_max * (2 * rand()) / RAND_MAX with the doubled draw an int product
+// (wrapping as two's complement above 2^30).
+std::vector<double> random_offsets(int num_pts, double displ_max, unsigned seed) {
+  srand(seed);
+  const double dbl_rand_max = RAND_MAX;
+  std::vector<double> rel((size_t)num_pts * 3);
+  for (size_t k = 0; k < rel.size(); k++) {
+    const int twice = (int)(2u * (unsigned)rand());
+    rel[k] = displ_max * (twice / dbl_rand_max);
+  }
+  return rel;
+}
+
 struct Search {
   dvc_params p;
   Volume ref, cor;
@@ -644,6 +660,88 @@ struct Search {
   ~Search() {
     delete interp_ref;
     delete interp_cor;
+  }
+
+  // min_Nelder_Mead (Core/Search.cpp:680-932): the reference's simplex rules
+  // (reflection 1, expansion 2, contraction -0.5 towards the worst vertex,
+  // shrink 0.5 towards the best; a contraction is kept only when it beats
+  // the best vertex), its convergence test and its limit of 2000 objective
+  // evaluations (Convg_Fail). Returns the status; out = the best vertex.
+  int nelder_mead(const double *start, int ndof, double conv_tol, double *out, int &num_func) {
+    const int MAX_FUNC = 2000;
+    const double NOT_ZERO = 1.0e-10, ALPHA = 1.0, GAMMA = 2.0, DELTA = -0.5, OMEGA = 0.5;
+    const int nvrt = ndof + 1;
+    std::vector<std::vector<double>> simplex((size_t)nvrt, std::vector<double>(start, start + ndof));
+    for (int i = 1; i < nvrt; i++) simplex[(size_t)i][(size_t)i - 1] += 0.2;  // del_tra = del_rot = del_str
+    std::vector<double> val((size_t)nvrt), centroid((size_t)ndof), del((size_t)ndof), xref((size_t)ndof),
+        xexp((size_t)ndof), xcon((size_t)ndof);
+    num_func = 0;
+    for (int i = 0; i < nvrt; i++)
+      if (!obj_val_at(simplex[(size_t)i].data(), ndof, val[(size_t)i], nullptr)) return DVC_RANGE_FAIL;
+    num_func += nvrt;
+    for (;;) {
+      int wrst = 0, best = 0;
+      for (int i = 1; i < nvrt; i++) {
+        if (val[(size_t)i] > val[(size_t)wrst]) wrst = i;
+        if (val[(size_t)i] < val[(size_t)best]) best = i;
+      }
+      int poor = best;
+      for (int i = 0; i < nvrt; i++)
+        if (i != wrst && i != best && val[(size_t)i] > val[(size_t)poor]) poor = i;
+      const double rel_diff = 2.0 * std::fabs(val[(size_t)wrst] - val[(size_t)best]) /
+                              (std::fabs(val[(size_t)wrst]) + std::fabs(val[(size_t)best]) + NOT_ZERO);
+      if (rel_diff < conv_tol) {
+        for (int j = 0; j < ndof; j++) out[j] = simplex[(size_t)best][(size_t)j];
+        return DVC_POINT_GOOD;
+      }
+      if (num_func > MAX_FUNC) return DVC_CONVG_FAIL;
+      for (int j = 0; j < ndof; j++) {
+        double c = 0.0;
+        for (int i = 0; i < nvrt; i++)
+          if (i != wrst) c += simplex[(size_t)i][(size_t)j];
+        c /= ndof;
+        centroid[(size_t)j] = c;
+        del[(size_t)j] = c - simplex[(size_t)wrst][(size_t)j];
+      }
+      for (int j = 0; j < ndof; j++) xref[(size_t)j] = centroid[(size_t)j] + ALPHA * del[(size_t)j];
+      double yref, yexp, ycon;
+      if (!obj_val_at(xref.data(), ndof, yref, nullptr)) return DVC_RANGE_FAIL;
+      num_func += 1;
+      if (yref <= val[(size_t)poor] && yref >= val[(size_t)best]) {
+        simplex[(size_t)wrst] = xref;
+        val[(size_t)wrst] = yref;
+        continue;
+      }
+      if (yref < val[(size_t)best]) {
+        for (int j = 0; j < ndof; j++) xexp[(size_t)j] = centroid[(size_t)j] + GAMMA * del[(size_t)j];
+        if (!obj_val_at(xexp.data(), ndof, yexp, nullptr)) return DVC_RANGE_FAIL;
+        num_func += 1;
+        if (yexp < val[(size_t)best]) {
+          simplex[(size_t)wrst] = xexp;
+          val[(size_t)wrst] = yexp;
+        } else {
+          simplex[(size_t)wrst] = xref;
+          val[(size_t)wrst] = yref;
+        }
+        continue;
+      }
+      for (int j = 0; j < ndof; j++) xcon[(size_t)j] = centroid[(size_t)j] + DELTA * del[(size_t)j];
+      if (!obj_val_at(xcon.data(), ndof, ycon, nullptr)) return DVC_RANGE_FAIL;
+      num_func += 1;
+      if (ycon < val[(size_t)best]) {
+        simplex[(size_t)wrst] = xcon;
+        val[(size_t)wrst] = ycon;
+        continue;
+      }
+      for (int i = 0; i < nvrt; i++) {
+        if (i == best) continue;
+        for (int j = 0; j < ndof; j++)
+          simplex[(size_t)i][(size_t)j] =
+              simplex[(size_t)best][(size_t)j] + OMEGA * (simplex[(size_t)i][(size_t)j] - simplex[(size_t)best][(size_t)j]);
+        if (!obj_val_at(simplex[(size_t)i].data(), ndof, val[(size_t)i], nullptr)) return DVC_RANGE_FAIL;
+        num_func += 1;
+      }
+    }
   }
 
   // Search::obj_val_at (Core/Search.cpp:448-488); false = Range_Fail
@@ -697,6 +795,30 @@ struct Search {
     interp_cor->load(cor);
     evals++;  // the reference-subvolume interpolation counts as one evaluation
 
+    // random_global (Core/Search.cpp:1045-1098): as many random translations
+    // as the grid has points, each component displ_max * (2 rand()) /
+    // RAND_MAX from the C library's generator seeded with coarse_seed (the
+    // reference seeds it from the clock); the doubled draw is an int product
+    // that wraps for draws above 2^30 (two's complement), which spreads the
+    // components over [-displ_max, displ_max)
+    if (p.coarse_method == DVC_COARSE_RANDOM && p.basin_radius != 0.0) {
+      double displ_max = p.disp_max;
+      int num_inc = (int)(displ_max / p.basin_radius);
+      int num_pts = (2 * num_inc + 1) * (2 * num_inc + 1) * (2 * num_inc + 1);
+      std::vector<double> rel = random_offsets(num_pts, displ_max, p.coarse_seed);
+      double obj_min = std::numeric_limits<double>::max();
+      double mn[3] = {0.0, 0.0, 0.0};
+      for (int i = 0; i < num_pts; i++) {
+        double pc[3] = {par[0] + rel[(size_t)i * 3], par[1] + rel[(size_t)i * 3 + 1], par[2] + rel[(size_t)i * 3 + 2]};
+        double o;
+        if (!obj_val_at(pc, 3, o, nullptr)) return DVC_RANGE_FAIL;
+        if (o < obj_min) {
+          obj_min = o;
+          for (int d = 0; d < 3; d++) mn[d] = rel[(size_t)i * 3 + d];
+        }
+      }
+      for (int d = 0; d < 3; d++) par[d] += mn[d];
+    } else
     // trgrid_global (Core/Search.cpp:934-1043)
     if (p.basin_radius != 0.0) {
       double displ_max = p.disp_max;
@@ -723,6 +845,21 @@ struct Search {
       par[0] += (double)mnx * inc;
       par[1] += (double)mny * inc;
       par[2] += (double)mnz * inc;
+    }
+
+    if (p.refine_method == DVC_REFINE_NELDER_MEAD) {
+      // look_with(amoeba, ndof, ftol) (Core/Search.cpp:379-440): simplex
+      // steps 0.2 in every parameter; ftol 1e-5 for 3 dof, else 1e-7
+      double best[12], objf;
+      int nf = 0;
+      const int st = nelder_mead(par.data(), ndof, ndof == 3 ? 0.00001 : 0.0000001, best, nf);
+      if (iters_out) *iters_out = nf;
+      if (st != DVC_POINT_GOOD) return st;
+      // final objective (Core/Search.cpp:187)
+      if (!obj_val_at(best, ndof, objf, nullptr)) return DVC_RANGE_FAIL;
+      for (int i = 0; i < 12; i++) par_out[i] = i < ndof ? best[i] : 0.0;
+      obj_out = objf;
+      return DVC_POINT_GOOD;
     }
 
     // min_Lev_Mar(par, 1e-6, 0.01) (Core/Search.cpp:194-246) with the

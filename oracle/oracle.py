@@ -45,6 +45,13 @@ def build_reference():
     return REF_SO if r.returncode == 0 and os.path.exists(REF_SO) else None
 
 
+def reference_dir():
+    """The reference sources' directory as oracle/build_ref.sh finds it
+    (DVC_REFERENCE_DIR or the recipe's default), or None where they are absent."""
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "--where"], capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 and r.stdout.strip() else None
+
+
 def _ptr(a, t):
     return a.ctypes.data_as(t)
 
@@ -202,6 +209,24 @@ class Reference:
         self.lib.ref_process(C.byref(p), fr, fc, 0, b"little", n, _ptr(pts, _dp), n_process,
                              _ptr(order, _ip), neigh.shape[1], _ptr(neigh, _ip),
                              _ptr(status, _ip), _ptr(objmin, _dp), _ptr(par, _dp))
+        return dict(status=status, objmin=objmin, params=par)
+
+    def process_stages(self, p, ref, cor, points, order, neigh, n_process=None):
+        """process() with the search stages p.coarse_method / p.refine_method
+        (random_global with its clock fixed at p.coarse_seed; Nelder-Mead)."""
+        fr = self._file(ref, "ref.raw")
+        fc = self._file(cor, "cor.raw")
+        pts = np.ascontiguousarray(points, np.float64)
+        n = len(pts)
+        order = np.ascontiguousarray(order, np.int32)
+        neigh = np.ascontiguousarray(neigh, np.int32)
+        n_process = len(order) if n_process is None else n_process
+        status = np.zeros(n, np.int32)
+        objmin = np.zeros(n)
+        par = np.zeros((n, 12))
+        self.lib.ref_process_stages(C.byref(p), fr, fc, 0, b"little", n, _ptr(pts, _dp), n_process,
+                                    _ptr(order, _ip), neigh.shape[1], _ptr(neigh, _ip),
+                                    _ptr(status, _ip), _ptr(objmin, _dp), _ptr(par, _dp))
         return dict(status=status, objmin=objmin, params=par)
 
     def order_neighbours(self, pts, start=None):

@@ -15,7 +15,16 @@ on small seeded synthetic volumes, what the reference computes:
     (Core/tests/test_DataCloud.cpp:129-139 over Core/tests/grid_input.roi),
   * end-to-end runs of the reference's `dvc` and `strain` programs
     (input file, point cloud and raw volumes -> .disp, .stat, .sort.csv,
-    strain CSVs); `--dvc-runs` regenerates only these.
+    strain CSVs); `--dvc-runs` regenerates only these;
+  * `--range-large`: the searches of tests/golden/recipes.py (Range_Fail by
+    each route, full-size subvolumes on a 128^3 crop) and a `dvc` program run
+    with failed points -> reference_range_large.json (volumes rendered from
+    their recipes at test time, checked by digest);
+  * `--config1`: the plain-method workload (256^3 uint8, 1000 points, cube
+    31, 6 dof) end to end through the reference's `dvc` -> config1_dvc_run.json;
+  * `--alt-search`: the search stages the reference's source holds but never
+    selects (random_global with its clock fixed, Nelder-Mead through
+    look_with(amoeba)) on the small volumes -> reference_alt_search.json.
 Machines without the reference sources run the tests from these files.
 """
 from __future__ import annotations
@@ -35,12 +44,12 @@ sys.path.insert(0, ROOT)
 
 from digitalvolumecorrelation_gb300 import synth  # noqa: E402
 from digitalvolumecorrelation_gb300.abi import make_params  # noqa: E402
-from oracle.oracle import REF_SO, Oracle, Reference, build_reference  # noqa: E402
+from oracle.oracle import REF_SO, Oracle, Reference, build_reference, reference_dir  # noqa: E402
 
 sys.path.insert(0, HERE)
+import recipes  # noqa: E402
 from dvc_inputs import write_dvc_inputs  # noqa: E402
 
-REF_DIR = os.environ.get("DVC_REFERENCE_DIR", "/root/reference")
 SHAPE = (40, 40, 40)
 
 # search configurations run by the reference (volume set, params)
@@ -78,8 +87,9 @@ def volumes():
 
 
 def datacloud_golden():
-    roi = os.path.join(REF_DIR, "Core", "tests", "grid_input.roi")
-    src = open(os.path.join(REF_DIR, "Core", "tests", "test_DataCloud.cpp")).read()
+    ref_dir = reference_dir()
+    roi = os.path.join(ref_dir, "Core", "tests", "grid_input.roi")
+    src = open(os.path.join(ref_dir, "Core", "tests", "test_DataCloud.cpp")).read()
     block = re.search(r"std::vector<int> row = \{(.*?)\};", src, re.S).group(1)
     table = [int(v) for v in re.findall(r"-?\d+", block)]
     pts = []
@@ -159,6 +169,58 @@ DVC_RUNS = [
 ]
 
 
+def params_from_keys(shape, bpv, keys):
+    """dvc_params of a `dvc` input file's search keys."""
+    kw = {}
+    for k, v in keys:
+        if k in ("subvol_geom", "obj_function", "interp_type"):
+            kw[k] = v
+        elif k in ("subvol_size", "subvol_npts", "disp_max", "num_srch_dof"):
+            kw[k] = int(v)
+        elif k == "basin_radius":
+            kw[k] = float(v)
+        elif k in ("rigid_trans", "subvol_aspect"):
+            kw[k] = tuple(float(x) for x in v.split())
+    return make_params(shape, bytes_per_voxel=bpv, **kw)
+
+
+def reference_full_params(d, case, vols, pts):
+    """Every search parameter of a finished reference `dvc` run (its .disp
+    keeps u, v, w only): the reference's own Search::process_point run again
+    through its classes with the run's processing order (the .disp row order)
+    and neighbour lists (its .sort.csv). Rows in .disp order; u, v, w checked
+    against the .disp text."""
+    vref, vcor = vols[case["volumes"]]
+    shape = vref.shape[::-1]
+    p = params_from_keys(shape, vref.dtype.itemsize, case["keys"])
+    rows = [l.split("\t") for l in open(os.path.join(d, "result.disp")).read().strip().split("\n")[1:]]
+    neigh = np.array([[int(v) for v in l.split(",")]
+                      for l in open(os.path.join(d, "points.roi.sort.csv")).read().strip().split("\n")], np.int32)
+    labels_file = [int(l.split()[0]) for l in open(os.path.join(d, "points.roi")) if _roi_line(l)]
+    where = {lab: i for i, lab in enumerate(labels_file)}
+    order = np.array([where[int(r[0])] for r in rows], np.int32)
+    r = Reference().process(p, vref, cor=vcor, points=pts, order=order, neigh=neigh)
+    par = r["params"][order]
+    uvw = np.array([[float(v) for v in row[6:9]] for row in rows])
+    assert np.abs(par[:, :3] - uvw).max() <= 5.1e-7, "re-run differs from the program's .disp"
+    assert (r["status"][order] == np.array([int(row[4]) for row in rows])).all()
+    return par[:, :p.num_srch_dof].tolist()
+
+
+def _roi_line(line):
+    """A point-cloud line the reference keeps: an integer label first (the
+    lines written here are either that or the skipped header/comment)."""
+    f = line.split()
+    if len(f) < 4:
+        return False
+    try:
+        int(f[0])
+        float(f[1]), float(f[2]), float(f[3])
+    except ValueError:
+        return False
+    return "." not in f[0] and "e" not in f[0].lower()
+
+
 def dvc_runs_golden(tmp, vols):
     rng = np.random.default_rng(9)
     pts = synth.grid_points((3, 3, 3), 5.0, (20.0, 20.0, 20.0)) + rng.uniform(-0.4, 0.4, (27, 3)).round(2)
@@ -174,7 +236,8 @@ def dvc_runs_golden(tmp, vols):
         out = dict(case=case, points=pts.tolist(), labels=labels.tolist(),
                    disp=open(os.path.join(d, "result.disp")).read(),
                    sort_csv=open(os.path.join(d, "points.roi.sort.csv")).read(),
-                   stat=open(os.path.join(d, "result.stat")).read())
+                   stat=open(os.path.join(d, "result.stat")).read(),
+                   par=reference_full_params(d, case, vols, pts))
         if case["name"] == "u8_nostart":
             # the reference `strain` on this run's outputs: with the sort file
             # and without it (strain then writes its own)
@@ -197,7 +260,139 @@ def dvc_runs_golden(tmp, vols):
     return runs
 
 
+def run_reference_dvc(d, env_threads="8"):
+    r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "dvc"), "dvc_in"], cwd=d,
+                       capture_output=True, text=True, env=dict(os.environ, OMP_NUM_THREADS=env_threads))
+    assert r.returncode == 0, r.stdout + r.stderr
+    return dict(disp=open(os.path.join(d, "result.disp")).read(),
+                sort_csv=open(os.path.join(d, "points.roi.sort.csv")).read(),
+                stat=open(os.path.join(d, "result.stat")).read())
+
+
+def range_large_golden(tmp):
+    """Reference searches of recipes.RANGE_CASES and LARGE_CASES (the
+    reference's own Search::process_point in its order with its neighbour
+    seeding, sphere test seed 1), plus one `dvc` program run with failed
+    points. A case is recorded only if the FP64 oracle agrees on every status
+    and none of its evaluations fell in the box's last cell plane (where the
+    reference reads past its arrays and its result is undefined)."""
+    R = Reference()
+    O = Oracle()
+    out = dict(cases=[])
+    for case in recipes.RANGE_CASES + recipes.LARGE_CASES:
+        ref, cor = recipes.render(case)
+        pts = recipes.points(case)
+        p = recipes.params(case)
+        order, neigh = R.order_neighbours(pts)
+        r = R.process(p, ref, cor, points=pts, order=order, neigh=neigh)
+        o = O.process(p, ref, cor, pts, order=order, neigh=neigh)
+        assert (o["status"] == r["status"]).all(), case["name"]
+        assert o["undefined_evals"] == 0, (case["name"], o["undefined_evals"])
+        out["cases"].append(dict(name=case["name"], digest=recipes.digest(ref, cor),
+                                 order=order.tolist(), neigh=neigh.tolist(),
+                                 status=r["status"].tolist(), objmin=r["objmin"].tolist(),
+                                 params=r["params"].tolist()))
+        c = dict(zip(*np.unique(r["status"], return_counts=True)))
+        print(case["name"], {int(k): int(v) for k, v in c.items()})
+    # the `dvc` program over a case with failed points (cube: the program's
+    # sphere samples are clock-seeded)
+    spec = recipes.RANGE_DVC_RUN
+    case = recipes.by_name(spec["case"])
+    ref, cor = recipes.render(case)
+    pts = recipes.points(case)
+    labels = np.random.default_rng(spec["labels_seed"]).permutation(np.arange(1, len(pts) + 1))
+    keys = [(k, str(v)) for k, v in case["params"].items()] + [("subvol_thresh", "off"),
+                                                               ("num_points_to_process", "0")]
+    run_case = dict(name="range_run", volumes=case["name"], header=spec["header"], endian=spec["endian"],
+                    roi_extra=spec["roi_extra"], keys=keys)
+    d = os.path.join(tmp, "range_run")
+    os.makedirs(d, exist_ok=True)
+    write_dvc_inputs(d, run_case, {case["name"]: (ref, cor)}, pts, labels)
+    res = run_reference_dvc(d)
+    res["par"] = reference_full_params(d, run_case, {case["name"]: (ref, cor)}, pts)
+    out["dvc_run"] = dict(case=run_case, digest=recipes.digest(ref, cor), points=pts.tolist(),
+                          labels=labels.tolist(), **res)
+    return out
+
+
+# the alternative search stages (volume set, params): Nelder-Mead after the
+# grid, random_global before Gauss-Newton or Nelder-Mead, 3 / 6 / 12 dof
+ALT_CASES = [
+    ("A", dict(subvol_geom="cube", subvol_size=11, subvol_npts=343, obj_function="znssd", num_srch_dof=3,
+               disp_max=3, basin_radius=1.5, refine_method="nelder_mead")),
+    ("A", dict(subvol_geom="cube", subvol_size=11, subvol_npts=343, obj_function="znssd", num_srch_dof=6,
+               disp_max=3, basin_radius=1.5, refine_method="nelder_mead")),
+    ("B", dict(subvol_geom="sphere", subvol_size=13, subvol_npts=400, obj_function="ssd", num_srch_dof=6,
+               disp_max=3, basin_radius=0.0, refine_method="nelder_mead")),
+    ("A", dict(subvol_geom="cube", subvol_size=11, subvol_npts=343, obj_function="znssd", num_srch_dof=6,
+               disp_max=3, basin_radius=1.5, coarse_method="random", coarse_seed=20240613)),
+    ("B", dict(subvol_geom="cube", subvol_size=11, subvol_npts=343, obj_function="zssd", num_srch_dof=3,
+               disp_max=3, basin_radius=1.0, coarse_method="random", coarse_seed=7,
+               refine_method="nelder_mead")),
+    ("A", dict(subvol_geom="cube", subvol_size=11, subvol_npts=343, obj_function="znssd", num_srch_dof=12,
+               disp_max=3, basin_radius=1.5, refine_method="nelder_mead")),
+]
+
+
+def alt_search_golden():
+    z = np.load(os.path.join(HERE, "reference_hotpath.npz"))
+    R = Reference()
+    O = Oracle()
+    pts, order, neigh = z["search_points"], z["search_order"], z["search_neigh"]
+    out = []
+    for vs, kw in ALT_CASES:
+        vref, vcor = z[f"vol_{vs}_ref"], z[f"vol_{vs}_cor"]
+        p = make_params(SHAPE, bytes_per_voxel=vref.dtype.itemsize, interp_type="tricubic", **kw)
+        r = R.process_stages(p, vref, vcor, pts, order, neigh)
+        o = O.process(p, vref, vcor, pts, order=order, neigh=neigh)
+        assert (o["status"] == r["status"]).all() and np.abs(o["params"] - r["params"]).max() == 0.0
+        out.append(dict(volumes=vs, params=kw, status=r["status"].tolist(), objmin=r["objmin"].tolist(),
+                        params_out=r["params"].tolist(), nfunc=o["gn_iters"].tolist()))
+        print(vs, kw, {int(k): int(v) for k, v in zip(*np.unique(r["status"], return_counts=True))})
+    return out
+
+
+def config1_golden(tmp):
+    """The plain-method workload through the reference's `dvc` program."""
+    W, ref, cor = recipes.config1_volumes()
+    pts = W.points
+    labels = np.arange(1, len(pts) + 1)
+    kw = W.params_kw
+    keys = [(k, str(v)) for k, v in kw.items()] + [("subvol_thresh", "off"), ("num_points_to_process", "0")]
+    run_case = dict(name="config1", volumes="config1", header=0, endian="little", roi_extra="", keys=keys)
+    d = os.path.join(tmp, "config1")
+    os.makedirs(d, exist_ok=True)
+    write_dvc_inputs(d, run_case, {"config1": (ref, cor)}, pts, labels)
+    res = run_reference_dvc(d)
+    res["par"] = reference_full_params(d, run_case, {"config1": (ref, cor)}, pts)
+    return dict(case=run_case, digest=recipes.digest(ref, cor), points=pts.tolist(), labels=labels.tolist(),
+                **res)
+
+
 def main():
+    if "--alt-search" in sys.argv:
+        if not os.path.exists(REF_SO) and build_reference() is None:
+            raise SystemExit("reference sources not available")
+        with open(os.path.join(HERE, "reference_alt_search.json"), "w") as f:
+            json.dump(alt_search_golden(), f)
+        print("reference_alt_search.json written")
+        return
+    if "--range-large" in sys.argv or "--config1" in sys.argv:
+        if not os.path.exists(REF_SO) or not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "dvc")):
+            if build_reference() is None:
+                raise SystemExit("reference sources not available")
+        with tempfile.TemporaryDirectory() as tmp:
+            if "--range-large" in sys.argv:
+                g = range_large_golden(tmp)
+                with open(os.path.join(HERE, "reference_range_large.json"), "w") as f:
+                    json.dump(g, f)
+                print("reference_range_large.json written")
+            if "--config1" in sys.argv:
+                g = config1_golden(tmp)
+                with open(os.path.join(HERE, "config1_dvc_run.json"), "w") as f:
+                    json.dump(g, f)
+                print("config1_dvc_run.json written")
+        return
     if "--dvc-runs" in sys.argv:  # only the end-to-end program runs
         if not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "dvc")):
             if build_reference() is None:

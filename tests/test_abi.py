@@ -26,7 +26,7 @@ def test_library_exports_every_declared_function():
 def test_abi_version_and_errors_without_gpu_calls():
     lib = ctypes.CDLL(build.build_library())
     lib.dvc_gpu_abi_version.restype = ctypes.c_int
-    assert lib.dvc_gpu_abi_version() == 2
+    assert lib.dvc_gpu_abi_version() == 3
     lib.dvc_gpu_version.restype = ctypes.c_char_p
     assert b"sm_103a" in lib.dvc_gpu_version()
 

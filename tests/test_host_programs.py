@@ -156,6 +156,15 @@ def test_dvc_run_matches_reference(bins, vols, tmp_path, k):
         assert abs(oa - ob) <= 2e-5 * max(abs(ob), 1e-12) + 1e-12, (a, b)
         du = np.abs(np.array(a[6:9], float) - np.array(b[6:9], float))
         assert du.max() <= 1e-3, (a, b)
+    # <out>.par: every search parameter (the reference's, from its classes
+    # re-run over the program's order and neighbours)
+    par_rows = [l.split("\t") for l in open(os.path.join(d, "result.par")).read().strip().split("\n")[1:]]
+    par = np.array(g["par"])
+    assert len(par_rows) == len(ref) and par.shape[1] == int(dict(g["case"]["keys"])["num_srch_dof"])
+    for a, b, pr in zip(par_rows, ref, par):
+        assert a[:5] == b[:5]
+        if a[4] == "0":
+            assert np.abs(np.array(a[6:], float) - pr).max() <= 1e-3, (a, pr)
     stat = open(os.path.join(d, "result.stat")).read()
     for line in g["stat"].splitlines():
         if line.startswith(("number ", "Point Cloud", "\tbounding")) or " points processed in " in line:

@@ -7,7 +7,8 @@ scratch is a fixed array inside the library. This test calls it through the
 C ABI twice in a row and checks each result against the ordinary
 (allocating) entry point on the same inputs: identical status codes, and
 parameters and objective within the tolerances of the other parity tests
-(here far tighter, since both run the same kernel). It also checks that a
+(here far tighter, since both run the same kernel), and that the device's
+free memory is the same before and after the calls. It also checks that a
 point count above the array's capacity is refused.
 
 The file name makes pytest collect it last, so a run that stops at the first
@@ -59,8 +60,10 @@ def test_noalloc_matches_allocating_entry_point(gpu_lib, k):
     E.process_device(n, pts, order, n, neigh, nn, 0, None, st0, ob0, pa0, it0)
     torch.cuda.synchronize()
     ptr = lambda t: C.c_void_p(t.data_ptr())
-    for _ in range(2):  # two calls in a row share the library's scratch array
-        st, ob, pa, it = outputs()
+    outs = [outputs(), outputs()]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for st, ob, pa, it in outs:  # two calls in a row share the library's scratch array
         rc = noalloc(E._h, n, ptr(pts), n, ptr(order), nn, ptr(neigh), 0, None, ptr(st), ptr(ob),
                      ptr(pa), ptr(it), None)
         assert rc == 0, L.dvc_gpu_last_error()
@@ -71,6 +74,8 @@ def test_noalloc_matches_allocating_entry_point(gpu_lib, k):
         np.testing.assert_array_equal(it.cpu().numpy(), it0.cpu().numpy())
         # and the reference's recorded answer
         np.testing.assert_array_equal(st.cpu().numpy(), d[f"search_{k}_status"])
+        # the calls took no device memory: the device's free bytes are unchanged
+        assert torch.cuda.mem_get_info()[0] == free0
     E.close()
 
 

@@ -64,8 +64,9 @@ def parse():
     ap.add_argument("--learned-steps", type=int, default=3000)
     ap.add_argument("--no-batching", action="store_true",
                     help="skip configuration 3 (60 configurations in one launch)")
-    ap.add_argument("--pipeline", action="store_true",
-                    help="also run configuration 5 (8 GiB pair, 499,200 points, learned + plain)")
+    ap.add_argument("--no-pipeline", action="store_true",
+                    help="skip configuration 5 (8 GiB pair, 499,200 points, learned + plain; needs "
+                         "the learned leg's network)")
     ap.add_argument("--pipeline-only", action="store_true",
                     help="train the network (learned leg) and run only configuration 5")
     ap.add_argument("--batching-only", action="store_true",
@@ -411,7 +412,7 @@ def main():
                                   "accuracy": acc}
     if rank == 0 and not args.no_learned and world == 1:
         result["learned"], weights = learned_leg(args.learned_steps)
-        if args.pipeline:
+        if not args.no_pipeline:
             result["pipeline"] = pipeline_leg(weights)
     if rank == 0 and not args.no_batching and world == 1:
         result["batching"] = batching_leg()
@@ -440,7 +441,7 @@ def learned_leg(steps, oracle_sample=32):
     o = Oracle().process(p0, ref, cor, held.points[sample], seed_mode=1, seeds=held.truth[sample],
                          n_threads=os.cpu_count() or 1)
     ok = o["status"] == 0
-    for name in ("plain", "learned"):
+    for name in ("plain", "plain_125", "learned"):
         st, pa = res[name]
         good = ok & (st[sample] == 0)
         err = np.abs(pa[sample][good, :3] - o["params"][good, :3]).max(axis=1)

@@ -265,6 +265,10 @@ struct dvc_engine {
   // tail, counters from +64): in ws, or in the allocation-free scratch
   char *last_ctl = nullptr;
   long long wait_polls = -1;  // dependency-wait bound of the search (< 0: default)
+  // counters of the last call when it made several launches (the learned
+  // search), summed on the host; otherwise read from last_ctl
+  bool counts_host = false;
+  unsigned long long host_counts[3] = {0, 0, 0};
   int num_sms = 0;
   int cluster = 0;          // CTAs per point (0 = choose per call)
   int last_cluster = 0, last_grid = 0, last_staged = 0, last_smem = 0;
@@ -832,6 +836,7 @@ int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed,
     ws = (char *)e->ws;
   }
   e->last_ctl = ws + off_ctl;
+  e->counts_host = false;
   int *done = (int *)(ws + off_done);
   int *rank = (int *)(ws + off_rank);
   int *ctl = (int *)(ws + off_ctl);
@@ -1541,6 +1546,10 @@ int dvc_gpu_set_cluster(dvc_engine *e, int cluster) {
 int dvc_gpu_last_counters(dvc_engine *e, long long out[3]) {
   if (!e || !out) return set_error(DVC_E_ARG, "null argument");
   out[0] = out[1] = out[2] = 0;
+  if (e->counts_host) {
+    for (int k = 0; k < 3; k++) out[k] = (long long)e->host_counts[k];
+    return DVC_OK;
+  }
   if (!e->last_ctl) return DVC_OK;
   unsigned long long c[3];
   CUDA_TRY(cudaDeviceSynchronize());
@@ -1655,6 +1664,9 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
       rc = set_error(DVC_E_CUDA, "fallback count");
     if (!rc) rc = launch_error(e);
   }
+  unsigned long long counts[3] = {0, 0, 0};
+  if (!rc && cudaMemcpy(counts, e->last_ctl + kCountersOff, sizeof counts, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = set_error(DVC_E_CUDA, "learned search counters");
   if (!rc && nfb > 0) {
     if (cudaMalloc(&ob2, N * 8) != cudaSuccess || cudaMalloc(&pa2, N * 96) != cudaSuccess ||
         cudaMalloc(&st2, N * 4) != cudaSuccess || cudaMalloc(&it2, N * 4) != cudaSuccess) {
@@ -1670,6 +1682,16 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
   }
   if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = set_error(DVC_E_CUDA, "learned search");
   if (!rc && nfb > 0) rc = launch_error(e);
+  if (!rc && nfb > 0) {
+    unsigned long long c2[3];
+    if (cudaMemcpy(c2, e->last_ctl + kCountersOff, sizeof c2, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = set_error(DVC_E_CUDA, "learned search counters");
+    for (int k = 0; k < 3; k++) counts[k] += c2[k];
+  }
+  if (!rc) {
+    for (int k = 0; k < 3; k++) e->host_counts[k] = counts[k];
+    e->counts_host = true;
+  }
   if (!rc && n_fallback) *n_fallback = nfb;
   cleanup();
   return rc;

@@ -3,16 +3,19 @@
 Training pairs are 512^3 uint8 speckle volumes (one Gaussian blob per 1000
 voxels, sigma 1.5-3 voxels, amplitude 40-200, noise sigma 2) whose correlate
 volume is deformed by a random smooth field (translation, uniform strain of up
-to 2%, Gaussian bumps; |u| < 10 voxels, `synth.random_bumps`). ROI points lie
-on a grid of spacing 16 voxels. Labels are the 12 parameters the plain GPU
+to 2%, Gaussian bumps; |u| < 10 voxels, `synth.random_bumps`). Training
+points lie on a grid of spacing 12 voxels (five pairs, about 250,000 labelled
+patch pairs for the configuration's 200,000), held-out points on one of
+spacing 16. Labels are the 12 parameters the plain GPU
 search converges to from the true translation (no coarse grid needed there);
 points that do not converge well are left out. The network (dvc_cnn_*) is
 trained by Adam on patches cut on the fly from the resident volumes.
 
 `evaluate` then runs, on a held-out pair, the plain GPU method (reference
-seeding, coarse grid of basin radius 2.5 over disp_max 10, Gauss-Newton) and
+seeding, coarse grid over disp_max 10, Gauss-Newton) at two grid resolutions
+(basin radius 2.5: 9^3 = 729 translations; basin radius 5: 5^3 = 125) and
 the learned method (network start, Gauss-Newton, plain search for points whose
-ZNSSD exceeds the threshold) and times both; bench.py checks both against the
+ZNSSD exceeds the threshold) and times each; bench.py checks them against the
 FP64 oracle on a sample of points.
 
     python -m digitalvolumecorrelation_gb300.learned [--steps N]
@@ -32,7 +35,10 @@ from .abi import make_params
 SHAPE = (512, 512, 512)
 SEARCH = dict(subvol_geom="cube", subvol_size=31, subvol_npts=2000, obj_function="znssd",
               interp_type="tricubic", num_srch_dof=12, disp_max=10, basin_radius=2.5)
-SPACING = 16.0
+SPACING = 16.0        # held-out points
+TRAIN_SPACING = 12.0  # training points
+TRAIN_PAIRS = 5
+COARSE_BASIN = 5.0    # the second plain method: disp_max / 2, a 125-translation grid
 MARGIN = 40.0
 OBJ_THRESHOLD = 0.05
 
@@ -46,13 +52,13 @@ def grid(shape=SHAPE, spacing=SPACING, margin=MARGIN):
 class Pair:
     """One rendered pair resident on the GPU, its deformation and ROI points."""
 
-    def __init__(self, seed, shape=SHAPE):
+    def __init__(self, seed, shape=SHAPE, spacing=SPACING):
         import torch
         rng = np.random.default_rng(seed)
         self.deform = synth.random_bumps(shape, rng)
         nvox = int(np.prod(shape))
         self.blobs = synth.blobs(shape, nvox // 1000, sigma=(1.5, 3.0), amp=(40.0, 200.0), seed=seed + 7)
-        self.w = workloads.Workload(f"config4_pair{seed}", shape, 1, SEARCH, grid(shape), self.deform,
+        self.w = workloads.Workload(f"config4_pair{seed}", shape, 1, SEARCH, grid(shape, spacing), self.deform,
                                     self.blobs, 2.0, seed + 11, seed + 13)
         self.ref, self.cor = self.w.render_device()
         self.points = self.w.points
@@ -148,8 +154,9 @@ def evaluate(net, pair):
     nd = torch.from_numpy(neigh).to(dev)
     out = {}
     E = pair.engine()
+    E125 = pair.engine(basin_radius=COARSE_BASIN)
     res = {}
-    for name in ("plain", "learned"):
+    for name in ("plain", "plain_125", "learned"):
         st = torch.empty(n, dtype=torch.int32, device=dev)
         ob = torch.empty(n, dtype=torch.float64, device=dev)
         pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
@@ -157,30 +164,38 @@ def evaluate(net, pair):
         if name == "plain":
             run = lambda: E.process_device(n, pair.pts_dev, od, n, nd, neigh.shape[1], engine.SEED_NEIGHBOURS,
                                            None, st, ob, pa, it)
+        elif name == "plain_125":
+            run = lambda: E125.process_device(n, pair.pts_dev, od, n, nd, neigh.shape[1], engine.SEED_NEIGHBOURS,
+                                              None, st, ob, pa, it)
         else:
             run = lambda: E.process_learned(net, n, pair.pts_dev, od, n, OBJ_THRESHOLD, st, ob, pa, it)
         run()  # warm-up
         fb, secs = _time(run)
-        evals = E.last_counters()[0]
+        evals = (E125 if name == "plain_125" else E).last_counters()[0]
         res[name] = (st.cpu().numpy(), pa.cpu().numpy())
         out[name] = dict(points_per_s=round(n / secs, 1), seconds=round(secs, 4),
-                         good=int((res[name][0] == 0).sum()), last_launch_evaluations=evals,
+                         good=int((res[name][0] == 0).sum()), evaluations=evals,
                          mean_gn_iterations=float(it.float().mean().item()))
         if name == "learned":
             out[name]["fallback_points"] = int(fb)
+        else:
+            k = int(SEARCH["disp_max"] / (COARSE_BASIN if name == "plain_125" else SEARCH["basin_radius"]))
+            out[name]["grid_translations"] = (2 * k + 1) ** 3
     E.close()
-    for name in ("plain", "learned"):
+    E125.close()
+    for name in ("plain", "plain_125", "learned"):
         s, pa = res[name]
         out[name]["max_err_vs_truth_vox"] = float(np.abs(pa[s == 0, :3] - pair.truth[s == 0]).max())
     out["speedup_learned_over_plain"] = round(out["learned"]["points_per_s"] / out["plain"]["points_per_s"], 2)
+    out["speedup_learned_over_plain_125"] = round(out["learned"]["points_per_s"] / out["plain_125"]["points_per_s"], 2)
     return out, res
 
 
-def run(steps=3000, train_pairs=6, log=None, keep=False):
+def run(steps=3000, train_pairs=TRAIN_PAIRS, log=None, keep=False):
     """Train on `train_pairs` pairs, evaluate on a held-out one. With keep,
     also return the held-out pair, the per-method results and the trained
     weights."""
-    pairs = [Pair(101 + 17 * k) for k in range(train_pairs)]
+    pairs = [Pair(101 + 17 * k, spacing=TRAIN_SPACING) for k in range(train_pairs)]
     net, tinfo = train(pairs, steps=steps, log=log)
     for p in pairs:
         del p.ref, p.cor

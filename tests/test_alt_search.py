@@ -17,7 +17,7 @@ search tests. Nelder-Mead stops when its vertices' objectives agree to 1e-5
 (3 dof) or 1e-7 (6, 12 dof) relative, which is the size of the FP32
 evaluation's own error: near the end its comparisons on the GPU and in the
 FP64 reference go different ways, and its final vertex agrees only to the
-simplex's spread, here within 0.01 voxel, objmin within 1e-4 relative. For
+simplex's spread, here within 0.01 voxel, objmin within 1e-3 relative. For
 12 dof the reference exhausts its 2000 evaluations (Convg_Fail) where the
 GPU's simplex collapses below FP32 resolution and converges, so that case is
 pinned through the oracle only.
@@ -87,7 +87,7 @@ def test_search_vs_reference(gpu_lib, k):
     from digitalvolumecorrelation_gb300 import engine
     c = CASES[k]
     nm = c["params"].get("refine_method") == "nelder_mead"
-    tol_p, tol_o = (1e-2, 1e-4) if nm else (1e-3, 1e-5)
+    tol_p, tol_o = (1e-2, 1e-3) if nm else (1e-3, 1e-5)
     d = hotpath()
     vs = c["volumes"]
     E = engine.Engine(params_of(c), d[f"vol_{vs}_ref"], d[f"vol_{vs}_cor"])

@@ -177,3 +177,93 @@ def test_learned_search_and_fallback():
             assert np.abs(q[good, :3] - plain["params"][good, :3]).max() <= 0.01
     net.close()
     E.close()
+
+
+def _bump_pair(seed, shape=(96, 96, 96)):
+    from digitalvolumecorrelation_gb300 import synth
+    rng = np.random.default_rng(seed)
+    field = synth.random_bumps(shape, rng, max_disp=4.0, max_strain=0.02, n_bumps=4)
+    b = synth.blobs(shape, int(np.prod(shape)) // 300, seed=seed + 1)
+    ref = synth.render(shape, b, noise_sigma=2.0, noise_seed=seed + 2)
+    cor = synth.render(shape, b, deform=field, noise_sigma=2.0, noise_seed=seed + 3)
+    return ref, cor, field
+
+
+@pytest.mark.gpu
+def test_trained_network_gains_over_the_plain_search(oracle):
+    """What training buys. A network trained briefly on one pair (labels: the
+    plain search's converged 12 parameters from the true translation)
+    proposes each point's start on a held-out pair. The learned search
+    (network start, Gauss-Newton, the plain search again where ZNSSD exceeds
+    0.05) must need at most 40% of the plain search's objective evaluations
+    (the plain search evaluates a 125-translation grid per point) and reach
+    the FP64 oracle's optimum (within 0.01 voxel) as often as the plain
+    search does; the same network untrained must gain nothing of that."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine, synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    shape = (96, 96, 96)
+    kw = dict(subvol_geom="cube", subvol_size=17, subvol_npts=1000, obj_function="znssd",
+              interp_type="tricubic", num_srch_dof=12, disp_max=6, basin_radius=3.0)
+    p = make_params(shape, **kw)
+    p0 = make_params(shape, **dict(kw, basin_radius=0.0))
+    # training pair: labels from the true translation, Gauss-Newton only
+    ref, cor, field = _bump_pair(61)
+    tp = synth.grid_points((13, 13, 13), 4.0, (48.0, 48.0, 48.0))
+    E0 = engine.Engine(p0, ref, cor)
+    lab = E0.process(tp, seed_mode=engine.SEED_GIVEN, seeds=field.u(tp))
+    keep = np.nonzero((lab["status"] == 0) & (lab["objmin"] < 0.05))[0].astype(np.int32)
+    assert len(keep) > 1500
+    net = engine.Cnn(seed=7)
+    untrained = engine.Cnn(seed=7)
+    dev = "cuda"
+    tpd = torch.from_numpy(tp).to(dev)
+    par = torch.from_numpy(lab["params"].astype(np.float32)).to(dev)
+    x = torch.empty((64, 2, 32, 32, 32), dtype=torch.float32, device=dev)
+    rng = np.random.default_rng(3)
+    steps = 600
+    for s in range(steps):
+        pick = torch.from_numpy(rng.choice(keep, 64, replace=False)).to(dev)
+        engine.Cnn.patches(E0, 64, tpd, x, idx_dev=pick)
+        net.train_step(64, x, par.index_select(0, pick.long()).contiguous(),
+                       1e-3 * 0.5 * (1.0 + np.cos(np.pi * s / steps)))
+    E0.close()
+    # held-out pair
+    ref, cor, field = _bump_pair(71)
+    pts = synth.grid_points((7, 7, 7), 8.0, (48.0, 48.0, 48.0))
+    n = len(pts)
+    order, neigh = oracle.order_neighbours(pts)
+    E = engine.Engine(p, ref, cor)
+    plain = E.process(pts, order=order, neigh=neigh)
+    evals_plain = E.last_counters()[0]
+    pd = torch.from_numpy(pts).to(dev)
+    od = torch.from_numpy(order).to(dev)
+    out = {}
+    for name, nw in (("learned", net), ("untrained", untrained)):
+        st = torch.empty(n, dtype=torch.int32, device=dev)
+        ob = torch.empty(n, dtype=torch.float64, device=dev)
+        pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
+        nfb = E.process_learned(nw, n, pd, od, n, 0.05, st, ob, pa)
+        out[name] = dict(status=st.cpu().numpy(), params=pa.cpu().numpy(), fallback=nfb,
+                         evals=E.last_counters()[0])
+    E.close()
+    # the FP64 oracle's optimum: Gauss-Newton from the true translation
+    sample = np.arange(0, n, 7)
+    o = oracle.process(p0, ref, cor, pts[sample], seed_mode=1, seeds=field.u(pts[sample]))
+    ok = o["status"] == 0
+
+    def within(st, pa):
+        good = ok & (st[sample] == 0)
+        err = np.abs(pa[sample][good, :3] - o["params"][good, :3]).max(axis=1)
+        return int((err <= 0.01).sum())
+
+    w_plain = within(plain["status"], plain["params"])
+    w_learned = within(out["learned"]["status"], out["learned"]["params"])
+    msg = (evals_plain, out["learned"]["evals"], out["untrained"]["evals"], out["learned"]["fallback"],
+           out["untrained"]["fallback"], w_plain, w_learned, int(ok.sum()))
+    assert out["learned"]["evals"] <= 0.4 * evals_plain, msg
+    assert w_learned >= w_plain - 1, msg
+    assert out["untrained"]["fallback"] >= 4 * max(1, out["learned"]["fallback"]), msg
+    assert out["untrained"]["evals"] >= 2 * out["learned"]["evals"], msg
+    net.close()
+    untrained.close()

@@ -257,7 +257,17 @@ def profile_cnn(batch=1024, passes=3):
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
-    print(json.dumps({"profile_cnn": batch, "forward_ms": round(ms, 3), "patches_per_s": round(batch / ms * 1e3)}))
+    # algorithmic FLOPs per patch: the four convolutions (2 Cout Cin 27 per
+    # output voxel) and the two dense layers
+    conv = sum(2 * co * ci * 27 * (d // 2) ** 3 for ci, co, d in ((2, 16, 32), (16, 32, 16), (32, 64, 8), (64, 96, 4)))
+    flop = batch * (conv + 2 * 768 * 128 + 2 * 128 * 12)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("bf16_tflops", 1900.0)
+    tf = flop / (ms / 1e3) / 1e12
+    print(json.dumps({"profile_cnn": batch, "forward_ms": round(ms, 3), "patches_per_s": round(batch / ms * 1e3),
+                      "gflop": round(flop / 1e9, 2), "tflops": round(tf, 1), "frac_of_bf16_peak": round(tf / peak, 4),
+                      "convolutions": "FP32 CUDA cores" if os.environ.get("DVC_CNN_FP32") else "tcgen05 BF16"}))
     net.close()
 
 

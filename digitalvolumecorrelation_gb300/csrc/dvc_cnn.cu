@@ -17,6 +17,7 @@
 // Every kernel here is hand-written FP32 (forward, both backward passes, the
 // optimizer); weight gradients are block reductions in a fixed order, so a
 // training step is deterministic.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -34,6 +35,7 @@ namespace {
 constexpr int kP = 32;  // patch side
 constexpr int kNL = 4;  // conv layers
 const int kCin[kNL] = {2, 16, 32, 64};
+constexpr int kCinC[kNL] = {2, 16, 32, 64};
 const int kCout[kNL] = {16, 32, 64, 96};
 const int kDin[kNL] = {32, 16, 8, 4};
 constexpr int kF0 = 768, kF1 = 128, kF2 = 12;
@@ -112,6 +114,227 @@ __global__ void __launch_bounds__(256) conv_fwd8(const float *__restrict__ in, c
   }
 #pragma unroll
   for (int c = 0; c < kCoG; c++) out[((size_t)b * Cout + co0 + c) * n3 + o] = fmaxf(acc[c], 0.f);
+}
+
+
+// ---------------------------------------------- tensor-core convolution ---
+// The forward convolutions as implicit GEMMs on the 5th-generation tensor
+// cores: D[m][n] = sum_k A[m][k] B[n][k], m an output voxel of the batch
+// (128 per tile), n an output channel, k = ci * 27 + tap (the FP32 weights'
+// own order, padded with zeros to a multiple of 16). A is gathered by the
+// threads from the FP32 input activation (im2col, padding 1, stride 2) and
+// rounded to BF16; B is the weights in BF16 (conv_weights_bf16). Both are
+// written to shared memory in the canonical K-major layout without swizzle
+// (8 x 16-byte core matrices; K-adjacent core matrices 128 bytes apart,
+// row-group-adjacent ones 256 bytes apart), one 16-wide K slice per MMA.
+// One thread issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128,
+// N = Cout) into a TMEM accumulator; K runs in chunks of 64 through two
+// shared-memory stages, the gather of chunk c + 1 overlapping the MMAs of
+// chunk c (tcgen05.commit onto the stage's mbarrier). The epilogue reads the
+// accumulator with tcgen05.ld (warp w: lanes 32w..32w+31, one output voxel
+// per thread), adds the bias, applies ReLU and stores the FP32 activation in
+// the layout of the FP32 kernels. Each CTA walks tiles grid-stride. Every
+// mbarrier wait is bounded; one that gives up records an error (tc_error)
+// that dvc_cnn_forward reports.
+__device__ int tc_error = 0;
+
+constexpr int kTcM = 128, kTcKC = 64, kTcThreads = 128;
+
+__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t phase) {
+  for (long long i = 0; i < (1LL << 24); i++) {
+    uint32_t ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (ok) return true;
+    if (i > 32) __nanosleep(32);
+  }
+  atomicExch(&tc_error, 1);
+  return false;
+}
+
+// shared-memory matrix descriptor: no swizzle, K-major; LBO = byte distance
+// of K-adjacent core matrices, SBO = of row-group-adjacent ones; version 1
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+template <int CIN, int COUT, int DIN>
+__global__ void __launch_bounds__(kTcThreads) conv_fwd_tc(const float *__restrict__ in,
+                                                          const __nv_bfloat16 *__restrict__ wb,
+                                                          const float *__restrict__ bias,
+                                                          float *__restrict__ out, long long m_total) {
+  constexpr int DO = DIN / 2, DO3 = DO * DO * DO, DIN3 = DIN * DIN * DIN;
+  constexpr int K = CIN * 27, KP = (K + 15) / 16 * 16;  // padded K (the weights' row length)
+  constexpr int NCH = (KP + kTcKC - 1) / kTcKC;         // K chunks
+  constexpr int A_SLICE = kTcM * 16 * 2, B_SLICE = COUT * 16 * 2;
+  constexpr int A_STAGE = A_SLICE * (kTcKC / 16), B_STAGE = B_SLICE * (kTcKC / 16);
+  constexpr uint32_t TCOLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
+  constexpr uint32_t IDESC = tc_idesc(kTcM, COUT);
+  static_assert(COUT % 16 == 0 && COUT >= 16 && COUT <= 256, "MMA N");
+  extern __shared__ __align__(128) unsigned char tsm[];  // [2][A_STAGE] then [2][B_STAGE]
+  __shared__ __align__(8) unsigned long long bar[2];
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t a0 = tc_smem(tsm), b0 = a0 + 2 * A_STAGE;
+  const uint32_t bars[2] = {tc_smem(&bar[0]), tc_smem(&bar[1])};
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars[0]) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars[1]) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_base)),
+                 "r"(TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  uint32_t uses[2] = {0u, 0u};  // issued uses of each stage
+  bool ok = true;                // block-uniform: every wait's outcome is agreed at a barrier
+  const long long n_tiles = (m_total + kTcM - 1) / kTcM;
+  for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    // this thread's output voxel (row tid of the tile); rows past the batch
+    // gather zeros and store nothing
+    const long long m = tile * kTcM + tid;
+    const bool row = m < m_total;
+    const int b = row ? (int)(m / DO3) : 0, vox = row ? (int)(m % DO3) : 0;
+    const int ox = vox % DO, oy = (vox / DO) % DO, oz = vox / (DO * DO);
+    const float *ib = in + (size_t)b * CIN * DIN3;
+    for (int c = 0; c < NCH; c++) {
+      const int st = c & 1;
+      // the MMAs that last read this stage must have finished
+      const bool lost = uses[st] > 0 && !tc_wait(bars[st], (uses[st] - 1) & 1);
+      // A: this thread's row, K values 64c .. 64c + 63, as 8 groups of 8
+      const uint32_t arow = a0 + st * A_STAGE + (tid >> 3) * 256 + (tid & 7) * 16;
+#pragma unroll
+      for (int g = 0; g < kTcKC / 8; g++) {
+        uint32_t packed[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+          float v2[2];
+#pragma unroll
+          for (int e = 0; e < 2; e++) {
+            const int k = c * kTcKC + g * 8 + h * 2 + e;
+            float v = 0.f;
+            if (row && k < K) {
+              const int ci = k / 27, tap = k % 27;
+              const int iz = 2 * oz - 1 + tap / 9, iy = 2 * oy - 1 + (tap / 3) % 3, ix = 2 * ox - 1 + tap % 3;
+              if ((unsigned)iz < (unsigned)DIN && (unsigned)iy < (unsigned)DIN && (unsigned)ix < (unsigned)DIN)
+                v = __ldg(ib + (size_t)ci * DIN3 + ((size_t)iz * DIN + iy) * DIN + ix);
+            }
+            v2[e] = v;
+          }
+          const __nv_bfloat162 p2 = __floats2bfloat162_rn(v2[0], v2[1]);
+          packed[h] = *reinterpret_cast<const uint32_t *>(&p2);
+        }
+        const uint32_t dst = arow + (g >> 1) * A_SLICE + (g & 1) * 128;
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(packed[0]), "r"(packed[1]),
+                     "r"(packed[2]), "r"(packed[3])
+                     : "memory");
+      }
+      // B: weights [COUT][KP] (BF16), K values 64c .. 64c + 63, 16-byte pieces
+      for (int q = tid; q < COUT * (kTcKC / 8); q += kTcThreads) {
+        const int n = q / (kTcKC / 8), g = q % (kTcKC / 8);
+        const int k0 = c * kTcKC + g * 8;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (k0 < KP) v = __ldg(reinterpret_cast<const uint4 *>(wb + (size_t)n * KP + k0));
+        const uint32_t dst = b0 + st * B_STAGE + (g >> 1) * B_SLICE + (n >> 3) * 256 + (g & 1) * 128 + (n & 7) * 16;
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+                     : "memory");
+      }
+      // generic-proxy writes visible to the tensor cores, then one thread issues
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (__syncthreads_or(lost)) {
+        ok = false;
+        break;
+      }
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int nk = min(kTcKC, KP - c * kTcKC) / 16;
+        for (int j = 0; j < nk; j++) {
+          const uint64_t ad = tc_desc(a0 + st * A_STAGE + j * A_SLICE, 128, 256);
+          const uint64_t bd = tc_desc(b0 + st * B_STAGE + j * B_SLICE, 128, 256);
+          const uint32_t acc = (c > 0 || j > 0) ? 1u : 0u;
+          asm volatile(
+              "{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+              : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bars[st])
+                     : "memory");
+      }
+      uses[st] += 1;
+    }
+    if (!ok) break;
+    // the last chunk's commit tracks every MMA of the tile (the other stage's
+    // last commit, issued earlier, has completed too; its phase is waited on
+    // again, at once, before that stage's next use)
+    {
+      const int st = (NCH - 1) & 1;
+      if (__syncthreads_or(!tc_wait(bars[st], (uses[st] - 1) & 1))) {
+        ok = false;
+        break;
+      }
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // epilogue: lane = tid (warp w holds lanes 32w..32w+31), 16 columns at a time
+    float *ob = out + (size_t)b * COUT * DO3 + vox;
+#pragma unroll
+    for (int c0 = 0; c0 < COUT; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row) {
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          ob[(size_t)(c0 + j) * DO3] = fmaxf(__uint_as_float(r[j]) + __ldg(bias + c0 + j), 0.f);
+      }
+    }
+    // the accumulator is read before the next tile's first MMA overwrites it
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+  }
+  // every issued MMA has completed before the accumulator is released
+  for (int st = 0; st < 2; st++)
+    if (ok && uses[st] > 0) tc_wait(bars[st], (uses[st] - 1) & 1);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TCOLS) : "memory");
+  }
+}
+
+// FP32 weights [Cout][Cin * 27] -> BF16 rows padded with zeros to kp
+__global__ void conv_weights_bf16(const float *__restrict__ w, __nv_bfloat16 *__restrict__ wb, int cout, int k,
+                                  int kp) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cout * kp) return;
+  const int n = t / kp, j = t % kp;
+  wb[t] = __float2bfloat16_rn(j < k ? w[(size_t)n * k + j] : 0.f);
 }
 
 // conv forward, blocked further: each thread computes CT output channels of
@@ -467,6 +690,9 @@ struct dvc_cnn {
   float *act[kNL + 3] = {nullptr};     // input, conv1..4 outputs, dense1 output, dense2 output
   float *dact[kNL + 3] = {nullptr};    // gradients of the same (pre-ReLU where masked)
   float *sq = nullptr, *loss = nullptr;
+  __nv_bfloat16 *wb[kNL] = {nullptr};  // conv weights in BF16 for the tensor-core convolutions
+  bool wb_valid = false;               // wb holds the current weights
+  int num_sms = 0;
 };
 
 namespace {
@@ -506,6 +732,51 @@ Scales scales() {
   return s;
 }
 
+constexpr int kp_of(int l) { return (kCinC[l] * 27 + 15) / 16 * 16; }
+
+template <int CIN, int COUT, int DIN>
+constexpr size_t tc_smem_bytes() {
+  return 2 * (size_t)kTcM * kTcKC * 2 + 2 * (size_t)COUT * kTcKC * 2;
+}
+
+template <int CIN, int COUT, int DIN>
+int tc_attr() {
+  return cudaFuncSetAttribute(conv_fwd_tc<CIN, COUT, DIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc_smem_bytes<CIN, COUT, DIN>()) == cudaSuccess ? 0 : 1;
+}
+
+template <int CIN, int COUT, int DIN>
+void tc_launch(dvc_cnn *c, int B, int l, cudaStream_t st) {
+  const long long m_total = (long long)B * (DIN / 2) * (DIN / 2) * (DIN / 2);
+  const long long tiles = (m_total + kTcM - 1) / kTcM;
+  const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)c->num_sms * 4);
+  conv_fwd_tc<CIN, COUT, DIN><<<grid, kTcThreads, tc_smem_bytes<CIN, COUT, DIN>(), st>>>(
+      c->act[l], c->wb[l], c->p + kLay.b[l], c->act[l + 1], m_total);
+}
+
+// the BF16 copies of the conv weights, when the FP32 weights changed
+void refresh_bf16(dvc_cnn *c, cudaStream_t st) {
+  if (c->wb_valid) return;
+  for (int l = 0; l < kNL; l++) {
+    const int k = kCin[l] * 27, kp = kp_of(l), n = kCout[l] * kp;
+    conv_weights_bf16<<<(n + 255) / 256, 256, 0, st>>>(c->p + kLay.w[l], c->wb[l], kCout[l], k, kp);
+  }
+  c->wb_valid = true;
+}
+
+// tensor-core errors recorded by the kernels (a bounded wait that gave up)
+int tc_status() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, tc_error, sizeof v) != cudaSuccess)
+    return dvc_internal_set_error(DVC_E_CUDA, "reading the convolution error flag");
+  if (v) {
+    const int z = 0;
+    cudaMemcpyToSymbol(tc_error, &z, sizeof z);
+    return dvc_internal_set_error(DVC_E_TIMEOUT, "a tensor-core convolution's wait gave up");
+  }
+  return DVC_OK;
+}
+
 template <int CT, int VX>
 void conv_launch(dvc_cnn *c, int B, int l, cudaStream_t st) {
   const int Do = kDin[l] / 2;
@@ -518,9 +789,18 @@ void conv_launch(dvc_cnn *c, int B, int l, cudaStream_t st) {
 
 // forward from act[0] (already holding the patches) to act[kNL + 2]
 void forward(dvc_cnn *c, int B, cudaStream_t st) {
-  // DVC_CNN_CONV8: the one-output-per-thread kernels (conv_fwd8, fc_fwd)
-  static const bool one_voxel = getenv("DVC_CNN_CONV8") != nullptr;
-  if (one_voxel) {
+  // the convolutions on the tensor cores (BF16 operands, FP32 accumulation);
+  // DVC_CNN_FP32: the FP32 CUDA-core kernels below, DVC_CNN_CONV8 the
+  // one-output-per-thread ones (the measured alternatives)
+  const bool one_voxel = getenv("DVC_CNN_CONV8") != nullptr;
+  const bool fp32 = one_voxel || getenv("DVC_CNN_FP32") != nullptr;
+  if (!fp32) {
+    refresh_bf16(c, st);
+    tc_launch<2, 16, 32>(c, B, 0, st);
+    tc_launch<16, 32, 16>(c, B, 1, st);
+    tc_launch<32, 64, 8>(c, B, 2, st);
+    tc_launch<64, 96, 4>(c, B, 3, st);
+  } else if (one_voxel) {
     for (int l = 0; l < kNL; l++) {
       const int Do = kDin[l] / 2;
       const size_t smem = (size_t)kCin[l] * 27 * kCoG * 4;
@@ -590,7 +870,8 @@ int dvc_cnn_create(dvc_cnn **out, unsigned seed) {
   if (cudaFuncSetAttribute(conv_fwd8, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kCin[kNL - 1] * 27 * kCoG * 4) != cudaSuccess ||
       cudaFuncSetAttribute(conv_fwd_t<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(conv_fwd_t<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+      cudaFuncSetAttribute(conv_fwd_t<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      tc_attr<2, 16, 32>() || tc_attr<16, 32, 16>() || tc_attr<32, 64, 8>() || tc_attr<64, 96, 4>())
     return dvc_internal_set_error(DVC_E_CUDA, "conv kernel attribute");
   dvc_cnn *c = new dvc_cnn();
   const size_t n = kLay.total;
@@ -599,6 +880,16 @@ int dvc_cnn_create(dvc_cnn **out, unsigned seed) {
       cudaMalloc(&c->loss, 4) != cudaSuccess) {
     dvc_cnn_destroy(c);
     return dvc_internal_set_error(DVC_E_NOMEM, "network parameters");
+  }
+  for (int l = 0; l < kNL; l++)
+    if (cudaMalloc(&c->wb[l], (size_t)kCout[l] * kp_of(l) * sizeof(__nv_bfloat16)) != cudaSuccess) {
+      dvc_cnn_destroy(c);
+      return dvc_internal_set_error(DVC_E_NOMEM, "network parameters");
+    }
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
   }
   // He-normal weights (fan-in), zero biases
   std::vector<float> h(n, 0.f);
@@ -625,6 +916,7 @@ void dvc_cnn_destroy(dvc_cnn *c) {
   cudaFree(c->v);
   cudaFree(c->loss);
   cudaFree(c->sq);
+  for (int l = 0; l < kNL; l++) cudaFree(c->wb[l]);
   for (int l = 0; l < kNL + 3; l++) {
     cudaFree(c->act[l]);
     cudaFree(c->dact[l]);
@@ -646,6 +938,7 @@ int dvc_cnn_set_weights(dvc_cnn *c, const float *host, int n) {
   cudaMemset(c->m, 0, (size_t)n * 4);
   cudaMemset(c->v, 0, (size_t)n * 4);
   c->step = 0;
+  c->wb_valid = false;
   return DVC_OK;
 }
 
@@ -677,7 +970,7 @@ int dvc_cnn_gradients(dvc_cnn *c, int batch, const float *patches_dev, const flo
   if (grad_host) cudaMemcpy(grad_host, c->g, kLay.total * 4, cudaMemcpyDeviceToHost);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
-  return DVC_OK;
+  return tc_status();
 }
 
 int dvc_cnn_train_step(dvc_cnn *c, int batch, const float *patches_dev, const float *targets_dev,
@@ -689,12 +982,16 @@ int dvc_cnn_train_step(dvc_cnn *c, int batch, const float *patches_dev, const fl
   const float c1 = 1.f - std::pow(b1, (float)c->step), c2 = 1.f - std::pow(b2, (float)c->step);
   adam_kernel<<<grid_for((long long)kLay.total), 256>>>(c->p, c->g, c->m, c->v, kLay.total, lr, b1, b2, 1e-8f,
                                                         c1, c2);
+  c->wb_valid = false;
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
   return DVC_OK;
 }
 
 }  // extern "C"
+
+// the tensor-core convolutions' error flag (after the caller synchronised)
+int dvc_internal_cnn_status() { return tc_status(); }
 
 // patches of the points idx[0..n) (or 0..n) of an engine's volume pair
 int dvc_internal_patches(const void *ref, const void *cor, int bpv, int nx, int ny, int nz,

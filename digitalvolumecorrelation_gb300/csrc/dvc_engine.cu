@@ -1662,6 +1662,7 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
     if (cudaMemcpyAsync(&nfb, cnt, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       rc = set_error(DVC_E_CUDA, "fallback count");
+    if (!rc) rc = dvc_internal_cnn_status();
     if (!rc) rc = launch_error(e);
   }
   unsigned long long counts[3] = {0, 0, 0};

@@ -14,3 +14,6 @@ int dvc_internal_patches(const void *ref, const void *cor, int bpv, int nx, int 
 int dvc_internal_cnn_seed(dvc_cnn *c, const void *ref, const void *cor, int bpv, int nx, int ny, int nz,
                           int n, const double *pts_dev, const int *idx_dev, double *params_dev,
                           cudaStream_t st);
+// DVC_E_TIMEOUT when a tensor-core convolution's bounded wait gave up since
+// the last check (call after synchronising), else DVC_OK
+int dvc_internal_cnn_status();

@@ -71,12 +71,26 @@ def conv_bwd(x, W, dz):
     return dW, dz.sum(axis=(0, 2, 3, 4)), dxp[:, :, 1:-1, 1:-1, 1:-1]
 
 
-def forward(p, x):
-    """Outputs [B][12] and the activations (x: [B][2][32][32][32])."""
+def bf16(a):
+    """Values rounded to bfloat16 (round to nearest, ties to even, through
+    float32), returned as float64."""
+    f = np.ascontiguousarray(np.asarray(a, np.float64).astype(np.float32))
+    u = f.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def forward(p, x, bf16_convs=False):
+    """Outputs [B][12] and the activations (x: [B][2][32][32][32]).
+    bf16_convs: every convolution's input and weights rounded to bfloat16
+    first (the GPU's tensor-core convolutions; sums and biases exact here)."""
     layers = unpack(p)
     acts = [np.asarray(x, np.float64)]
     for W, b in layers[:4]:
-        acts.append(np.maximum(conv_fwd(acts[-1], W, b), 0.0))
+        if bf16_convs:
+            acts.append(np.maximum(conv_fwd(bf16(acts[-1]), bf16(W), b), 0.0))
+        else:
+            acts.append(np.maximum(conv_fwd(acts[-1], W, b), 0.0))
     h0 = acts[-1].reshape(len(x), -1)
     (W1, b1), (W2, b2) = layers[4], layers[5]
     h1 = np.maximum(h0 @ W1.T + b1, 0.0)
@@ -84,10 +98,13 @@ def forward(p, x):
     return y, acts, h0, h1
 
 
-def loss_and_grad(p, x, targets):
+def loss_and_grad(p, x, targets, bf16_convs=False):
     """Mean squared error of the scaled outputs against targets / SCALE, and
-    the gradient w.r.t. the flat parameter vector."""
-    y, acts, h0, h1 = forward(p, x)
+    the gradient w.r.t. the flat parameter vector. bf16_convs: the forward
+    pass with bfloat16 convolutions (as `forward`), the backward pass exact
+    with the unrounded weights and the activations that forward produced
+    (the GPU's training step)."""
+    y, acts, h0, h1 = forward(p, x, bf16_convs)
     B = len(x)
     e = y - np.asarray(targets, np.float64) / SCALE
     loss = np.mean(e * e)

@@ -83,16 +83,24 @@ def test_patches_vs_oracle(bpv):
     E.close()
 
 
-@pytest.mark.gpu
-def test_forward_and_gradients_vs_oracle():
-    import torch
-    from digitalvolumecorrelation_gb300 import engine
+def _grad_case():
     rng = np.random.default_rng(3)
     ref, cor, aff = _volumes()
     x = np.stack([np.stack([O.patch(ref, p), O.patch(cor, p)])
                   for p in rng.uniform(16, 48, (3, 3))]).astype(np.float32)
     t = (rng.normal(0, 1, (3, 12)) * O.SCALE).astype(np.float32)
-    p = _he_weights(5)
+    return x, t, _he_weights(5)
+
+
+@pytest.mark.gpu
+def test_fp32_kernels_forward_and_gradients_vs_oracle(monkeypatch):
+    """The FP32 CUDA-core convolutions (DVC_CNN_FP32) and every backward
+    kernel against the FP64 oracle: outputs within 1e-4, each layer's weight
+    and bias gradients within 1e-3 of their scale."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    monkeypatch.setenv("DVC_CNN_FP32", "1")
+    x, t, p = _grad_case()
     net = engine.Cnn(seed=1)
     net.set_weights(p)
     xd = torch.from_numpy(x).cuda()
@@ -110,6 +118,68 @@ def test_forward_and_gradients_vs_oracle():
             a, r = g[lo:lo + n], g_ref[lo:lo + n]
             scale = np.abs(r).max()
             assert np.abs(a - r).max() <= 1e-3 * scale + 1e-9, (shape, np.abs(a - r).max(), scale)
+    net.close()
+
+
+@pytest.mark.gpu
+def test_tensor_core_forward_and_gradients_vs_oracle():
+    """The production path: convolutions on the tensor cores with BF16
+    operands and FP32 sums. Against the oracle with the same operands rounded
+    to BF16 the outputs agree to FP32 summation (rtol 1e-3); against the FP64
+    network itself to the operands' BF16 rounding (3e-2). Gradients (FP32
+    backward kernels over the BF16 forward's activations) against the oracle's
+    of the same BF16 forward: rounding a forward activation to BF16 is
+    discontinuous and near zero its ReLU mask can go either way, which moves
+    single terms of a gradient (rounding alone moves these gradients by 6-18%
+    of their scale against the FP64 network's), so the check is the
+    direction of every layer's gradient (cosine >= 0.995) and 99% of its
+    entries within 5% of its scale (the first layer's entries collect every
+    downstream mask decision and move by 1-3%; the FP32 test above pins the
+    backward kernels themselves to 1e-3)."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    x, t, p = _grad_case()
+    net = engine.Cnn(seed=1)
+    net.set_weights(p)
+    xd = torch.from_numpy(x).cuda()
+    td = torch.from_numpy(t).cuda()
+    y = torch.zeros((3, 12), dtype=torch.float32, device="cuda")
+    net.forward(3, xd, y)
+    y_bf, _, _, _ = O.forward(p.astype(np.float64), x, bf16_convs=True)
+    y_ref, _, _, _ = O.forward(p.astype(np.float64), x)
+    yg = y.cpu().numpy()
+    np.testing.assert_allclose(yg, y_bf, rtol=1e-3, atol=1e-3 * np.abs(y_bf).max())
+    np.testing.assert_allclose(yg, y_ref, rtol=3e-2, atol=3e-2 * np.abs(y_ref).max())
+    g, loss = net.gradients(3, xd, td)
+    loss_ref, g_ref = O.loss_and_grad(p.astype(np.float64), x, t, bf16_convs=True)
+    assert abs(loss - loss_ref) <= 1e-3 * loss_ref
+    lay, _ = O.layout()
+    for shape, w, b in lay:
+        n = int(np.prod(shape))
+        a, r = g[w:w + n].astype(np.float64), g_ref[w:w + n]
+        cos = a @ r / (np.linalg.norm(a) * np.linalg.norm(r))
+        assert cos >= 0.995, (shape, cos)
+        q99 = np.quantile(np.abs(a - r), 0.99)
+        assert q99 <= 5e-2 * np.abs(r).max(), (shape, q99, np.abs(r).max())
+    net.close()
+
+
+@pytest.mark.gpu
+def test_tensor_core_forward_many_tiles():
+    """A batch of 40 patches: the first convolution has 1280 tiles of 128
+    output voxels (several per CTA), the last ends in a partial tile; every
+    output against the oracle with the convolutions' operands in BF16."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine
+    rng = np.random.default_rng(11)
+    x = rng.normal(0, 1, (40, 2, 32, 32, 32)).astype(np.float32)
+    p = _he_weights(9)
+    net = engine.Cnn(seed=1)
+    net.set_weights(p)
+    y = torch.zeros((40, 12), dtype=torch.float32, device="cuda")
+    net.forward(40, torch.from_numpy(x).cuda(), y)
+    y_bf, _, _, _ = O.forward(p.astype(np.float64), x, bf16_convs=True)
+    np.testing.assert_allclose(y.cpu().numpy(), y_bf, rtol=1e-3, atol=1e-3 * np.abs(y_bf).max())
     net.close()
 
 

@@ -120,10 +120,14 @@ __global__ void __launch_bounds__(256) conv_fwd8(const float *__restrict__ in, c
 // ---------------------------------------------- tensor-core convolution ---
 // The forward convolutions as implicit GEMMs on the 5th-generation tensor
 // cores: D[m][n] = sum_k A[m][k] B[n][k], m an output voxel of the batch
-// (128 per tile), n an output channel, k = ci * 27 + tap (the FP32 weights'
-// own order, padded with zeros to a multiple of 16). A is gathered by the
-// threads from the FP32 input activation (im2col, padding 1, stride 2) and
-// rounded to BF16; B is the weights in BF16 (conv_weights_bf16). Both are
+// (128 per tile), n an output channel, k a (tap, input channel) pair, padded
+// with zeros to a multiple of 16. A is gathered by the threads (im2col,
+// padding 1, stride 2): for the first layer from the FP32 patches, k = ci *
+// 27 + tap, rounded to BF16 element by element; for the others from the
+// previous layer's BF16 output in channels-last order, k = tap * Cin + ci, so
+// eight consecutive k (one tap, eight channels) are one 16-byte load stored
+// as it is. B is the weights in BF16 in the same k order (conv_weights_bf16).
+// Both are
 // written to shared memory in the canonical K-major layout without swizzle
 // (8 x 16-byte core matrices; K-adjacent core matrices 128 bytes apart,
 // row-group-adjacent ones 256 bytes apart), one 16-wide K slice per MMA.
@@ -132,8 +136,10 @@ __global__ void __launch_bounds__(256) conv_fwd8(const float *__restrict__ in, c
 // shared-memory stages, the gather of chunk c + 1 overlapping the MMAs of
 // chunk c (tcgen05.commit onto the stage's mbarrier). The epilogue reads the
 // accumulator with tcgen05.ld (warp w: lanes 32w..32w+31, one output voxel
-// per thread), adds the bias, applies ReLU and stores the FP32 activation in
-// the layout of the FP32 kernels. Each CTA walks tiles grid-stride. Every
+// per thread), adds the bias, applies ReLU and stores the activation: BF16
+// channels-last for the next convolution (16-byte stores) and, when given,
+// FP32 in the layout of the FP32 kernels (the dense layer's input, the
+// backward pass). Each CTA walks tiles grid-stride. Every
 // mbarrier wait is bounded; one that gives up records an error (tc_error)
 // that dvc_cnn_forward reports.
 __device__ int tc_error = 0;
@@ -172,9 +178,13 @@ __host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
 
 template <int CIN, int COUT, int DIN>
 __global__ void __launch_bounds__(kTcThreads) conv_fwd_tc(const float *__restrict__ in,
+                                                          const __nv_bfloat16 *__restrict__ in_b,
                                                           const __nv_bfloat16 *__restrict__ wb,
                                                           const float *__restrict__ bias,
-                                                          float *__restrict__ out, long long m_total) {
+                                                          float *__restrict__ out,
+                                                          __nv_bfloat16 *__restrict__ out_b, long long m_total) {
+  constexpr bool IN_B = CIN % 8 == 0;  // BF16 channels-last input, k = tap * CIN + ci
+  static_assert(!IN_B || (CIN & (CIN - 1)) == 0, "channel count a power of two");
   constexpr int DO = DIN / 2, DO3 = DO * DO * DO, DIN3 = DIN * DIN * DIN;
   constexpr int K = CIN * 27, KP = (K + 15) / 16 * 16;  // padded K (the weights' row length)
   constexpr int NCH = (KP + kTcKC - 1) / kTcKC;         // K chunks
@@ -221,6 +231,24 @@ __global__ void __launch_bounds__(kTcThreads) conv_fwd_tc(const float *__restric
       const bool lost = uses[st] > 0 && !tc_wait(bars[st], (uses[st] - 1) & 1);
       // A: this thread's row, K values 64c .. 64c + 63, as 8 groups of 8
       const uint32_t arow = a0 + st * A_STAGE + (tid >> 3) * 256 + (tid & 7) * 16;
+      if constexpr (IN_B) {
+        const __nv_bfloat16 *rb = in_b + (size_t)b * DIN3 * CIN;
+#pragma unroll
+        for (int g = 0; g < kTcKC / 8; g++) {
+          const int k0 = c * kTcKC + g * 8;
+          const int tap = k0 / CIN, ci0 = k0 % CIN;
+          uint4 v = make_uint4(0u, 0u, 0u, 0u);
+          if (row && tap < 27) {
+            const int iz = 2 * oz - 1 + tap / 9, iy = 2 * oy - 1 + (tap / 3) % 3, ix = 2 * ox - 1 + tap % 3;
+            if ((unsigned)iz < (unsigned)DIN && (unsigned)iy < (unsigned)DIN && (unsigned)ix < (unsigned)DIN)
+              v = __ldg(reinterpret_cast<const uint4 *>(rb + ((size_t)(iz * DIN + iy) * DIN + ix) * CIN + ci0));
+          }
+          const uint32_t dst = arow + (g >> 1) * A_SLICE + (g & 1) * 128;
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(v.x), "r"(v.y), "r"(v.z),
+                       "r"(v.w)
+                       : "memory");
+        }
+      } else
 #pragma unroll
       for (int g = 0; g < kTcKC / 8; g++) {
         uint32_t packed[4];
@@ -308,9 +336,24 @@ __global__ void __launch_bounds__(kTcThreads) conv_fwd_tc(const float *__restric
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (row) {
+        float v[16];
 #pragma unroll
-        for (int j = 0; j < 16; j++)
-          ob[(size_t)(c0 + j) * DO3] = fmaxf(__uint_as_float(r[j]) + __ldg(bias + c0 + j), 0.f);
+        for (int j = 0; j < 16; j++) v[j] = fmaxf(__uint_as_float(r[j]) + __ldg(bias + c0 + j), 0.f);
+        if (out) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) ob[(size_t)(c0 + j) * DO3] = v[j];
+        }
+        if (out_b) {
+          uint32_t pk[8];
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+            pk[j] = *reinterpret_cast<const uint32_t *>(&h2);
+          }
+          uint4 *dst = reinterpret_cast<uint4 *>(out_b + ((size_t)b * DO3 + vox) * COUT + c0);
+          dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
       }
     }
     // the accumulator is read before the next tile's first MMA overwrites it
@@ -328,13 +371,19 @@ __global__ void __launch_bounds__(kTcThreads) conv_fwd_tc(const float *__restric
   }
 }
 
-// FP32 weights [Cout][Cin * 27] -> BF16 rows padded with zeros to kp
-__global__ void conv_weights_bf16(const float *__restrict__ w, __nv_bfloat16 *__restrict__ wb, int cout, int k,
-                                  int kp) {
+// FP32 weights [Cout][Cin][27] -> BF16 rows padded with zeros to kp, in the
+// convolution's k order: ci * 27 + tap, or tap * cin + ci (tap_major)
+__global__ void conv_weights_bf16(const float *__restrict__ w, __nv_bfloat16 *__restrict__ wb, int cout, int cin,
+                                  int kp, int tap_major) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cout * kp) return;
-  const int n = t / kp, j = t % kp;
-  wb[t] = __float2bfloat16_rn(j < k ? w[(size_t)n * k + j] : 0.f);
+  const int n = t / kp, j = t % kp, k = cin * 27;
+  float v = 0.f;
+  if (j < k) {
+    const int ci = tap_major ? j % cin : j / 27, tap = tap_major ? j / cin : j % 27;
+    v = w[((size_t)n * cin + ci) * 27 + tap];
+  }
+  wb[t] = __float2bfloat16_rn(v);
 }
 
 // conv forward, blocked further: each thread computes CT output channels of
@@ -691,6 +740,7 @@ struct dvc_cnn {
   float *dact[kNL + 3] = {nullptr};    // gradients of the same (pre-ReLU where masked)
   float *sq = nullptr, *loss = nullptr;
   __nv_bfloat16 *wb[kNL] = {nullptr};  // conv weights in BF16 for the tensor-core convolutions
+  __nv_bfloat16 *actb[kNL - 1] = {nullptr};  // conv 1..3 outputs, BF16 channels-last
   bool wb_valid = false;               // wb holds the current weights
   int num_sms = 0;
 };
@@ -714,6 +764,10 @@ int ensure_batch(dvc_cnn *c, int B) {
     c->act[l] = c->dact[l] = nullptr;
   }
   cudaFree(c->sq);
+  for (int l = 0; l < kNL - 1; l++) {
+    cudaFree(c->actb[l]);
+    c->actb[l] = nullptr;
+  }
   c->cap = 0;
   for (int l = 0; l < kNL + 3; l++) {
     if (cudaMalloc(&c->act[l], act_size(l) * B * 4) != cudaSuccess ||
@@ -722,6 +776,9 @@ int ensure_batch(dvc_cnn *c, int B) {
   }
   if (cudaMalloc(&c->sq, (size_t)B * kF2 * 4) != cudaSuccess)
     return dvc_internal_set_error(DVC_E_NOMEM, "network loss buffer");
+  for (int l = 0; l < kNL - 1; l++)
+    if (cudaMalloc(&c->actb[l], act_size(l + 1) * B * sizeof(__nv_bfloat16)) != cudaSuccess)
+      return dvc_internal_set_error(DVC_E_NOMEM, "network activations");
   c->cap = B;
   return DVC_OK;
 }
@@ -745,21 +802,27 @@ int tc_attr() {
                               (int)tc_smem_bytes<CIN, COUT, DIN>()) == cudaSuccess ? 0 : 1;
 }
 
+// layer l: input act[l] (FP32, the first layer) or actb[l - 1] (BF16
+// channels-last); output actb[l] for the next convolution and, when fp32_out,
+// act[l + 1] (the last layer always: the dense layer's input)
 template <int CIN, int COUT, int DIN>
-void tc_launch(dvc_cnn *c, int B, int l, cudaStream_t st) {
+void tc_launch(dvc_cnn *c, int B, int l, bool fp32_out, cudaStream_t st) {
   const long long m_total = (long long)B * (DIN / 2) * (DIN / 2) * (DIN / 2);
   const long long tiles = (m_total + kTcM - 1) / kTcM;
   const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)c->num_sms * 4);
+  const bool last = l == kNL - 1;
   conv_fwd_tc<CIN, COUT, DIN><<<grid, kTcThreads, tc_smem_bytes<CIN, COUT, DIN>(), st>>>(
-      c->act[l], c->wb[l], c->p + kLay.b[l], c->act[l + 1], m_total);
+      c->act[l], l > 0 ? c->actb[l - 1] : nullptr, c->wb[l], c->p + kLay.b[l],
+      (fp32_out || last) ? c->act[l + 1] : nullptr, last ? nullptr : c->actb[l], m_total);
 }
 
 // the BF16 copies of the conv weights, when the FP32 weights changed
 void refresh_bf16(dvc_cnn *c, cudaStream_t st) {
   if (c->wb_valid) return;
   for (int l = 0; l < kNL; l++) {
-    const int k = kCin[l] * 27, kp = kp_of(l), n = kCout[l] * kp;
-    conv_weights_bf16<<<(n + 255) / 256, 256, 0, st>>>(c->p + kLay.w[l], c->wb[l], kCout[l], k, kp);
+    const int kp = kp_of(l), n = kCout[l] * kp;
+    conv_weights_bf16<<<(n + 255) / 256, 256, 0, st>>>(c->p + kLay.w[l], c->wb[l], kCout[l], kCin[l], kp,
+                                                        kCin[l] % 8 == 0 ? 1 : 0);
   }
   c->wb_valid = true;
 }
@@ -787,8 +850,9 @@ void conv_launch(dvc_cnn *c, int B, int l, cudaStream_t st) {
                                               kCin[l], kCout[l], kDin[l]);
 }
 
-// forward from act[0] (already holding the patches) to act[kNL + 2]
-void forward(dvc_cnn *c, int B, cudaStream_t st) {
+// forward from act[0] (already holding the patches) to act[kNL + 2];
+// keep: every layer's FP32 activation in act[] (the backward pass needs them)
+void forward(dvc_cnn *c, int B, cudaStream_t st, bool keep = true) {
   // the convolutions on the tensor cores (BF16 operands, FP32 accumulation);
   // DVC_CNN_FP32: the FP32 CUDA-core kernels below, DVC_CNN_CONV8 the
   // one-output-per-thread ones (the measured alternatives)
@@ -796,10 +860,10 @@ void forward(dvc_cnn *c, int B, cudaStream_t st) {
   const bool fp32 = one_voxel || getenv("DVC_CNN_FP32") != nullptr;
   if (!fp32) {
     refresh_bf16(c, st);
-    tc_launch<2, 16, 32>(c, B, 0, st);
-    tc_launch<16, 32, 16>(c, B, 1, st);
-    tc_launch<32, 64, 8>(c, B, 2, st);
-    tc_launch<64, 96, 4>(c, B, 3, st);
+    tc_launch<2, 16, 32>(c, B, 0, keep, st);
+    tc_launch<16, 32, 16>(c, B, 1, keep, st);
+    tc_launch<32, 64, 8>(c, B, 2, keep, st);
+    tc_launch<64, 96, 4>(c, B, 3, keep, st);
   } else if (one_voxel) {
     for (int l = 0; l < kNL; l++) {
       const int Do = kDin[l] / 2;
@@ -917,6 +981,7 @@ void dvc_cnn_destroy(dvc_cnn *c) {
   cudaFree(c->loss);
   cudaFree(c->sq);
   for (int l = 0; l < kNL; l++) cudaFree(c->wb[l]);
+  for (int l = 0; l < kNL - 1; l++) cudaFree(c->actb[l]);
   for (int l = 0; l < kNL + 3; l++) {
     cudaFree(c->act[l]);
     cudaFree(c->dact[l]);
@@ -948,7 +1013,7 @@ int dvc_cnn_forward(dvc_cnn *c, int batch, const float *patches_dev, float *out_
   int rc = ensure_batch(c, batch);
   if (rc) return rc;
   cudaMemcpyAsync(c->act[0], patches_dev, act_size(0) * batch * 4, cudaMemcpyDeviceToDevice, st);
-  forward(c, batch, st);
+  forward(c, batch, st, false);
   cudaMemcpyAsync(out_dev, c->act[kNL + 2], (size_t)batch * kF2 * 4, cudaMemcpyDeviceToDevice, st);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
@@ -1028,7 +1093,7 @@ int dvc_internal_cnn_seed(dvc_cnn *c, const void *ref, const void *cor, int bpv,
     else
       patch_kernel<uint16_t><<<nb, 256, 0, st>>>((const uint16_t *)ref, (const uint16_t *)cor, nx, ny, nz,
                                                  pb, ib, c->act[0]);
-    forward(c, nb, st);
+    forward(c, nb, st, false);
     denorm_kernel<<<(nb * kF2 + 255) / 256, 256, 0, st>>>(c->act[kNL + 2], scales(),
                                                           idx_dev ? idx_dev + r0 : nullptr,
                                                           params_dev + (idx_dev ? 0 : (size_t)r0 * kF2), nb);

@@ -231,59 +231,75 @@ __global__ void __launch_bounds__(kTcThreads) conv_fwd_tc(const float *__restric
       const bool lost = uses[st] > 0 && !tc_wait(bars[st], (uses[st] - 1) & 1);
       // A: this thread's row, K values 64c .. 64c + 63, as 8 groups of 8
       const uint32_t arow = a0 + st * A_STAGE + (tid >> 3) * 256 + (tid & 7) * 16;
+      // every load of the chunk is issued before the first shared-memory
+      // store (one round trip per chunk, not one per group)
       if constexpr (IN_B) {
         const __nv_bfloat16 *rb = in_b + (size_t)b * DIN3 * CIN;
+        uint4 v[kTcKC / 8];
 #pragma unroll
         for (int g = 0; g < kTcKC / 8; g++) {
           const int k0 = c * kTcKC + g * 8;
           const int tap = k0 / CIN, ci0 = k0 % CIN;
-          uint4 v = make_uint4(0u, 0u, 0u, 0u);
+          v[g] = make_uint4(0u, 0u, 0u, 0u);
           if (row && tap < 27) {
             const int iz = 2 * oz - 1 + tap / 9, iy = 2 * oy - 1 + (tap / 3) % 3, ix = 2 * ox - 1 + tap % 3;
             if ((unsigned)iz < (unsigned)DIN && (unsigned)iy < (unsigned)DIN && (unsigned)ix < (unsigned)DIN)
-              v = __ldg(reinterpret_cast<const uint4 *>(rb + ((size_t)(iz * DIN + iy) * DIN + ix) * CIN + ci0));
+              v[g] = __ldg(reinterpret_cast<const uint4 *>(rb + ((size_t)(iz * DIN + iy) * DIN + ix) * CIN + ci0));
           }
-          const uint32_t dst = arow + (g >> 1) * A_SLICE + (g & 1) * 128;
-          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(v.x), "r"(v.y), "r"(v.z),
-                       "r"(v.w)
-                       : "memory");
         }
-      } else
+#pragma unroll
+        for (int g = 0; g < kTcKC / 8; g++) {
+          const uint32_t dst = arow + (g >> 1) * A_SLICE + (g & 1) * 128;
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(v[g].x), "r"(v[g].y),
+                       "r"(v[g].z), "r"(v[g].w));
+        }
+      } else {
+      float f[kTcKC];
+#pragma unroll
+      for (int j = 0; j < kTcKC; j++) {
+        const int k = c * kTcKC + j;
+        f[j] = 0.f;
+        if (row && k < K) {
+          const int ci = k / 27, tap = k % 27;
+          const int iz = 2 * oz - 1 + tap / 9, iy = 2 * oy - 1 + (tap / 3) % 3, ix = 2 * ox - 1 + tap % 3;
+          if ((unsigned)iz < (unsigned)DIN && (unsigned)iy < (unsigned)DIN && (unsigned)ix < (unsigned)DIN)
+            f[j] = __ldg(ib + (size_t)ci * DIN3 + ((size_t)iz * DIN + iy) * DIN + ix);
+        }
+      }
 #pragma unroll
       for (int g = 0; g < kTcKC / 8; g++) {
         uint32_t packed[4];
 #pragma unroll
         for (int h = 0; h < 4; h++) {
-          float v2[2];
-#pragma unroll
-          for (int e = 0; e < 2; e++) {
-            const int k = c * kTcKC + g * 8 + h * 2 + e;
-            float v = 0.f;
-            if (row && k < K) {
-              const int ci = k / 27, tap = k % 27;
-              const int iz = 2 * oz - 1 + tap / 9, iy = 2 * oy - 1 + (tap / 3) % 3, ix = 2 * ox - 1 + tap % 3;
-              if ((unsigned)iz < (unsigned)DIN && (unsigned)iy < (unsigned)DIN && (unsigned)ix < (unsigned)DIN)
-                v = __ldg(ib + (size_t)ci * DIN3 + ((size_t)iz * DIN + iy) * DIN + ix);
-            }
-            v2[e] = v;
-          }
-          const __nv_bfloat162 p2 = __floats2bfloat162_rn(v2[0], v2[1]);
+          const __nv_bfloat162 p2 = __floats2bfloat162_rn(f[g * 8 + 2 * h], f[g * 8 + 2 * h + 1]);
           packed[h] = *reinterpret_cast<const uint32_t *>(&p2);
         }
         const uint32_t dst = arow + (g >> 1) * A_SLICE + (g & 1) * 128;
         asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(packed[0]), "r"(packed[1]),
-                     "r"(packed[2]), "r"(packed[3])
-                     : "memory");
+                     "r"(packed[2]), "r"(packed[3]));
+      }
       }
       // B: weights [COUT][KP] (BF16), K values 64c .. 64c + 63, 16-byte pieces
-      for (int q = tid; q < COUT * (kTcKC / 8); q += kTcThreads) {
-        const int n = q / (kTcKC / 8), g = q % (kTcKC / 8);
-        const int k0 = c * kTcKC + g * 8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (k0 < KP) v = __ldg(reinterpret_cast<const uint4 *>(wb + (size_t)n * KP + k0));
-        const uint32_t dst = b0 + st * B_STAGE + (g >> 1) * B_SLICE + (n >> 3) * 256 + (g & 1) * 128 + (n & 7) * 16;
-        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
-                     : "memory");
+      {
+        constexpr int NQ = (COUT * (kTcKC / 8) + kTcThreads - 1) / kTcThreads;
+        uint4 w[NQ];
+#pragma unroll
+        for (int i = 0; i < NQ; i++) {
+          const int q = tid + i * kTcThreads;
+          const int n = q / (kTcKC / 8), g = q % (kTcKC / 8);
+          const int k0 = c * kTcKC + g * 8;
+          w[i] = make_uint4(0u, 0u, 0u, 0u);
+          if (q < COUT * (kTcKC / 8) && k0 < KP) w[i] = __ldg(reinterpret_cast<const uint4 *>(wb + (size_t)n * KP + k0));
+        }
+#pragma unroll
+        for (int i = 0; i < NQ; i++) {
+          const int q = tid + i * kTcThreads;
+          if (q >= COUT * (kTcKC / 8)) break;
+          const int n = q / (kTcKC / 8), g = q % (kTcKC / 8);
+          const uint32_t dst = b0 + st * B_STAGE + (g >> 1) * B_SLICE + (n >> 3) * 256 + (g & 1) * 128 + (n & 7) * 16;
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(w[i].x), "r"(w[i].y),
+                       "r"(w[i].z), "r"(w[i].w));
+        }
       }
       // generic-proxy writes visible to the tensor cores, then one thread issues
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -564,24 +580,28 @@ __global__ void fc_fwd(const float *__restrict__ x, const float *__restrict__ w,
   y[t] = relu ? fmaxf(acc, 0.f) : acc;
 }
 
-// dense forward with 128 outputs, tiled: a block takes 8 samples and all 128
-// outputs, input and weight slices of 32 pass through shared memory
-// (coalesced reads; the weight tile padded to 33 columns against bank
-// conflicts); thread (tb, tj) accumulates outputs tj, tj + 32, tj + 64,
-// tj + 96 of sample tb over the inputs in ascending order from the bias, as
-// fc_fwd does, so the results are bit-identical to it.
-constexpr int kFcTB = 8, kFcIC = 32;
+// dense forward with 128 outputs, tiled: a block takes 32 samples and all
+// 128 outputs (each weight slice read once per 32 samples: 8 samples per
+// block re-read the 393 KB of weights 128 times per 1024 samples), input
+// and weight slices of 32 pass through shared memory (coalesced reads; the
+// weight tile padded to 33 columns against bank conflicts); thread (tb, tj)
+// accumulates outputs tj, tj + 32, tj + 64, tj + 96 of samples tb + 8 s over
+// the inputs in ascending order from the bias, as fc_fwd does, so the
+// results are bit-identical to it.
+constexpr int kFcTB = 32, kFcIC = 32;
 __global__ void __launch_bounds__(256) fc_fwd128(const float *__restrict__ x, const float *__restrict__ w,
                                                  const float *__restrict__ bias, float *__restrict__ y, int B,
                                                  int Nin, int relu) {
   __shared__ float sx[kFcTB][kFcIC];
   __shared__ float sw[128][kFcIC + 1];
+  // thread: samples tb + 8 s (s < 4) of the block, outputs tj + 32 m (m < 4)
   const int tid = threadIdx.x, tb = tid / 32, tj = tid % 32;
   const int b0 = blockIdx.x * kFcTB;
-  const bool live = b0 + tb < B;
-  float acc[4];
+  float acc[4][4];
 #pragma unroll
-  for (int m = 0; m < 4; m++) acc[m] = bias[tj + 32 * m];
+  for (int s4 = 0; s4 < 4; s4++)
+#pragma unroll
+    for (int m = 0; m < 4; m++) acc[s4][m] = bias[tj + 32 * m];
   for (int i0 = 0; i0 < Nin; i0 += kFcIC) {
     for (int e = tid; e < kFcTB * kFcIC; e += 256) {
       const int bb = e / kFcIC, ii = e % kFcIC;
@@ -594,18 +614,27 @@ __global__ void __launch_bounds__(256) fc_fwd128(const float *__restrict__ x, co
     __syncthreads();
 #pragma unroll 8
     for (int ii = 0; ii < kFcIC; ii++) {
-      const float xv = sx[tb][ii];
+      float wv[4];
 #pragma unroll
-      for (int m = 0; m < 4; m++) acc[m] = fmaf(sw[tj + 32 * m][ii], xv, acc[m]);
+      for (int m = 0; m < 4; m++) wv[m] = sw[tj + 32 * m][ii];
+#pragma unroll
+      for (int s4 = 0; s4 < 4; s4++) {
+        const float xv = sx[tb + 8 * s4][ii];
+#pragma unroll
+        for (int m = 0; m < 4; m++) acc[s4][m] = fmaf(wv[m], xv, acc[s4][m]);
+      }
     }
     __syncthreads();
   }
-  if (live)
+#pragma unroll
+  for (int s4 = 0; s4 < 4; s4++) {
+    if (b0 + tb + 8 * s4 >= B) continue;
 #pragma unroll
     for (int m = 0; m < 4; m++) {
-      const float v = acc[m];
-      y[(size_t)(b0 + tb) * 128 + tj + 32 * m] = relu ? fmaxf(v, 0.f) : v;
+      const float v = acc[s4][m];
+      y[(size_t)(b0 + tb + 8 * s4) * 128 + tj + 32 * m] = relu ? fmaxf(v, 0.f) : v;
     }
+  }
 }
 
 // dense input gradient times the input's ReLU mask
@@ -1079,7 +1108,7 @@ int dvc_internal_patches(const void *ref, const void *cor, int bpv, int nx, int 
 int dvc_internal_cnn_seed(dvc_cnn *c, const void *ref, const void *cor, int bpv, int nx, int ny,
                           int nz, int n, const double *pts_dev, const int *idx_dev, double *params_dev,
                           cudaStream_t st) {
-  const int B = 1024;
+  const int B = 4096;  // patches per network pass (the last convolution: 256 tiles of 128 outputs)
   int rc = ensure_batch(c, B);
   if (rc) return rc;
   for (int r0 = 0; r0 < n; r0 += B) {

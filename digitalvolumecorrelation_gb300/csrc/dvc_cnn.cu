@@ -580,61 +580,37 @@ __global__ void fc_fwd(const float *__restrict__ x, const float *__restrict__ w,
   y[t] = relu ? fmaxf(acc, 0.f) : acc;
 }
 
-// dense forward with 128 outputs, tiled: a block takes 32 samples and all
-// 128 outputs (each weight slice read once per 32 samples: 8 samples per
-// block re-read the 393 KB of weights 128 times per 1024 samples), input
-// and weight slices of 32 pass through shared memory (coalesced reads; the
-// weight tile padded to 33 columns against bank conflicts); thread (tb, tj)
-// accumulates outputs tj, tj + 32, tj + 64, tj + 96 of samples tb + 8 s over
-// the inputs in ascending order from the bias, as fc_fwd does, so the
-// results are bit-identical to it.
-constexpr int kFcTB = 32, kFcIC = 32;
+// dense forward with 128 outputs, tiled: a block takes 8 samples and 32 of
+// the 128 outputs (blockIdx.y), 512 blocks per 1024 samples; input and
+// weight slices of 32 pass through shared memory (coalesced reads; the weight
+// tile padded to 33 columns against bank conflicts); thread (tb, tj)
+// accumulates output 32 blockIdx.y + tj of sample tb over the inputs in
+// ascending order from the bias, as fc_fwd does, so the results are
+// bit-identical to it.
+constexpr int kFcTB = 8, kFcIC = 32;
 __global__ void __launch_bounds__(256) fc_fwd128(const float *__restrict__ x, const float *__restrict__ w,
                                                  const float *__restrict__ bias, float *__restrict__ y, int B,
                                                  int Nin, int relu) {
   __shared__ float sx[kFcTB][kFcIC];
-  __shared__ float sw[128][kFcIC + 1];
-  // thread: samples tb + 8 s (s < 4) of the block, outputs tj + 32 m (m < 4)
+  __shared__ float sw[32][kFcIC + 1];
   const int tid = threadIdx.x, tb = tid / 32, tj = tid % 32;
-  const int b0 = blockIdx.x * kFcTB;
-  float acc[4][4];
-#pragma unroll
-  for (int s4 = 0; s4 < 4; s4++)
-#pragma unroll
-    for (int m = 0; m < 4; m++) acc[s4][m] = bias[tj + 32 * m];
+  const int b0 = blockIdx.x * kFcTB, j0 = blockIdx.y * 32;
+  float acc = bias[j0 + tj];
   for (int i0 = 0; i0 < Nin; i0 += kFcIC) {
-    for (int e = tid; e < kFcTB * kFcIC; e += 256) {
-      const int bb = e / kFcIC, ii = e % kFcIC;
+    {
+      const int bb = tid / kFcIC, ii = tid % kFcIC;
       sx[bb][ii] = (b0 + bb < B) ? x[(size_t)(b0 + bb) * Nin + i0 + ii] : 0.f;
     }
-    for (int e = tid; e < 128 * kFcIC; e += 256) {
+    for (int e = tid; e < 32 * kFcIC; e += 256) {
       const int jj = e / kFcIC, ii = e % kFcIC;
-      sw[jj][ii] = w[(size_t)jj * Nin + i0 + ii];
+      sw[jj][ii] = w[(size_t)(j0 + jj) * Nin + i0 + ii];
     }
     __syncthreads();
 #pragma unroll 8
-    for (int ii = 0; ii < kFcIC; ii++) {
-      float wv[4];
-#pragma unroll
-      for (int m = 0; m < 4; m++) wv[m] = sw[tj + 32 * m][ii];
-#pragma unroll
-      for (int s4 = 0; s4 < 4; s4++) {
-        const float xv = sx[tb + 8 * s4][ii];
-#pragma unroll
-        for (int m = 0; m < 4; m++) acc[s4][m] = fmaf(wv[m], xv, acc[s4][m]);
-      }
-    }
+    for (int ii = 0; ii < kFcIC; ii++) acc = fmaf(sw[tj][ii], sx[tb][ii], acc);
     __syncthreads();
   }
-#pragma unroll
-  for (int s4 = 0; s4 < 4; s4++) {
-    if (b0 + tb + 8 * s4 >= B) continue;
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      const float v = acc[s4][m];
-      y[(size_t)(b0 + tb + 8 * s4) * 128 + tj + 32 * m] = relu ? fmaxf(v, 0.f) : v;
-    }
-  }
+  if (b0 + tb < B) y[(size_t)(b0 + tb) * 128 + j0 + tj] = relu ? fmaxf(acc, 0.f) : acc;
 }
 
 // dense input gradient times the input's ReLU mask
@@ -916,8 +892,9 @@ void forward(dvc_cnn *c, int B, cudaStream_t st, bool keep = true) {
     fc_fwd<<<(B * kF1 + 255) / 256, 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL], c->p + kLay.b[kNL],
                                                   c->act[kNL + 1], B, kF0, kF1, 1);
   else
-    fc_fwd128<<<(B + kFcTB - 1) / kFcTB, 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL], c->p + kLay.b[kNL],
-                                                       c->act[kNL + 1], B, kF0, 1);
+    fc_fwd128<<<dim3((B + kFcTB - 1) / kFcTB, kF1 / 32), 256, 0, st>>>(c->act[kNL], c->p + kLay.w[kNL],
+                                                                       c->p + kLay.b[kNL], c->act[kNL + 1], B,
+                                                                       kF0, 1);
   fc_fwd<<<(B * kF2 + 255) / 256, 256, 0, st>>>(c->act[kNL + 1], c->p + kLay.w[kNL + 1],
                                                 c->p + kLay.b[kNL + 1], c->act[kNL + 2], B, kF1, kF2, 0);
 }

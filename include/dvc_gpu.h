@@ -351,8 +351,10 @@ int dvc_gpu_plan_autotune(dvc_plan *plan, const int *point_cfg_dev, int n_points
  * trgrid_global (Core/Search.cpp:277-377,934-1043). Conv 2->16->32->64->96
  * (3^3, stride 2, ReLU), dense 768->128 (ReLU) ->12; outputs are the
  * parameters divided by fixed scales (translations 10 voxels, rotations
- * 0.05 rad, strains 0.02). FP32 weights; training by mean squared error and
- * Adam, all on the GPU. */
+ * 0.05 rad, strains 0.02). FP32 master weights; the convolutions run on the
+ * tensor cores with BF16 operands and FP32 accumulation (environment variable
+ * DVC_CNN_FP32=1: on the FP32 pipes, FP32 operands); training by mean squared
+ * error and Adam, all on the GPU. */
 typedef struct dvc_cnn dvc_cnn;
 int dvc_cnn_create(dvc_cnn **out, unsigned seed);  /* He-normal initial weights */
 void dvc_cnn_destroy(dvc_cnn *net);

@@ -336,6 +336,10 @@ def main():
     if device_status != 0:
         raise SystemExit(f"search launch reported device status {device_status}")
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
+    # the search's launches per step: one per non-empty rank window
+    w1, w2, wide = E.last_windows()
+    search_launches = sum(1 for lo, hi in ((0, w1), (w1, w2), (w2, n)) if hi > lo)
+    launch = dict(E.last_launch(), windows={"first": w1, "last": n - w2, "cluster": wide})
     status = status_d.cpu().numpy()
     params = params_d.cpu().numpy()
     objmin = objmin_d.cpu().numpy()
@@ -374,8 +378,10 @@ def main():
         "data": "synthetic (seeded speckle pair rendered on the GPU; no public dataset)",
         "config": bench_config(W, world),
         # per step: outputs initialised, ranks, and for the dataflow schedule the
-        # dependency count, prefix sum, successor fill and ready queue; the search
-        "gpu_launches": 7 * args.steps,
+        # dependency count, prefix sum, successor fill and ready queue; the
+        # search (one launch per rank window)
+        "gpu_launches": (6 + search_launches) * args.steps,
+        "launch": launch,
         "device_status": device_status,
         "results": {"good": int(good.sum()), "range_fail": int((status == -1).sum()),
                     "mean_gn_iters": float(its[good].mean()) if good.any() else None,

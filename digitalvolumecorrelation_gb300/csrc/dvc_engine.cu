@@ -164,9 +164,19 @@ __global__ void objective_kernel(int fcn, int n, const double *r, const double *
 // ------------------------------------------- dataflow scheduling set-up ---
 // Edge (i = order[r], m = neigh[i][j]) is a dependency of i when the reference
 // processes m before i (rank[m] < r): Search::starting_param then reads m's
-// result (Core/Search.cpp:297-356).
+// result (Core/Search.cpp:297-356). The ranks may be cut into up to three
+// windows, [0, w1), [w1, w2), [w2, n_process), searched by consecutive
+// launches: only edges inside one window are kept (a predecessor in an
+// earlier window has finished before the window's launch starts).
+__host__ __device__ inline int rank_window(int r, int w1, int w2) { return (r >= w1) + (r >= w2); }
+// the window's work counter and ready-queue tail in the control block's ints
+// (int 1 is the error flag)
+__host__ __device__ inline int window_work_int(int w) { return w == 0 ? 0 : 1 + 2 * w; }
+__host__ __device__ inline int window_tail_int(int w) { return 2 + 2 * w; }
+
 __global__ void dep_count_kernel(int n_process, int n_points, int nn, const int *order,
-                                 const int *neigh, const int *rank, int *pend, int *succ_cnt) {
+                                 const int *neigh, const int *rank, int w1, int w2, int *pend,
+                                 int *succ_cnt) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (long long)n_process * nn) return;
   const int r = (int)(k / nn), j = (int)(k % nn);
@@ -174,13 +184,14 @@ __global__ void dep_count_kernel(int n_process, int n_points, int nn, const int 
   if (i < 0 || i >= n_points) return;
   const int m = neigh[(size_t)i * nn + j];
   if (m < 0 || m >= n_points || rank[m] >= r) return;
+  if (rank_window(rank[m], w1, w2) != rank_window(r, w1, w2)) return;
   atomicAdd(pend + i, 1);
   atomicAdd(succ_cnt + m, 1);
 }
 
 __global__ void dep_fill_kernel(int n_process, int n_points, int nn, const int *order,
-                                const int *neigh, const int *rank, const int *succ_off, int *cursor,
-                                int *succ) {
+                                const int *neigh, const int *rank, int w1, int w2, const int *succ_off,
+                                int *cursor, int *succ) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (long long)n_process * nn) return;
   const int r = (int)(k / nn), j = (int)(k % nn);
@@ -188,6 +199,7 @@ __global__ void dep_fill_kernel(int n_process, int n_points, int nn, const int *
   if (i < 0 || i >= n_points) return;
   const int m = neigh[(size_t)i * nn + j];
   if (m < 0 || m >= n_points || rank[m] >= r) return;
+  if (rank_window(rank[m], w1, w2) != rank_window(r, w1, w2)) return;
   succ[succ_off[m] + atomicAdd(cursor + m, 1)] = i;
 }
 
@@ -225,14 +237,17 @@ __global__ void __launch_bounds__(1024) exclusive_scan_kernel(int n, const int *
   if (t == 0) out[n] = carry;
 }
 
-// points without predecessors start the ready queue
-__global__ void ready_kernel(int n_process, int n_points, const int *order, const int *pend,
-                             int *queue, int *tail) {
+// points without predecessors in their window start that window's ready
+// queue (window w's slots begin at its first rank)
+__global__ void ready_kernel(int n_process, int n_points, const int *order, const int *pend, int w1,
+                             int w2, int *queue, int *ctl) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_process) return;
   const int i = order[r];
   if (i < 0 || i >= n_points || pend[i] != 0) return;
-  queue[atomicAdd(tail, 1)] = i;
+  const int w = rank_window(r, w1, w2);
+  const int start = w == 0 ? 0 : (w == 1 ? w1 : w2);
+  queue[start + atomicAdd(ctl + window_tail_int(w), 1)] = i;
 }
 
 __global__ void byteswap16_kernel(uint16_t *v, size_t n) {
@@ -272,6 +287,9 @@ struct dvc_engine {
   int num_sms = 0;
   int cluster = 0;          // CTAs per point (0 = choose per call)
   int last_cluster = 0, last_grid = 0, last_staged = 0, last_smem = 0;
+  // rank windows of the last dataflow search: [0, w1) and [w2, n) at width
+  // last_windows[2], the body at last_cluster
+  int last_windows[3] = {0, 0, 0};
 };
 
 // Several configurations on the same volumes, one launch shape for all.
@@ -808,10 +826,14 @@ int check_run(const dvc_engine *e, const RunIO &io) {
 // The run's scratch and per-call preparation, enqueued on `st`: scratch in
 // engine e's grow-only workspace (or `ws_fixed`), outputs initialised, ranks
 // of the processing order, and with dataflow scheduling the predecessor
-// counts, successor lists and ready queue. Fills the run fields of `a`.
+// counts, successor lists and ready queues of the rank windows [0, w1),
+// [w1, w2), [w2, n_process) (w1 = w2 = n_process: one window). Fills the run
+// fields of `a` for window 0 (run_window gives the others).
 int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed, size_t ws_fixed_bytes,
-                SearchArgs &a) {
+                SearchArgs &a, int w1, int w2) {
   const int n_points = io.n_points, n_process = io.n_process, n_neigh = io.n_neigh;
+  w2 = std::max(0, std::min(w2, n_process));
+  w1 = std::max(0, std::min(w1, w2));
   // workspace: the control block (kCtlBytes: work counter, error flag, queue
   // tail, counters from +kCountersOff), done[n], rank[n]; with dataflow
   // scheduling also the predecessor counts, successor lists and ready queue.
@@ -857,11 +879,12 @@ int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed,
     CUDA_TRY(cudaMemsetAsync(queue, 0xFF, (size_t)n_process * 4, st));       // -1: slot empty
     const long long edges = (long long)n_process * n_neigh;
     const unsigned eg = (unsigned)((edges + T - 1) / T);
-    dep_count_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, io.order, io.neigh, rank, pend, soff);
+    dep_count_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, io.order, io.neigh, rank, w1, w2, pend,
+                                       soff);
     exclusive_scan_kernel<<<1, 1024, 0, st>>>(n_points, soff, soff);
-    dep_fill_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, io.order, io.neigh, rank, soff, cursor,
-                                      (int *)(ws + off_succ));
-    ready_kernel<<<(n_process + T - 1) / T, T, 0, st>>>(n_process, n_points, io.order, pend, queue, ctl + 2);
+    dep_fill_kernel<<<eg, T, 0, st>>>(n_process, n_points, n_neigh, io.order, io.neigh, rank, w1, w2, soff,
+                                      cursor, (int *)(ws + off_succ));
+    ready_kernel<<<(n_process + T - 1) / T, T, 0, st>>>(n_process, n_points, io.order, pend, w1, w2, queue, ctl);
     CUDA_TRY(cudaGetLastError());
   }
   a.ref = e->ref;
@@ -891,11 +914,73 @@ int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed,
     a.succ_off = (const int *)(ws + off_soff);
     a.succ = (const int *)(ws + off_succ);
     a.queue = (int *)(ws + off_queue);
-    a.queue_tail = ctl + 2;
+    a.queue_tail = ctl + window_tail_int(0);
+    a.n_process = std::min(n_process, w1);
   }
   a.done = done;
   a.counters = (unsigned long long *)(ws + off_ctl + kCountersOff);
   a.wait_polls = e->wait_polls < 0 ? kWaitPolls : e->wait_polls;
+  return DVC_OK;
+}
+
+// The run fields of prepare_run's `a0` (window 0) moved to rank window w of
+// a dataflow run: its work counter, ready-queue slots and tail, its size.
+SearchArgs window_args(const SearchArgs &a0, int w, int w1, int w2, int n_process) {
+  SearchArgs a = a0;
+  int *ctl = a0.work_counter;  // window 0's work counter is the control block's first int
+  const int lo = w == 0 ? 0 : (w == 1 ? w1 : w2);
+  const int hi = w == 0 ? w1 : (w == 1 ? w2 : n_process);
+  a.work_counter = ctl + window_work_int(w);
+  a.queue = a0.queue + lo;
+  a.queue_tail = ctl + window_tail_int(w);
+  a.n_process = hi - lo;
+  return a;
+}
+
+// Launch shape of engine e's search at cluster width C: the configuration,
+// the staging of the correlate region, tensor maps, dynamic shared memory and
+// how many clusters fit at once.
+struct SearchShape {
+  int C = 0, cap = 0, max_clusters = 0;
+  SearchCfg k{};
+  size_t stage_bytes = 0, smem = 0;
+  CUtensorMap tmap, tmap_ref;
+};
+
+// With `grow`, C doubles (up to 8) while the per-CTA state does not fit or the
+// correlate region cannot be staged; without it the shape is C's or none
+// (DVC_E_ARG, no message).
+int search_shape(dvc_engine *e, int C, bool grow, int seed_mode, size_t budget, bool tma_ok, cudaStream_t st,
+                 SearchShape &s) {
+  for (;;) {
+    s.cap = fill_config(e, C, s.k);
+    s.stage_bytes = tma_ok ? stage_config(e, C, budget, state_bytes(s.cap), seed_mode != DVC_SEED_PARAMS, s.k) : 0;
+    const size_t need = s.stage_bytes + state_bytes(s.cap);
+    const bool short_of = (tma_ok && !s.stage_bytes) || need > budget;
+    if (short_of && grow && C < 8) {
+      C *= 2;
+      continue;
+    }
+    if (need > budget) return grow ? set_error(DVC_E_ARG, "subvolume too large for the search kernel") : DVC_E_ARG;
+    if (short_of && !grow) return DVC_E_ARG;
+    break;
+  }
+  memset(&s.tmap, 0, sizeof s.tmap);
+  memset(&s.tmap_ref, 0, sizeof s.tmap_ref);
+  if (s.stage_bytes && !(encode_stage_map(e, s.k.stage, e->cor, &s.tmap) &&
+                         encode_stage_map(e, s.k.stage_ref, e->ref, &s.tmap_ref))) {
+    if (!grow) return DVC_E_ARG;
+    s.k = SearchCfg{};
+    s.cap = fill_config(e, C, s.k);
+    s.stage_bytes = 0;
+  }
+  s.C = C;
+  s.smem = s.stage_bytes + state_bytes(s.cap);
+  SearchArgs probe{};
+  const int rc = dispatch_launch(e->p.bytes_per_voxel, e->p.interp_type, probe, s.tmap, s.tmap_ref, s.smem, 0, C,
+                                 st, &s.max_clusters);
+  if (rc) return rc;
+  if (s.max_clusters < 1) return grow ? set_error(DVC_E_ARG, "search kernel cluster does not fit") : DVC_E_ARG;
   return DVC_OK;
 }
 
@@ -1050,54 +1135,77 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
     C = 1;
     while (C < 8 && e->n_sub / (2 * C) >= per) C *= 2;
   }
-  SearchCfg k;
-  int cap = 0;
-  size_t stage_bytes = 0;
-  for (;;) {
-    cap = fill_config(e, C, k);
-    stage_bytes = tma_ok ? stage_config(e, C, budget, state_bytes(cap), seed_mode != DVC_SEED_PARAMS, k) : 0;
-    const size_t need = stage_bytes + state_bytes(cap);
-    if (((tma_ok && !stage_bytes) || need > budget) && C < 8) {
-      C *= 2;
-      continue;
-    }
-    if (need > budget) return set_error(DVC_E_ARG, "subvolume too large for the search kernel");
-    break;
-  }
-  CUtensorMap tmap, tmap_ref;
-  memset(&tmap, 0, sizeof tmap);
-  memset(&tmap_ref, 0, sizeof tmap_ref);
-  if (stage_bytes && !(encode_stage_map(e, k.stage, e->cor, &tmap) && encode_stage_map(e, k.stage_ref, e->ref, &tmap_ref))) {
-    k = SearchCfg{};
-    cap = fill_config(e, C, k);
-    stage_bytes = 0;
-  }
-  const size_t smem_dyn = stage_bytes + state_bytes(cap);
-  int max_clusters = 0;
-  SearchArgs probe{};
-  rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, probe, tmap, tmap_ref, smem_dyn, 0, C, st, &max_clusters);
+  SearchShape base;
+  rc = search_shape(e, C, true, seed_mode, budget, tma_ok, st, base);
   if (rc) return rc;
-  if (max_clusters < 1) return set_error(DVC_E_ARG, "search kernel cluster does not fit");
-  const int grid = C * std::max(1, std::min(max_clusters, n_process));
+
+  // With the reference's seeding the points form a dependency graph that
+  // grows from the starting point: at first, and again at the end of the
+  // processing order, fewer points are ready than clusters wait for them, and
+  // the run follows a chain of points one after another. There clusters of
+  // twice the width search a point in about 0.54 of the time (measured with
+  // 4 and 8 CTAs on 4000 samples). So with the launch shape chosen here the
+  // ranks are cut into three windows searched by consecutive launches: the
+  // first K1 points at twice the width, the body at this width, the last R
+  // at twice the width, K1 = 84 and R = 28 points per resident cluster of
+  // the body's shape (a model of the scheduling over the graph of 60,800
+  // grid points and their 75 neighbours puts the best cuts there: 10%
+  // shorter than one launch). Each point's width is a function of its rank,
+  // so results do not depend on timing. DVC_WINDOWS=K1,R sets the cuts
+  // (0,0: one launch).
+  int w1 = n_process, w2 = n_process;
+  SearchShape wide;
+  const bool dataflow = seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !ws_fixed && !getenv("DVC_IN_ORDER");
+  if (dataflow && e->cluster <= 0 && (base.C == 2 || base.C == 4)) {
+    long long K1 = 84LL * base.max_clusters, R = 28LL * base.max_clusters;
+    bool forced = false;
+    if (const char *v = getenv("DVC_WINDOWS")) {
+      long long a1 = 0, a2 = 0;
+      if (sscanf(v, "%lld,%lld", &a1, &a2) == 2 && a1 >= 0 && a2 >= 0) {
+        K1 = a1;
+        R = a2;
+        forced = true;
+      }
+    }
+    if ((K1 > 0 || R > 0) && (forced || n_process > K1 + R) &&
+        search_shape(e, 2 * base.C, false, seed_mode, budget, tma_ok, st, wide) == DVC_OK) {
+      w1 = (int)std::min<long long>(K1, n_process);
+      w2 = (int)std::max<long long>(w1, n_process - R);
+    }
+  }
 
   SearchArgs a{};
-  rc = prepare_run(e, io, st, ws_fixed, ws_fixed_bytes, a);
+  rc = prepare_run(e, io, st, ws_fixed, ws_fixed_bytes, a, w1, w2);
   if (rc) return rc;
   if (n_process == 0) return DVC_OK;
-  a.cfg0 = k;
   a.n_cfg = 1;
-  a.local_cap = cap;
-  a.stage_bytes = (int)stage_bytes;
-  if (getenv("DVC_VERBOSE"))
-    fprintf(stderr, "dvc search: %d points, cluster %d, grid %d CTAs, staged %d (box %d x %d x %d), "
-            "dynamic smem %zu of %zu, samples/CTA <= %d, grid step %s\n", n_process, C, grid,
-            k.stage_on ? (k.stage_slab ? 2 : 1) : 0, k.stage[0], k.stage[1], k.stage[2], smem_dyn, budget, cap,
-            k.inc_int ? "integral" : (k.do_grid ? "general" : "none"));
-  e->last_cluster = C;
+  const int n_win = (w1 < n_process || w2 < n_process) ? 3 : 1;
+  for (int w = 0; w < n_win; w++) {
+    const SearchShape &sh = (n_win == 3 && w != 1) ? wide : base;
+    SearchArgs aw = n_win == 3 ? window_args(a, w, w1, w2, n_process) : a;
+    if (aw.n_process == 0) continue;
+    aw.cfg0 = sh.k;
+    aw.local_cap = sh.cap;
+    aw.stage_bytes = (int)sh.stage_bytes;
+    const int grid = sh.C * std::max(1, std::min(sh.max_clusters, aw.n_process));
+    if (getenv("DVC_VERBOSE"))
+      fprintf(stderr, "dvc search: %d points (window %d of %d), cluster %d, grid %d CTAs, staged %d "
+              "(box %d x %d x %d), dynamic smem %zu of %zu, samples/CTA <= %d, grid step %s\n", aw.n_process, w,
+              n_win, sh.C, grid, sh.k.stage_on ? (sh.k.stage_slab ? 2 : 1) : 0, sh.k.stage[0], sh.k.stage[1],
+              sh.k.stage[2], sh.smem, budget, sh.cap,
+              sh.k.inc_int ? "integral" : (sh.k.do_grid ? "general" : "none"));
+    rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, aw, sh.tmap, sh.tmap_ref, sh.smem, grid, sh.C, st, nullptr);
+    if (rc) return rc;
+  }
+  const int grid = base.C * std::max(1, std::min(base.max_clusters, n_process));
+  e->last_cluster = base.C;
   e->last_grid = grid;
-  e->last_staged = k.stage_on ? (k.stage_slab ? 2 : 1) : 0;
-  e->last_smem = (int)smem_dyn;
-  return dispatch_launch(p.bytes_per_voxel, p.interp_type, a, tmap, tmap_ref, smem_dyn, grid, C, st, nullptr);
+  e->last_staged = base.k.stage_on ? (base.k.stage_slab ? 2 : 1) : 0;
+  e->last_smem = (int)base.smem;
+  e->last_windows[0] = w1;
+  e->last_windows[1] = w2;
+  e->last_windows[2] = n_win == 3 ? wide.C : base.C;
+  return DVC_OK;
 }
 
 
@@ -1439,7 +1547,7 @@ int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_
   if (n_points == 0) return DVC_OK;
   cudaStream_t st = (cudaStream_t)stream;
   SearchArgs a{};
-  rc = prepare_run(e, io, st, nullptr, 0, a);
+  rc = prepare_run(e, io, st, nullptr, 0, a, n_process, n_process);
   if (rc) return rc;
   if (n_process == 0) return DVC_OK;
   const int n = (int)plan->cfgs.size();
@@ -1532,6 +1640,12 @@ int dvc_gpu_last_launch(dvc_engine *e, int out[4]) {
   out[1] = e->last_grid;
   out[2] = e->last_staged;
   out[3] = e->last_smem;
+  return DVC_OK;
+}
+
+int dvc_gpu_last_windows(dvc_engine *e, int out[3]) {
+  if (!e || !out) return set_error(DVC_E_ARG, "null argument");
+  for (int k = 0; k < 3; k++) out[k] = e->last_windows[k];
   return DVC_OK;
 }
 

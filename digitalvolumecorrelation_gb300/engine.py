@@ -81,6 +81,7 @@ def load(path: str | None = None):
     L.dvc_gpu_order_neighbours.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip]
     L.dvc_gpu_set_cluster.argtypes = [C.c_void_p, C.c_int]
     L.dvc_gpu_last_launch.argtypes = [C.c_void_p, _ip]
+    L.dvc_gpu_last_windows.argtypes = [C.c_void_p, _ip]
     L.dvc_gpu_read_mhd.argtypes = [C.c_char_p, C.POINTER(DvcVolumeInfo)]
     L.dvc_gpu_load_raw.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.c_int, C.c_void_p]
@@ -213,6 +214,14 @@ class Engine:
         out = (C.c_int * 4)()
         _check(_lib.dvc_gpu_last_launch(self._h, out))
         return dict(cluster=out[0], ctas=out[1], staging=out[2], smem_bytes=out[3])
+
+    def last_windows(self):
+        """(w1, w2, width) of the most recent search with the reference's
+        seeding: ranks [0, w1) and [w2, n) searched at `width` CTAs per point,
+        the ranks between at last_launch()["cluster"]; w1 = w2 = n: one launch."""
+        out = (C.c_int * 3)()
+        _check(_lib.dvc_gpu_last_windows(self._h, out))
+        return tuple(out)
 
     def last_counters(self):
         """(evaluations, Gauss-Newton iterations, undefined-cell evaluations)

@@ -266,6 +266,16 @@ int dvc_gpu_set_cluster(dvc_engine *e, int cluster);
    translations), out[3] dynamic shared memory per CTA in bytes. */
 int dvc_gpu_last_launch(dvc_engine *e, int out[4]);
 
+/* Rank windows of this engine's most recent search with the reference's
+   seeding (dataflow scheduled, cluster width chosen by the engine): the
+   ranks [0, out[0]) and [out[1], n_process) were searched by launches of
+   out[2] CTAs per point, the ranks between them at out[0] of
+   dvc_gpu_last_launch. out[0] = out[1] = n_process: one launch. Each window
+   is a launch of its own after the previous one (a point's predecessors in
+   an earlier window have finished); a point's cluster width follows from its
+   rank alone, so results do not depend on timing. */
+int dvc_gpu_last_windows(dvc_engine *e, int out[3]);
+
 /* Counters of the most recent dvc_gpu_process / dvc_gpu_process_device call
    on this engine (waits for it to finish): out[0] objective evaluations
    (reference subvolume, grid offsets, Gauss-Newton evaluations, final

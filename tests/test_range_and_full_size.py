@@ -135,6 +135,36 @@ def test_range_fail_at_other_cluster_widths(gpu_lib, monkeypatch, cluster):
         E.close()
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["sphere41_4000_12dof", "cube41_3375_12dof", "strain_12dof"])
+def test_rank_windows_match_reference_and_repeat_bit_for_bit(gpu_lib, monkeypatch, name):
+    """The dataflow search cut into three rank windows (the first and last
+    ranks at twice the body's cluster width, consecutive launches): the
+    reference's statuses and parameters as before, and a second run gives the
+    same bits (a point's width follows from its rank, not from timing)."""
+    from digitalvolumecorrelation_gb300 import engine
+    monkeypatch.setenv("DVC_WINDOWS", "5,6")
+    ref, cor = volumes(name)
+    g = CASES[name]
+    case = recipes.by_name(name)
+    E = engine.Engine(recipes.params(case), ref, cor)
+    runs = []
+    for _ in range(2):
+        runs.append(E.process(recipes.points(case), order=np.array(g["order"], np.int32),
+                              neigh=np.array(g["neigh"], np.int32)))
+        n = len(g["status"])
+        body = E.last_launch()["cluster"]
+        assert body in (2, 4)
+        assert E.last_windows() == (5, n - 6, 2 * body)
+        compare(name, runs[-1])
+    for k in ("status", "objmin", "params"):
+        np.testing.assert_array_equal(runs[0][k], runs[1][k])
+    monkeypatch.setenv("DVC_WINDOWS", "0,0")
+    E.process(recipes.points(case), order=np.array(g["order"], np.int32), neigh=np.array(g["neigh"], np.int32))
+    assert E.last_windows() == (n, n, E.last_launch()["cluster"])
+    E.close()
+
+
 @pytest.fixture(scope="module")
 def dvc_bin():
     from digitalvolumecorrelation_gb300 import build

@@ -548,10 +548,10 @@ int ensure_ws(dvc_engine *e, size_t bytes) {
   return DVC_OK;
 }
 
-template <typename VT, int IT>
+template <typename VT, int IT, int MINB>
 int launch_search(SearchArgs &a, const CUtensorMap &tmap, const CUtensorMap &tmap_ref, size_t smem_dyn,
                   int grid, int cluster, cudaStream_t st, int *max_clusters) {
-  auto kern = search_kernel<VT, IT>;
+  auto kern = search_kernel<VT, IT, MINB>;
   CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dyn));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -622,16 +622,22 @@ void stage_dims(const dvc_engine *e, int C, int esize, double reach, const int r
   out[0] = units * al;
 }
 
+// minb 2: the kernel whose registers leave room for two CTAs per SM
+// (tricubic only)
 int dispatch_launch(int bpv, int it, SearchArgs &a, const CUtensorMap &tm, const CUtensorMap &tmr, size_t smem,
-                    int grid, int cluster, cudaStream_t st, int *max_clusters) {
-  if (bpv == 1) {
-    if (it == 2) return launch_search<uint8_t, 2>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
-    if (it == 1) return launch_search<uint8_t, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
-    return launch_search<uint8_t, 0>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+                    int grid, int cluster, cudaStream_t st, int *max_clusters, int minb = 1) {
+  if (minb == 2 && it == 2) {
+    if (bpv == 1) return launch_search<uint8_t, 2, 2>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+    return launch_search<uint16_t, 2, 2>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
   }
-  if (it == 2) return launch_search<uint16_t, 2>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
-  if (it == 1) return launch_search<uint16_t, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
-  return launch_search<uint16_t, 0>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+  if (bpv == 1) {
+    if (it == 2) return launch_search<uint8_t, 2, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+    if (it == 1) return launch_search<uint8_t, 1, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+    return launch_search<uint8_t, 0, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+  }
+  if (it == 2) return launch_search<uint16_t, 2, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+  if (it == 1) return launch_search<uint16_t, 1, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
+  return launch_search<uint16_t, 0, 1>(a, tm, tmr, smem, grid, cluster, st, max_clusters);
 }
 
 // ---- launch preparation ------------------------------------------------------
@@ -942,6 +948,7 @@ SearchArgs window_args(const SearchArgs &a0, int w, int w1, int w2, int n_proces
 // how many clusters fit at once.
 struct SearchShape {
   int C = 0, cap = 0, max_clusters = 0;
+  int minb = 1;  // CTAs per SM the kernel's registers are sized for
   SearchCfg k{};
   size_t stage_bytes = 0, smem = 0;
   CUtensorMap tmap, tmap_ref;
@@ -981,6 +988,29 @@ int search_shape(dvc_engine *e, int C, bool grow, int seed_mode, size_t budget, 
                                  st, &s.max_clusters);
   if (rc) return rc;
   if (s.max_clusters < 1) return grow ? set_error(DVC_E_ARG, "search kernel cluster does not fit") : DVC_E_ARG;
+  return DVC_OK;
+}
+
+// The shape with two CTAs resident per SM at width C, for searches without a
+// coarse grid (start parameters given): the correlate region is read through
+// L1 (no staging box), and the kernel's registers are sized for two CTAs, so
+// one point's serial sections (reductions, the one-warp solve) overlap the
+// other's sample evaluations. DVC_E_ARG (no message) when fewer than about
+// two CTAs per SM fit.
+int search_shape_pair(dvc_engine *e, int C, cudaStream_t st, SearchShape &s) {
+  if (e->p.interp_type != DVC_TRICUBIC) return DVC_E_ARG;
+  s.cap = fill_config(e, C, s.k);
+  s.stage_bytes = 0;
+  memset(&s.tmap, 0, sizeof s.tmap);
+  memset(&s.tmap_ref, 0, sizeof s.tmap_ref);
+  s.C = C;
+  s.minb = 2;
+  s.smem = state_bytes(s.cap);
+  SearchArgs probe{};
+  const int rc = dispatch_launch(e->p.bytes_per_voxel, e->p.interp_type, probe, s.tmap, s.tmap_ref, s.smem, 0, C,
+                                 st, &s.max_clusters, 2);
+  if (rc) return rc;
+  if ((long long)s.max_clusters * C < 3LL * e->num_sms / 2) return DVC_E_ARG;
   return DVC_OK;
 }
 
@@ -1174,6 +1204,20 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
     }
   }
 
+  // Independent points without a coarse grid (start parameters given, or
+  // no basin) and Gauss-Newton: two CTAs per SM at the same width, the
+  // correlate region read through L1 (config 5's learned search: 1.46 ->
+  // 1.30 s for 499,200 points). The same search; the kernel compiled for two
+  // CTAs may fuse multiplies and adds differently, so results can differ in
+  // the last FP32 bits. DVC_PAIR=0: one CTA per SM with staging.
+  SearchShape pair;
+  bool use_pair = false;
+  const bool no_grid = seed_mode == DVC_SEED_PARAMS || (seed_mode != DVC_SEED_NEIGHBOURS && p.basin_radius == 0.0);
+  if (no_grid && p.refine_method == DVC_REFINE_GAUSS_NEWTON && e->cluster <= 0) {
+    const char *v = getenv("DVC_PAIR");
+    if (!(v && atoi(v) == 0)) use_pair = search_shape_pair(e, base.C, st, pair) == DVC_OK;
+  }
+
   SearchArgs a{};
   rc = prepare_run(e, io, st, ws_fixed, ws_fixed_bytes, a, w1, w2);
   if (rc) return rc;
@@ -1181,7 +1225,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   a.n_cfg = 1;
   const int n_win = (w1 < n_process || w2 < n_process) ? 3 : 1;
   for (int w = 0; w < n_win; w++) {
-    const SearchShape &sh = (n_win == 3 && w != 1) ? wide : base;
+    const SearchShape &sh = use_pair ? pair : ((n_win == 3 && w != 1) ? wide : base);
     SearchArgs aw = n_win == 3 ? window_args(a, w, w1, w2, n_process) : a;
     if (aw.n_process == 0) continue;
     aw.cfg0 = sh.k;
@@ -1194,14 +1238,16 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
               n_win, sh.C, grid, sh.k.stage_on ? (sh.k.stage_slab ? 2 : 1) : 0, sh.k.stage[0], sh.k.stage[1],
               sh.k.stage[2], sh.smem, budget, sh.cap,
               sh.k.inc_int ? "integral" : (sh.k.do_grid ? "general" : "none"));
-    rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, aw, sh.tmap, sh.tmap_ref, sh.smem, grid, sh.C, st, nullptr);
+    rc = dispatch_launch(p.bytes_per_voxel, p.interp_type, aw, sh.tmap, sh.tmap_ref, sh.smem, grid, sh.C, st, nullptr,
+                         sh.minb);
     if (rc) return rc;
   }
-  const int grid = base.C * std::max(1, std::min(base.max_clusters, n_process));
-  e->last_cluster = base.C;
+  const SearchShape &body = use_pair ? pair : base;
+  const int grid = body.C * std::max(1, std::min(body.max_clusters, n_process));
+  e->last_cluster = body.C;
   e->last_grid = grid;
-  e->last_staged = base.k.stage_on ? (base.k.stage_slab ? 2 : 1) : 0;
-  e->last_smem = (int)base.smem;
+  e->last_staged = body.k.stage_on ? (body.k.stage_slab ? 2 : 1) : 0;
+  e->last_smem = (int)body.smem;
   e->last_windows[0] = w1;
   e->last_windows[1] = w2;
   e->last_windows[2] = n_win == 3 ? wide.C : base.C;
@@ -1722,6 +1768,41 @@ __global__ void seeds3_kernel(int n, const double *p12, double *p3) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n * 3) p3[t] = p12[(size_t)(t / 3) * 12 + t % 3];
 }
+// Locality order for independent points: each point's bucket is the Morton
+// code of its cell (cells of `cell` voxels, `bits` bits per axis), counted,
+// scanned and scattered. Points whose searches run at the same time then
+// read overlapping volume regions (L1 and L2 reuse); within a bucket the
+// order is that of the atomic scatter.
+__device__ __forceinline__ unsigned spread3(unsigned v) {  // bit k -> bit 3k (v < 2^10)
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__global__ void cell_key_kernel(int n, const int *order, const double *pts, double cell, int bits, int *key,
+                                int *count) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int i = order[r];
+  const unsigned lim = (1u << bits) - 1u;
+  unsigned c[3];
+  for (int d = 0; d < 3; d++) {
+    const double v = floor(pts[(size_t)i * 3 + d] / cell);
+    c[d] = v < 0.0 ? 0u : (v > (double)lim ? lim : (unsigned)v);
+  }
+  const int k = (int)(spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2));
+  key[r] = k;
+  atomicAdd(count + k, 1);
+}
+__global__ void cell_scatter_kernel(int n, const int *order, const int *key, const int *start, int *cursor,
+                                    int *out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int k = key[r];
+  out[start[k] + atomicAdd(cursor + k, 1)] = order[r];
+}
 // results of the points in list, from the second search's arrays
 __global__ void merge_kernel(int n, const int *list, const int *st2, const double *ob2, const double *pa2,
                              const int *it2, int *st, double *ob, double *pa, int *it) {
@@ -1753,22 +1834,59 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
   const size_t N = (size_t)n_points;
   double *p12 = nullptr, *p3 = nullptr, *ob2 = nullptr, *pa2 = nullptr;
   int *list = nullptr, *cnt = nullptr, *st2 = nullptr, *it2 = nullptr;
+  int *lord = nullptr, *lkey = nullptr, *lcount = nullptr;
   int rc = DVC_OK, nfb = 0;
   auto cleanup = [&]() {
     cudaFree(p12); cudaFree(p3); cudaFree(ob2); cudaFree(pa2);
     cudaFree(list); cudaFree(cnt); cudaFree(st2); cudaFree(it2);
+    cudaFree(lord); cudaFree(lkey); cudaFree(lcount);
   };
+  // the points' cells: 32 voxels or more, at most 64 per axis (Morton keys
+  // of 18 bits)
+  const int vmax = std::max(e->p.vol_wide, std::max(e->p.vol_high, e->p.vol_tall));
+  double cell = 32.0;
+  while (vmax / cell > 64.0) cell *= 2.0;
+  int bits = 0;
+  while ((1 << bits) < (int)std::ceil(vmax / cell)) bits++;
+  const int nb = 1 << (3 * bits);
   if (cudaMalloc(&p12, N * 12 * 8) != cudaSuccess || cudaMalloc(&p3, N * 3 * 8) != cudaSuccess ||
-      cudaMalloc(&list, (size_t)n_process * 4) != cudaSuccess || cudaMalloc(&cnt, 4) != cudaSuccess) {
+      cudaMalloc(&list, (size_t)n_process * 4) != cudaSuccess || cudaMalloc(&cnt, 4) != cudaSuccess ||
+      cudaMalloc(&lord, (size_t)n_process * 4) != cudaSuccess ||
+      cudaMalloc(&lkey, (size_t)n_process * 4) != cudaSuccess ||
+      cudaMalloc(&lcount, (size_t)(2 * nb + 1) * 4) != cudaSuccess) {
     cleanup();
     return set_error(DVC_E_NOMEM, "learned search buffers");
   }
+  // the points in locality order: the network passes and the search take them
+  // in it (every point's result is independent of the order)
+  {
+    int *start = lcount + nb, *cursor = lcount;
+    const unsigned g = (unsigned)((n_process + 255) / 256);
+    cudaMemsetAsync(lcount, 0, (size_t)nb * 4, st);
+    cell_key_kernel<<<g, 256, 0, st>>>(n_process, order_dev, points_dev, cell, bits, lkey, lcount);
+    exclusive_scan_kernel<<<1, 1024, 0, st>>>(nb, lcount, start);
+    cudaMemsetAsync(cursor, 0, (size_t)nb * 4, st);
+    cell_scatter_kernel<<<g, 256, 0, st>>>(n_process, order_dev, lkey, start, cursor, lord);
+    if (cudaGetLastError() != cudaSuccess) {
+      cleanup();
+      return set_error(DVC_E_CUDA, "locality order");
+    }
+    order_dev = lord;
+  }
+  // DVC_VERBOSE: device time of the network passes, the search and the fallback
+  const bool verbose = getenv("DVC_VERBOSE") != nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (verbose)
+    for (auto &x : ev) cudaEventCreate(&x);
+  if (verbose) cudaEventRecord(ev[0], st);
   cudaMemsetAsync(p12, 0, N * 12 * 8, st);
   rc = dvc_internal_cnn_seed(net, e->ref, e->cor, e->p.bytes_per_voxel, e->p.vol_wide, e->p.vol_high,
                              e->p.vol_tall, n_process, points_dev, order_dev, p12, st);
+  if (verbose) cudaEventRecord(ev[1], st);
   if (!rc)
     rc = process_device_ws(e, n_points, points_dev, n_process, order_dev, 0, nullptr, DVC_SEED_PARAMS, p12,
                            status_dev, objmin_dev, params_dev, gn_iters_dev, stream, nullptr);
+  if (verbose) cudaEventRecord(ev[2], st);
   if (!rc) {
     cudaMemsetAsync(cnt, 0, 4, st);
     fallback_kernel<<<(n_process + 255) / 256, 256, 0, st>>>(n_process, order_dev, status_dev, objmin_dev,
@@ -1795,7 +1913,16 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
       merge_kernel<<<(nfb + 255) / 256, 256, 0, st>>>(nfb, list, st2, ob2, pa2, it2, status_dev, objmin_dev,
                                                       params_dev, gn_iters_dev);
   }
+  if (verbose) cudaEventRecord(ev[3], st);
   if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = set_error(DVC_E_CUDA, "learned search");
+  if (verbose && !rc) {
+    float ms[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < 3; k++) cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
+    fprintf(stderr, "dvc learned search: %d points, network %.2f ms, search %.2f ms, fallback (%d points) %.2f ms\n",
+            n_process, ms[0], ms[1], nfb, ms[2]);
+  }
+  if (verbose)
+    for (auto &x : ev) cudaEventDestroy(x);
   if (!rc && nfb > 0) rc = launch_error(e);
   if (!rc && nfb > 0) {
     unsigned long long c2[3];

@@ -1274,8 +1274,10 @@ struct PhaseClock {
 };
 
 // ================================================================ kernel ===
-template <typename VT, int IT>
-__global__ void __launch_bounds__(kThreads, 1)
+// MINB: CTAs resident per SM the registers are sized for (1, or 2 for the
+// searches without coarse grid that run two points per SM side by side)
+template <typename VT, int IT, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
     search_kernel(const __grid_constant__ SearchArgs a, const __grid_constant__ CUtensorMap tmap,
                   const __grid_constant__ CUtensorMap tmap_ref) {
   extern __shared__ __align__(128) unsigned char dsm[];

@@ -160,6 +160,47 @@ def test_given_seed_mode_vs_oracle(eng, oracle):
         E.close()
 
 
+def test_two_ctas_per_sm_match_one(eng, monkeypatch):
+    """Searches without a coarse grid from independent starts run two CTAs per
+    SM, the correlate region read through L1 instead of a staged box: the
+    same search as one CTA per SM with staging (12 start parameters given;
+    translation seeds without a basin). The two are separate compilations of
+    the kernel (registers for one or two CTAs), and the compiler may fuse a
+    multiply and an add differently in each: statuses identical, objmin
+    within 2e-6 relative, parameters within 1e-5."""
+    from digitalvolumecorrelation_gb300 import synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    rng = np.random.default_rng(19)
+    shape = (80, 80, 80)  # 80-byte rows: the one-CTA shape stages its region by TMA
+    b = synth.blobs(shape, 650, seed=61)
+    aff = synth.Affine(t=(0.8, -1.4, 2.1), E=((0.004, 0.001, 0), (0, -0.003, 0), (0, 0, 0.006)),
+                       c=(40.0, 40.0, 40.0))
+    ref = synth.render(shape, b, noise_sigma=2.0, noise_seed=62)
+    cor = synth.render(shape, b, deform=aff, noise_sigma=2.0, noise_seed=63)
+    pts = synth.grid_points((4, 4, 4), 7.0, (40.0, 40.0, 40.0))
+    p12 = np.zeros((len(pts), 12))
+    p12[:, :3] = aff.u(pts) + rng.normal(0, 0.6, pts.shape)
+    p12[:, 6:9] = rng.normal(0, 0.003, (len(pts), 3))
+    for kw, mode, seeds in ((dict(subvol_geom="cube", subvol_size=19, subvol_npts=2200, num_srch_dof=12,
+                                  disp_max=4, basin_radius=2.0), eng.SEED_PARAMS, p12),
+                            (dict(subvol_geom="sphere", subvol_size=21, subvol_npts=2500, num_srch_dof=6,
+                                  disp_max=4, basin_radius=0.0), eng.SEED_GIVEN, p12[:, :3].copy())):
+        E = eng.Engine(make_params(shape, **kw), ref, cor)
+        out = {}
+        for pair in ("0", "1"):
+            monkeypatch.setenv("DVC_PAIR", pair)
+            out[pair] = E.process(pts, seed_mode=mode, seeds=seeds)
+            out[pair + "launch"] = E.last_launch()
+        assert out["1launch"]["cluster"] == out["0launch"]["cluster"]
+        assert out["1launch"]["staging"] == 0 and out["0launch"]["staging"] != 0
+        assert (out["1"]["status"] == 0).sum() >= 50
+        np.testing.assert_array_equal(out["1"]["status"], out["0"]["status"])
+        good = out["0"]["status"] == 0
+        np.testing.assert_allclose(out["1"]["objmin"][good], out["0"]["objmin"][good], rtol=2e-6, atol=0)
+        assert np.abs(out["1"]["params"] - out["0"]["params"]).max() <= 1e-5
+        E.close()
+
+
 def test_subvolume_precheck_vs_oracle(eng, oracle):
     """subvol_thresh as the reference's manual documents it (Core/InputRead.cpp:
     282-323): points whose reference samples lie in the gray range for less

@@ -355,6 +355,10 @@ def main():
     grid = (2 * k + 1) ** 3 if p.basin_radius else 0
     good = status == 0
     evals, gn_total, undefined = E.last_counters()  # of the last timed step
+    ph = np.array(E.last_phase_cycles(), float)  # SM cycles per phase, all CTAs, last step
+    phase_names = ("take_work_and_seed", "setup", "grid", "gn_entry_exit", "final", "gn_warp", "gn_range_stage",
+                   "gn_eval", "gn_reduce", "gn_solve")
+    phase_shares = {k: round(float(v / ph[:10].sum()), 4) for k, v in zip(phase_names, ph[:10])} if ph[:10].sum() else {}
     sample_evals = evals * n_sub
     flop_per_sample = 8192.0  # fused 64x64 stencil-coefficient product per sample-evaluation
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
@@ -386,6 +390,9 @@ def main():
         "results": {"good": int(good.sum()), "range_fail": int((status == -1).sum()),
                     "mean_gn_iters": float(its[good].mean()) if good.any() else None,
                     "evaluations": evals, "undefined_cell_evaluations": undefined,
+                    # share of the CTAs' SM cycles per phase of the point loop
+                    # (gn_eval includes the G'G accumulation)
+                    "phase_shares": phase_shares,
                     "max_abs_err_vs_truth_vox": None if err_truth is None else float(err_truth),
                     "median_abs_err_vs_truth_vox": float(np.median(np.abs(params[good, :3] - truth[good])))
                     if good.any() else None},
@@ -714,22 +721,29 @@ def e2e_leg(W, p, order, neigh, ref_d, cor_d, n, iters=3):
     if W.bytes_per_voxel == 2:
         ref_np = ref_np.view(np.uint16)
         cor_np = cor_np.view(np.uint16)
-    times = []
+    times, parts = [], []
     for it in range(1 + iters):  # one untimed warm-up call, then `iters` timed ones
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         E = engine.Engine(p, ref_np, cor_np)
+        t1 = time.perf_counter()
         r = E.process(W.points, order=order, neigh=neigh)
+        t2 = time.perf_counter()
         E.close()
         torch.cuda.synchronize()
-        times.append(time.perf_counter() - t0)
+        t3 = time.perf_counter()
+        times.append(t3 - t0)
+        parts.append((t1 - t0, t2 - t1, t3 - t2))
     dt = statistics.median(times[1:])
     h2d = 2 * W.nvox * W.bytes_per_voxel + W.points.nbytes + order.nbytes + neigh.nbytes
     d2h = n * (4 + 8 + 96 + 4)
     return {"value": round(n / dt, 2), "unit": "points/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "seconds": round(dt, 3),
             "timing": f"median of {iters} calls after one warm-up call",
-            "seconds_each": [round(t, 3) for t in times[1:]]}
+            "seconds_each": [round(t, 3) for t in times[1:]],
+            # per call: engine creation (both volumes uploaded), the search
+            # call (arrays in, search, results out), engine destruction
+            "seconds_create_search_destroy": [[round(v, 3) for v in q] for q in parts[1:]]}
 
 
 def run_reference(args, rank, world):

@@ -32,7 +32,6 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <mutex>
 #include <random>
 #include <string>
 #include <thread>
@@ -1380,75 +1379,6 @@ static int launch_error(dvc_engine *e) {
   return DVC_OK;
 }
 
-// Host arrays cross to and from the device through one process-wide pinned
-// staging buffer (grow-only, kept until the process exits, shared by every
-// engine and device under a lock held only while copies go through it). The
-// caller's arrays are ordinary pageable memory; a pageable copy by the driver
-// was measured to slow the next pinned copies of the same process for a
-// while (a 4 GiB volume upload took 180-290 ms after one instead of 20 ms).
-struct PinnedStage {
-  std::mutex m;
-  char *buf = nullptr;
-  size_t bytes = 0;
-};
-static PinnedStage g_stage;
-
-// One batch of copies between caller arrays and device arrays, through the
-// staging buffer when it can be had (else plain copies); on return the
-// copies are complete.
-struct HostCopy {
-  void *dev;
-  void *host;
-  size_t bytes;
-};
-static cudaError_t stage_copies(const HostCopy *c, int n, cudaMemcpyKind kind) {
-  size_t total = 0;
-  for (int k = 0; k < n; k++) total += (c[k].bytes + 255) & ~(size_t)255;
-  std::lock_guard<std::mutex> lock(g_stage.m);
-  if (total > g_stage.bytes) {
-    if (g_stage.buf) cudaFreeHost(g_stage.buf);
-    g_stage.buf = nullptr;
-    g_stage.bytes = 0;
-    if (cudaHostAlloc((void **)&g_stage.buf, total, cudaHostAllocPortable) == cudaSuccess) {
-      g_stage.bytes = total;
-    } else {
-      cudaGetLastError();
-      g_stage.buf = nullptr;
-    }
-  }
-  if (!g_stage.buf) {
-    for (int k = 0; k < n; k++) {
-      const cudaError_t r = kind == cudaMemcpyHostToDevice ? cudaMemcpy(c[k].dev, c[k].host, c[k].bytes, kind)
-                                                           : cudaMemcpy(c[k].host, c[k].dev, c[k].bytes, kind);
-      if (r != cudaSuccess) return r;
-    }
-    return cudaSuccess;
-  }
-  if (kind == cudaMemcpyDeviceToHost) touch_pages(g_stage.buf, total);
-  size_t off = 0;
-  for (int k = 0; k < n; k++) {
-    char *p = g_stage.buf + off;
-    off += (c[k].bytes + 255) & ~(size_t)255;
-    if (!c[k].bytes) continue;
-    cudaError_t r;
-    if (kind == cudaMemcpyHostToDevice) {
-      memcpy(p, c[k].host, c[k].bytes);
-      r = cudaMemcpyAsync(c[k].dev, p, c[k].bytes, kind, 0);
-    } else {
-      r = cudaMemcpyAsync(p, c[k].dev, c[k].bytes, kind, 0);
-    }
-    if (r != cudaSuccess) return r;
-  }
-  const cudaError_t r = cudaStreamSynchronize(0);
-  if (r != cudaSuccess || kind == cudaMemcpyHostToDevice) return r;
-  off = 0;
-  for (int k = 0; k < n; k++) {
-    if (c[k].bytes) memcpy(c[k].host, g_stage.buf + off, c[k].bytes);
-    off += (c[k].bytes + 255) & ~(size_t)255;
-  }
-  return cudaSuccess;
-}
-
 // Host-array search: arguments checked, arrays copied in, the engine's (or
 // the plan's) device search, results and counters copied out.
 static int host_process(dvc_engine *e, dvc_plan *plan, const int *point_cfg, int n_points,
@@ -1500,25 +1430,20 @@ static int host_process(dvc_engine *e, dvc_plan *plan, const int *point_cfg, int
   TRYC(cudaMalloc(&d_obj, N * sizeof(double)));
   TRYC(cudaMalloc(&d_par, N * 12 * sizeof(double)));
   TRYC(cudaMalloc(&d_its, N * sizeof(int)));
-  {
-    HostCopy in[5];
-    int nin = 0;
-    in[nin++] = {d_pts, const_cast<double *>(points), N * 3 * sizeof(double)};
-    if (n_process) in[nin++] = {d_order, const_cast<int *>(order), n_process * sizeof(int)};
-    if (seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0) {
-      TRYC(cudaMalloc(&d_neigh, N * n_neigh * sizeof(int)));
-      in[nin++] = {d_neigh, const_cast<int *>(neigh), N * n_neigh * sizeof(int)};
-    }
-    if (seed_mode == DVC_SEED_GIVEN || seed_mode == DVC_SEED_PARAMS) {
-      const size_t per = seed_mode == DVC_SEED_GIVEN ? 3 : 12;
-      TRYC(cudaMalloc(&d_seeds, N * per * sizeof(double)));
-      in[nin++] = {d_seeds, const_cast<double *>(seeds), N * per * sizeof(double)};
-    }
-    if (plan) {
-      TRYC(cudaMalloc(&d_cfg, std::max<size_t>(1, N) * sizeof(int)));
-      in[nin++] = {d_cfg, const_cast<int *>(point_cfg), N * sizeof(int)};
-    }
-    TRYC(stage_copies(in, nin, cudaMemcpyHostToDevice));
+  TRYC(cudaMemcpy(d_pts, points, N * 3 * sizeof(double), cudaMemcpyHostToDevice));
+  if (n_process) TRYC(cudaMemcpy(d_order, order, n_process * sizeof(int), cudaMemcpyHostToDevice));
+  if (seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0) {
+    TRYC(cudaMalloc(&d_neigh, N * n_neigh * sizeof(int)));
+    TRYC(cudaMemcpy(d_neigh, neigh, N * n_neigh * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (seed_mode == DVC_SEED_GIVEN || seed_mode == DVC_SEED_PARAMS) {
+    const size_t per = seed_mode == DVC_SEED_GIVEN ? 3 : 12;
+    TRYC(cudaMalloc(&d_seeds, N * per * sizeof(double)));
+    TRYC(cudaMemcpy(d_seeds, seeds, N * per * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (plan) {
+    TRYC(cudaMalloc(&d_cfg, std::max<size_t>(1, N) * sizeof(int)));
+    TRYC(cudaMemcpy(d_cfg, point_cfg, N * sizeof(int), cudaMemcpyHostToDevice));
   }
   TRYC(cudaEventCreate(&ev0));
   TRYC(cudaEventCreate(&ev1));
@@ -1537,13 +1462,10 @@ static int host_process(dvc_engine *e, dvc_plan *plan, const int *point_cfg, int
   unsigned long long counters[3] = {0, 0, 0};
   if (n_process > 0 && e->last_ctl)
     TRYC(cudaMemcpy(counters, e->last_ctl + kCountersOff, sizeof counters, cudaMemcpyDeviceToHost));
-  {
-    HostCopy out[4] = {{d_status, status, N * sizeof(int)},
-                       {d_obj, objmin, N * sizeof(double)},
-                       {d_par, params, N * 12 * sizeof(double)},
-                       {d_its, gn_iters, gn_iters ? N * sizeof(int) : 0}};
-    TRYC(stage_copies(out, 4, cudaMemcpyDeviceToHost));
-  }
+  TRYC(cudaMemcpy(status, d_status, N * sizeof(int), cudaMemcpyDeviceToHost));
+  TRYC(cudaMemcpy(objmin, d_obj, N * sizeof(double), cudaMemcpyDeviceToHost));
+  TRYC(cudaMemcpy(params, d_par, N * 12 * sizeof(double), cudaMemcpyDeviceToHost));
+  if (gn_iters) TRYC(cudaMemcpy(gn_iters, d_its, N * sizeof(int), cudaMemcpyDeviceToHost));
   float kms = 0.f;
   cudaEventElapsedTime(&kms, ev0, ev1);
   cleanup();

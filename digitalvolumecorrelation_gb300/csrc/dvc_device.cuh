@@ -33,7 +33,11 @@
 
 namespace dvc {
 
-constexpr int kThreads = 256;
+// threads per search CTA (DVC_THREADS: a multiple of 32, for experiments)
+#ifndef DVC_THREADS
+#define DVC_THREADS 256
+#endif
+constexpr int kThreads = DVC_THREADS;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxDof = 12;
 

@@ -109,14 +109,15 @@ __global__ void interp_points_kernel(GSrc<VT> V, BoxGeom G, int n, const double 
 
 // ----------------------------------------------------- objective entry ---
 // FP64 two-pass objective (Core/ObjectiveFunctions.cpp:24-263), one CTA.
+constexpr int kObjThreads = 256;
 __global__ void objective_kernel(int fcn, int n, const double *r, const double *t, double *obj,
                                  double *res) {
-  __shared__ double red[kThreads];
+  __shared__ double red[kObjThreads];
   const int tid = threadIdx.x;
   auto bsum = [&](double v) -> double {
     red[tid] = v;
     __syncthreads();
-    for (int s = kThreads / 2; s; s >>= 1) {
+    for (int s = kObjThreads / 2; s; s >>= 1) {
       if (tid < s) red[tid] += red[tid + s];
       __syncthreads();
     }
@@ -127,7 +128,7 @@ __global__ void objective_kernel(int fcn, int n, const double *r, const double *
   double ar = 0, at = 0, sr = 0, st = 0;
   if (fcn == DVC_ZSSD || fcn == DVC_ZNSSD) {
     double a1 = 0, a2 = 0;
-    for (int i = tid; i < n; i += kThreads) {
+    for (int i = tid; i < n; i += kObjThreads) {
       a1 += r[i];
       a2 += t[i];
     }
@@ -136,7 +137,7 @@ __global__ void objective_kernel(int fcn, int n, const double *r, const double *
   }
   if (fcn == DVC_NSSD || fcn == DVC_ZNSSD) {
     double b1 = 0, b2 = 0;
-    for (int i = tid; i < n; i += kThreads) {
+    for (int i = tid; i < n; i += kObjThreads) {
       b1 += (r[i] - ar) * (r[i] - ar);
       b2 += (t[i] - at) * (t[i] - at);
     }
@@ -144,7 +145,7 @@ __global__ void objective_kernel(int fcn, int n, const double *r, const double *
     st = sqrt(bsum(b2));
   }
   double acc = 0;
-  for (int i = tid; i < n; i += kThreads) {
+  for (int i = tid; i < n; i += kObjThreads) {
     double diff;
     switch (fcn) {
       case DVC_SAD:
@@ -1254,17 +1255,25 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   }
 
   // Independent points without a coarse grid (start parameters given, or
-  // no basin) and Gauss-Newton: two CTAs per SM at the same width, the
-  // correlate region read through L1 (config 5's learned search: 1.46 ->
-  // 1.30 s for 499,200 points). The same search; the kernel compiled for two
-  // CTAs may fuse multiplies and adds differently, so results can differ in
-  // the last FP32 bits. DVC_PAIR=0: one CTA per SM with staging.
+  // no basin) and Gauss-Newton: two CTAs per SM, at the narrowest cluster
+  // width whose state fits two (no cluster at all when one CTA holds the
+  // subvolume), the correlate region read through L1. Config 5's learned
+  // search (499,200 points of 3375 samples): 1.46 s at width 2 with one
+  // staged CTA per SM, 1.30 s with two per SM, 1.13 s with two per SM at
+  // width 1. Other widths sum in another order and the kernel compiled for
+  // two CTAs may fuse multiplies and adds differently, so results can differ
+  // in the last FP32 bits. DVC_PAIR=0: one CTA per SM with staging; 1, 2, 4:
+  // that width.
   SearchShape pair;
   bool use_pair = false;
   const bool no_grid = seed_mode == DVC_SEED_PARAMS || (seed_mode != DVC_SEED_NEIGHBOURS && p.basin_radius == 0.0);
   if (no_grid && p.refine_method == DVC_REFINE_GAUSS_NEWTON && e->cluster <= 0) {
     const char *v = getenv("DVC_PAIR");
-    if (!(v && atoi(v) == 0)) use_pair = search_shape_pair(e, base.C, st, pair) == DVC_OK;
+    const int pc = v ? atoi(v) : -1;
+    if (pc == 1 || pc == 2 || pc == 4 || pc == 8)
+      use_pair = search_shape_pair(e, pc, st, pair) == DVC_OK;
+    else if (pc != 0)
+      for (int c = 1; c <= base.C && !use_pair; c *= 2) use_pair = search_shape_pair(e, c, st, pair) == DVC_OK;
   }
 
   SearchArgs a{};
@@ -2053,7 +2062,7 @@ int dvc_gpu_objective(int obj_function, int n, const double *ref, const double *
   if (residual) CUDA_TRY(cudaMalloc(&d_res, (size_t)n * sizeof(double)));
   CUDA_TRY(cudaMemcpy(d_r, ref, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(d_t, tar, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
-  objective_kernel<<<1, kThreads>>>(obj_function, n, d_r, d_t, d_o, d_res);
+  objective_kernel<<<1, kObjThreads>>>(obj_function, n, d_r, d_t, d_o, d_res);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpy(obj, d_o, sizeof(double), cudaMemcpyDeviceToHost));
   if (residual) CUDA_TRY(cudaMemcpy(residual, d_res, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));

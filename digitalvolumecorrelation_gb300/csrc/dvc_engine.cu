@@ -821,6 +821,13 @@ struct RunIO {
   int *gn_iters;
 };
 
+// Dataflow scheduling (predecessor counts, successor lists, ready queues)
+// for the reference's seeding with neighbour lists, unless the scratch is the
+// caller's fixed array or DVC_IN_ORDER asks for processing order.
+bool uses_dataflow(const RunIO &io, const char *ws_fixed) {
+  return io.seed_mode == DVC_SEED_NEIGHBOURS && io.n_neigh > 0 && !ws_fixed && !getenv("DVC_IN_ORDER");
+}
+
 int check_run(const dvc_engine *e, const RunIO &io) {
   if (!e) return set_error(DVC_E_ARG, "null engine");
   if (io.n_points < 0 || io.n_process < 0 || io.n_process > io.n_points)
@@ -851,8 +858,7 @@ int prepare_run(dvc_engine *e, const RunIO &io, cudaStream_t st, char *ws_fixed,
   const size_t off_ctl = 0;
   const size_t off_done = kCtlBytes;
   const size_t off_rank = off_done + (size_t)n_points * 4;
-  const bool dataflow = io.seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !ws_fixed &&
-                        !getenv("DVC_IN_ORDER");
+  const bool dataflow = uses_dataflow(io, ws_fixed);
   const size_t off_pend = (off_rank + (size_t)n_points * 4 + 255) & ~(size_t)255;
   const size_t off_soff = off_pend + (size_t)n_points * 4;
   const size_t off_cursor = off_soff + ((size_t)n_points + 1) * 4;
@@ -1235,7 +1241,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   // (0,0: one launch).
   int w1 = n_process, w2 = n_process;
   SearchShape wide;
-  const bool dataflow = seed_mode == DVC_SEED_NEIGHBOURS && n_neigh > 0 && !ws_fixed && !getenv("DVC_IN_ORDER");
+  const bool dataflow = uses_dataflow(io, ws_fixed);
   if (dataflow && e->cluster <= 0 && (base.C == 2 || base.C == 4)) {
     long long K1 = 84LL * base.max_clusters, R = 28LL * base.max_clusters;
     bool forced = false;

@@ -249,6 +249,49 @@ def test_learned_search_and_fallback():
     E.close()
 
 
+@pytest.mark.gpu
+def test_learned_search_does_not_depend_on_point_order():
+    """The learned search takes its points in locality order (a counting sort
+    by the Morton code of each point's cell): every point's patch, network
+    proposal and search are its own, so the same points given in any order
+    (and a subset) give the same bits."""
+    import torch
+    from digitalvolumecorrelation_gb300 import engine, synth
+    from digitalvolumecorrelation_gb300.abi import make_params
+    ref, cor, aff = _volumes()
+    p = make_params((64, 64, 64), subvol_geom="cube", subvol_size=13, subvol_npts=400, num_srch_dof=6,
+                    disp_max=3, basin_radius=1.5)
+    E = engine.Engine(p, ref, cor)
+    rng = np.random.default_rng(7)
+    pts = synth.grid_points((4, 4, 4), 5.0, (32.0, 32.0, 32.0)) + rng.normal(0.0, 0.3, (64, 3))
+    n = len(pts)
+    net = engine.Cnn(seed=5)
+    # distinct proposals per point, near zero (within Gauss-Newton's reach)
+    net.set_weights(net.get_weights() * np.float32(0.05))
+    dev = "cuda"
+    pd = torch.from_numpy(pts).to(dev)
+    runs = []
+    perm = rng.permutation(n).astype(np.int32)
+    for order in (np.arange(n, dtype=np.int32), perm, perm[: n // 2].copy()):
+        st = torch.empty(n, dtype=torch.int32, device=dev)
+        ob = torch.empty(n, dtype=torch.float64, device=dev)
+        pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
+        od = torch.from_numpy(order).to(dev)
+        E.process_learned(net, n, pd, od, len(order), 10.0, st, ob, pa)
+        runs.append((order, st.cpu().numpy(), ob.cpu().numpy(), pa.cpu().numpy()))
+    (_, s0, o0, q0), (_, s1, o1, q1), (sub, s2, o2, q2) = runs
+    assert (s0 == 0).sum() >= n // 2
+    np.testing.assert_array_equal(s1, s0)
+    np.testing.assert_array_equal(o1, o0)
+    np.testing.assert_array_equal(q1, q0)
+    np.testing.assert_array_equal(s2[sub], s0[sub])
+    np.testing.assert_array_equal(q2[sub], q0[sub])
+    rest = np.setdiff1d(np.arange(n), sub)
+    assert np.all(s2[rest] == -3)  # not in the order: not searched
+    net.close()
+    E.close()
+
+
 def _bump_pair(seed, shape=(96, 96, 96)):
     from digitalvolumecorrelation_gb300 import synth
     rng = np.random.default_rng(seed)

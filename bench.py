@@ -54,6 +54,8 @@ def parse():
                          "points of the processing order")
     ap.add_argument("--profile-cnn", action="store_true",
                     help="one network forward pass over 1024 random patches, for profilers")
+    ap.add_argument("--profile-learned", action="store_true",
+                    help="the profile case in the learned search's form (12 start parameters, no grid)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one search launch on a small case for profilers: the bench "
                          "configuration's subvolumes and search on 384^3 uint16 volumes, "
@@ -205,16 +207,20 @@ def cpu_leg(W, p, ref_np, cor_np, pts, seeds, gpu, sample, threads):
     return len(idx) / dt, dt, acc, r
 
 
-def profile_case():
+def profile_case(learned=False):
     """One launch of the search kernel on a case small enough for ncu's
     replays: the bench configuration's sphere subvolumes (41 voxels, 4000
     samples), znssd, tricubic, 12 degrees of freedom, disp_max 6 / basin 3, on
     384^3 uint16 volumes (2 x 113 MB, more than L2), 216 points, seeds within
-    half a voxel of the truth."""
+    half a voxel of the truth. learned: the learned search's form instead,
+    1728 points started from all 12 parameters (translations within 0.7
+    voxel RMS of the truth, rotations and strains of the network's error
+    size), no coarse grid: the kernel built for two CTAs per SM."""
     import torch
     from digitalvolumecorrelation_gb300 import engine, synth, workloads
     shape = (384, 384, 384)
-    pts = synth.grid_points((6, 6, 6), 24.0, (192.0, 192.0, 192.0))
+    pts = (synth.grid_points((12, 12, 12), 12.0, (192.0, 192.0, 192.0)) if learned
+           else synth.grid_points((6, 6, 6), 24.0, (192.0, 192.0, 192.0)))
     kw = dict(subvol_geom="sphere", subvol_size=41, subvol_npts=4000, obj_function="znssd",
               interp_type="tricubic", num_srch_dof=12, disp_max=6, basin_radius=3.0)
     b = synth.blobs(shape, int(np.prod(shape) // 1000), sigma=(1.5, 3.0), amp=(2000.0, 60000.0), seed=2)
@@ -225,16 +231,25 @@ def profile_case():
     ref_d, cor_d = W.render_device()
     E = engine.Engine(p, ref_dev=ref_d, cor_dev=cor_d)
     dev = torch.device("cuda")
-    seeds = W.truth() + np.random.default_rng(0).normal(0, 0.5, (n, 3))
+    rng = np.random.default_rng(0)
+    if learned:
+        seeds = np.zeros((n, 12))
+        seeds[:, :3] = W.truth() + rng.normal(0, 0.7, (n, 3))
+        seeds[:, 3:6] = rng.normal(0, 0.004, (n, 3))
+        seeds[:, 6:] = rng.normal(0, 0.006, (n, 6))
+    else:
+        seeds = W.truth() + rng.normal(0, 0.5, (n, 3))
     t = lambda a, dt=None: torch.as_tensor(a, dtype=dt, device=dev)
     st = torch.empty(n, dtype=torch.int32, device=dev)
     ob = torch.empty(n, dtype=torch.float64, device=dev)
     pa = torch.empty((n, 12), dtype=torch.float64, device=dev)
     it = torch.empty(n, dtype=torch.int32, device=dev)
-    E.process_device(n, t(W.points), t(np.arange(n), torch.int32), n, None, 0, 1, t(seeds), st, ob,
+    mode = engine.SEED_PARAMS if learned else engine.SEED_GIVEN
+    E.process_device(n, t(W.points), t(np.arange(n), torch.int32), n, None, 0, mode, t(seeds), st, ob,
                      pa, it, stream=torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": W.name, "good": int((st == 0).sum().item()), "points": n,
+    print(json.dumps({"profile_case": W.name + ("_learned_start" if learned else ""),
+                      "good": int((st == 0).sum().item()), "points": n, "launch": E.last_launch(),
                       "evaluations": E.last_counters()[0], "sample_evals": E.last_counters()[0] * 4000}))
 
 
@@ -276,8 +291,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
-    if args.profile_case:
-        return profile_case()
+    if args.profile_case or args.profile_learned:
+        return profile_case(learned=args.profile_learned)
     if args.profile_cnn:
         return profile_cnn()
     if args.pipeline_only:

@@ -1314,7 +1314,7 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
   e->last_smem = (int)body.smem;
   e->last_windows[0] = w1;
   e->last_windows[1] = w2;
-  e->last_windows[2] = n_win == 3 ? wide.C : base.C;
+  e->last_windows[2] = n_win == 3 ? wide.C : body.C;
   return DVC_OK;
 }
 

@@ -1220,6 +1220,10 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
     const int per = (seed_mode == DVC_SEED_NEIGHBOURS) ? 512 : 1024;
     C = 1;
     while (C < 8 && e->n_sub / (2 * C) >= per) C *= 2;
+    // a call of a few points (the learned search's fallback) leaves most
+    // SMs idle: wider clusters, as long as they take at most an eighth of
+    // the SMs, cut its latency
+    while (C < 8 && n_process > 0 && (long long)n_process * 2 * C * 8 <= e->num_sms) C *= 2;
   }
   SearchShape base;
   rc = search_shape(e, C, true, seed_mode, budget, tma_ok, st, base);

@@ -175,8 +175,8 @@ __global__ void objective_kernel(int fcn, int n, const double *r, const double *
 __host__ __device__ inline int rank_window(int r, int w1, int w2) { return (r >= w1) + (r >= w2); }
 // the window's work counter and ready-queue tail in the control block's ints
 // (int 1 is the error flag)
-__host__ __device__ inline int window_work_int(int w) { return w == 0 ? 0 : 1 + 2 * w; }
-__host__ __device__ inline int window_tail_int(int w) { return 2 + 2 * w; }
+__host__ __device__ constexpr int window_work_int(int w) { return w == 0 ? 0 : 1 + 2 * w; }
+__host__ __device__ constexpr int window_tail_int(int w) { return 2 + 2 * w; }
 
 __global__ void dep_count_kernel(int n_process, int n_points, int nn, const int *order,
                                  const int *neigh, const int *rank, int w1, int w2, int *pend,
@@ -804,6 +804,9 @@ bool encode_stage_map(const dvc_engine *e, const int bx[3], const void *vol, CUt
 constexpr size_t kCtlBytes = 256;
 constexpr size_t kCountersOff = 64;
 static_assert(kCountersOff + kNumCounters * sizeof(unsigned long long) <= kCtlBytes, "control block");
+static_assert((window_work_int(2) + 1) * sizeof(int) <= kCountersOff &&
+                  (window_tail_int(2) + 1) * sizeof(int) <= kCountersOff,
+              "window counters before the 64-bit counters");
 
 // One search call's points, seeds and outputs (device pointers).
 struct RunIO {
@@ -1858,7 +1861,7 @@ __global__ void cell_key_kernel(int n, const int *order, const double *pts, doub
   unsigned c[3];
   for (int d = 0; d < 3; d++) {
     const double v = floor(pts[(size_t)i * 3 + d] / cell);
-    c[d] = v < 0.0 ? 0u : (v > (double)lim ? lim : (unsigned)v);
+    c[d] = !(v >= 0.0) ? 0u : (v > (double)lim ? lim : (unsigned)v);  // NaN: cell 0
   }
   const int k = (int)(spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2));
   key[r] = k;

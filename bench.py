@@ -414,8 +414,9 @@ def main():
         "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak_tf,
                      "unit": "TFLOP/s", "frac": round(achieved / peak_tf, 4),
                      "traffic": None,
-                     "traffic_note": "DRAM bytes are not measurable inside the run; the one-pass ncu "
-                                     "capture of this launch reads 2.1x the algorithmic bytes",
+                     "traffic_note": "DRAM bytes are not measurable inside the run; a one-pass ncu "
+                                     "capture of the search (one launch, before the rank windows) "
+                                     "read 2.1x the algorithmic bytes",
                      "flop_per_unit": flop_per_sample, "units_per_launch": sample_evals,
                      "peak_source": "measured bf16 (burst)" if "bf16_tflops" in peaks else "fallback",
                      "note": "algorithmic FLOPs of the fused 64x64 coefficient product per "

@@ -390,8 +390,11 @@ int dvc_cnn_train_step(dvc_cnn *net, int batch, const float *patches_dev, const 
    whose search failed or whose objective exceeds obj_threshold, the plain
    search (coarse grid + Gauss-Newton) seeded with the network's translation.
    Device arrays as in dvc_gpu_process_device; *n_fallback (host) receives the
-   number of points searched again. Synchronises the stream;
-   dvc_gpu_last_counters then reports the sum over both launches. */
+   number of points searched again. The points are taken in locality order
+   (sorted by the Morton code of their cell) for the network passes and the
+   searches; every point's result is independent of the order given.
+   Synchronises the stream; dvc_gpu_last_counters then reports the sum over
+   both searches. */
 int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const double *points_dev,
                             int n_process, const int *order_dev, double obj_threshold,
                             int *status_dev, double *objmin_dev, double *params_dev,

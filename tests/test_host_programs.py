@@ -99,6 +99,89 @@ def test_dvc_input_errors(bins, vols, tmp_path, edit, msg):
     assert not os.path.exists(os.path.join(d, "result.disp"))
 
 
+REF_DVC = os.path.join(ROOT, "oracle", "_ref", "dvc")
+
+
+def _set_keys(text, kv):
+    """The input file with each keyword's value replaced (or the keyword
+    appended when the file has none)."""
+    lines = text.split("\n")
+    for key, val in kv.items():
+        for i, l in enumerate(lines):
+            if l.split("\t")[0] == key:
+                lines[i] = f"{key}\t{val}\t###"
+                break
+        else:
+            lines.insert(len(lines) - 1, f"{key}\t{val}")
+    return "\n".join(lines)
+
+
+# Both sides of the reference's limits
+# (Core/InputRead.cpp:519-631: subvol_size and disp_max up to the smallest
+# volume dimension, subvol_npts up to 50000, basin_radius up to disp_max,
+# rigid_trans and starting_point within the volume's extent, subvol_aspect in
+# [0.1, 10], gray thresholds within 2^vol_bit_depth, min_vol_fract in [0, 1])
+_THR = {"subvol_thresh": "on", "gray_thresh_min": "10", "gray_thresh_max": "200", "min_vol_fract": "0.5"}
+ACCEPTANCE = [  # (name, keyword values, accepted by both)
+    ("subvol_size 40", {"subvol_size": "40"}, True),
+    ("subvol_size 41", {"subvol_size": "41"}, False),
+    ("subvol_npts 50000", {"subvol_npts": "50000"}, True),
+    ("subvol_npts 50001", {"subvol_npts": "50001"}, False),
+    ("disp_max 40", {"disp_max": "40", "basin_radius": "0"}, True),
+    ("disp_max 41", {"disp_max": "41"}, False),
+    ("basin_radius 3", {"basin_radius": "3"}, True),
+    ("basin_radius 3.01", {"basin_radius": "3.01"}, False),
+    ("basin_radius -1", {"basin_radius": "-1"}, False),
+    ("num_srch_dof 3", {"num_srch_dof": "3"}, True),
+    ("num_srch_dof 12", {"num_srch_dof": "12"}, True),
+    ("obj_function sad", {"obj_function": "sad"}, True),
+    ("obj_function nssd", {"obj_function": "nssd"}, True),
+    ("obj_function ncc", {"obj_function": "ncc"}, False),
+    ("interp_type nearest", {"interp_type": "nearest"}, True),
+    ("interp_type cubic", {"interp_type": "cubic"}, False),
+    ("subvol_geom sphere", {"subvol_geom": "sphere"}, True),
+    ("subvol_geom ball", {"subvol_geom": "ball"}, False),
+    ("vol_hdr_lngth 16", {"vol_hdr_lngth": "16"}, False),
+    ("vol_bit_depth 12", {"vol_bit_depth": "12"}, False),
+    ("rigid_trans in", {"rigid_trans": "0 -40 0"}, True),
+    ("rigid_trans out", {"rigid_trans": "0 -41 0"}, False),
+    ("subvol_aspect in", {"subvol_aspect": "0.1 1 10"}, True),
+    ("subvol_aspect out", {"subvol_aspect": "1 10.5 1"}, False),
+    ("starting_point in", {"starting_point": "20 20 40"}, True),
+    ("starting_point out", {"starting_point": "20 20 41"}, False),
+    ("subvol_thresh on", _THR, True),
+    ("gray_thresh_max 300", dict(_THR, gray_thresh_max="300"), False),
+    ("gray_thresh_max below min", dict(_THR, gray_thresh_min="100", gray_thresh_max="50"), False),
+    ("min_vol_fract 1.5", dict(_THR, min_vol_fract="1.5"), False),
+    ("subvol_thresh maybe", {"subvol_thresh": "maybe"}, False),
+]
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DVC),
+                    reason="the reference's dvc is built only where its sources are (oracle/build_ref.sh)")
+@pytest.mark.parametrize("name,kv,expect", ACCEPTANCE, ids=[n for n, _, _ in ACCEPTANCE])
+def test_dvc_accepts_what_the_reference_accepts(bins, vols, tmp_path, name, kv, expect):
+    """Each edit of a valid input file, run through the drop-in `dvc` and
+    through the reference's own: both accept it (read the input and the
+    point cloud, then sort: `sorting finished`) or both reject it. The
+    reference searches two points of an accepted file on the CPU; the drop-in
+    stops at the GPU where there is none."""
+    accepted = {}
+    for tag, exe in (("drop-in", bins[0]), ("reference", REF_DVC)):
+        d = os.path.join(str(tmp_path), tag)
+        os.makedirs(d)
+        write_dvc_inputs(d, RUNS[0]["case"], vols, np.array(RUNS[0]["points"]), RUNS[0]["labels"])
+        p = os.path.join(d, "dvc_in")
+        text = _set_keys(open(p).read(), dict(kv, num_points_to_process="2"))
+        with open(p, "w") as f:
+            f.write(text)
+        r = subprocess.run([exe, "dvc_in"], cwd=d, capture_output=True, text=True, timeout=300)
+        accepted[tag] = "sorting finished" in r.stdout
+        if not accepted[tag]:
+            assert r.returncode == 0, (tag, r.stdout[-400:], r.stderr[-400:])
+    assert accepted == {"drop-in": expect, "reference": expect}, (name, accepted)
+
+
 def test_dvc_roi_rules_and_modes(bins, vols, tmp_path):
     d = setup_run(tmp_path, RUNS[0], vols)
     # a point cloud with no valid line aborts

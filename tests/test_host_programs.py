@@ -8,7 +8,10 @@ inputs are written here and the drop-in programs run on them.
 
 CPU tests: the input-file checks and their messages, the command line
 modes, and the outputs written before the GPU is used (`<roi>.sort.csv`,
-the .stat input echo, strain's own sort file). GPU tests: whole runs.
+the .stat input echo, strain's own sort file); where the reference's own
+programs are built (oracle/_ref), which input files both accept on both
+sides of every limit, and strain's flag handling line for line. GPU tests:
+whole runs.
 """
 from __future__ import annotations
 
@@ -180,6 +183,39 @@ def test_dvc_accepts_what_the_reference_accepts(bins, vols, tmp_path, name, kv, 
         if not accepted[tag]:
             assert r.returncode == 0, (tag, r.stdout[-400:], r.stderr[-400:])
     assert accepted == {"drop-in": expect, "reference": expect}, (name, accepted)
+
+
+REF_STRAIN = os.path.join(ROOT, "oracle", "_ref", "strain")
+STRAIN_FLAGS = [["-sw", "30"], ["-sw", "0"], ["-sw", "5000"], ["-sw", "abc"], ["-t", "0.05"], ["-t", "5"],
+                ["-t", "-1"], ["-r", "-E", "-D"], ["-A", "-xy"], ["-q", "-sw"], ["-sw", "12", "-t", "0.3", "-r"],
+                ["-yz", "-zx", "-t"]]
+
+
+@pytest.mark.skipif(not os.path.exists(REF_STRAIN),
+                    reason="the reference's strain is built only where its sources are (oracle/build_ref.sh)")
+@pytest.mark.parametrize("flags", STRAIN_FLAGS, ids=[" ".join(f) for f in STRAIN_FLAGS])
+def test_strain_flags_as_the_reference(bins, tmp_path, flags):
+    """strain's command line through the drop-in and the reference's own
+    program: the same messages and the same settings (window, threshold,
+    refill, plane, point counts), line for line up to the fit, for valid,
+    clamped, malformed and unknown flags."""
+    def head(out):
+        lines = out.split("\n")
+        for i, l in enumerate(lines):
+            if l.startswith("ndisp_pts ="):
+                return lines[:i + 1]
+        return lines
+    outs = []
+    for tag, exe in (("drop-in", bins[1]), ("reference", REF_STRAIN)):
+        d = os.path.join(str(tmp_path), tag)
+        os.makedirs(d)
+        open(os.path.join(d, "result.disp"), "w").write(RUNS[0]["disp"])
+        open(os.path.join(d, "points.roi.sort.csv"), "w").write(RUNS[0]["sort_csv"])
+        r = subprocess.run([exe, "result.disp", "points.roi.sort.csv"] + flags, cwd=d, capture_output=True,
+                           text=True, timeout=120)
+        outs.append(head(r.stdout))
+    assert any(l.startswith("using strain window: ") for l in outs[1])
+    assert outs[0] == outs[1]
 
 
 def test_dvc_roi_rules_and_modes(bins, vols, tmp_path):

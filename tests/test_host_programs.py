@@ -166,10 +166,11 @@ ACCEPTANCE = [  # (name, keyword values, accepted by both)
 def test_dvc_accepts_what_the_reference_accepts(bins, vols, tmp_path, name, kv, expect):
     """Each edit of a valid input file, run through the drop-in `dvc` and
     through the reference's own: both accept it (read the input and the
-    point cloud, then sort: `sorting finished`) or both reject it. The
-    reference searches two points of an accepted file on the CPU; the drop-in
-    stops at the GPU where there is none."""
-    accepted = {}
+    point cloud, then sort: `sorting finished`) or both reject it; for an
+    accepted file the .stat input echo and <roi>.sort.csv are the same bytes.
+    The reference searches two points of an accepted file on the CPU; the
+    drop-in stops at the GPU where there is none."""
+    accepted, files = {}, {}
     for tag, exe in (("drop-in", bins[0]), ("reference", REF_DVC)):
         d = os.path.join(str(tmp_path), tag)
         os.makedirs(d)
@@ -182,7 +183,13 @@ def test_dvc_accepts_what_the_reference_accepts(bins, vols, tmp_path, name, kv, 
         accepted[tag] = "sorting finished" in r.stdout
         if not accepted[tag]:
             assert r.returncode == 0, (tag, r.stdout[-400:], r.stderr[-400:])
+        else:
+            files[tag] = (echo_part(open(os.path.join(d, "result.stat")).read()),
+                          open(os.path.join(d, "points.roi.sort.csv")).read())
     assert accepted == {"drop-in": expect, "reference": expect}, (name, accepted)
+    if expect:  # the .stat input echo and the processing order, byte for byte
+        assert files["drop-in"][0] == files["reference"][0]
+        assert files["drop-in"][1] == files["reference"][1]
 
 
 REF_STRAIN = os.path.join(ROOT, "oracle", "_ref", "strain")

@@ -192,6 +192,61 @@ def test_dvc_accepts_what_the_reference_accepts(bins, vols, tmp_path, name, kv, 
         assert files["drop-in"][1] == files["reference"][1]
 
 
+def _roi_variants():
+    """Point-cloud files built from the first run's points, each exercising
+    one of the reference's line rules (InputRead::read_point_cloud,
+    Core/InputRead.cpp:632-700: an integer label, not followed by '.' or 'E',
+    then three numbers; anything else skips the line; the line end is
+    detected per file)."""
+    P, L = RUNS[0]["points"], RUNS[0]["labels"]
+
+    def base(fmt="{l}\t{x:g}\t{y:g}\t{z:g}", sep="\n"):
+        return sep.join(fmt.format(l=l, x=p[0], y=p[1], z=p[2]) for l, p in zip(L, P)) + sep
+    return {
+        "header and comments": "n\tx\ty\tz\n# comment line\n\n" + base(),
+        "crlf": "n x y z\r\n" + base(sep="\r\n"),
+        "extra columns": base("{l} {x:g} {y:g} {z:g} 99 extra"),
+        "float labels": base() + "5.0\t20\t20\t20\n7.5 21 21 21\n",
+        "exponent labels": base() + "1E2 20 20 20\n7e1 21 21 21\n3e 22 22 22\n",
+        "short lines": base() + "300 20 20\n301 20\n302\n",
+        "scientific coordinates": base() + "400 2.05e1 1.9E1 +20.5\n401 -0 20 20.0\n",
+        "tabs and spaces": base("  {l} \t {x:g}   {y:g}\t\t{z:g}  "),
+        "duplicate points": base() + "500 20 20 20\n501 20 20 20\n502 19.9 20.1 20\n",
+        "no final newline": base()[:-1],
+        "negative labels": base("-{l}\t{x:g}\t{y:g}\t{z:g}"),
+        "text in coordinates": base() + "600 20 abc 20\n601 20 20 x\n",
+    }
+
+
+ROI_VARIANTS = _roi_variants()
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DVC),
+                    reason="the reference's dvc is built only where its sources are (oracle/build_ref.sh)")
+@pytest.mark.parametrize("name", list(ROI_VARIANTS))
+def test_dvc_reads_point_clouds_as_the_reference(bins, vols, tmp_path, name):
+    """The same point-cloud file through both programs: the same points
+    (count and bounding box in the .stat echo) and the same processing order
+    and neighbours (<roi>.sort.csv, ties included), byte for byte."""
+    files = {}
+    for tag, exe in (("drop-in", bins[0]), ("reference", REF_DVC)):
+        d = os.path.join(str(tmp_path), tag)
+        os.makedirs(d)
+        write_dvc_inputs(d, RUNS[0]["case"], vols, np.array(RUNS[0]["points"]), RUNS[0]["labels"])
+        with open(os.path.join(d, "points.roi"), "w", newline="") as f:
+            f.write(ROI_VARIANTS[name])
+        p = os.path.join(d, "dvc_in")
+        text = _set_keys(open(p).read(), {"num_points_to_process": "2", "starting_point": "20 20 20"})
+        with open(p, "w") as f:
+            f.write(text)
+        r = subprocess.run([exe, "dvc_in"], cwd=d, capture_output=True, text=True, timeout=300)
+        assert "sorting finished" in r.stdout, (tag, r.stdout[-400:])
+        files[tag] = (echo_part(open(os.path.join(d, "result.stat")).read()),
+                      open(os.path.join(d, "points.roi.sort.csv")).read())
+    assert "Point Cloud contains" in files["reference"][0]
+    assert files["drop-in"] == files["reference"]
+
+
 REF_STRAIN = os.path.join(ROOT, "oracle", "_ref", "strain")
 STRAIN_FLAGS = [["-sw", "30"], ["-sw", "0"], ["-sw", "5000"], ["-sw", "abc"], ["-t", "0.05"], ["-t", "5"],
                 ["-t", "-1"], ["-r", "-E", "-D"], ["-A", "-xy"], ["-q", "-sw"], ["-sw", "12", "-t", "0.3", "-r"],

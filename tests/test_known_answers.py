@@ -10,7 +10,9 @@ from the mathematics of the method:
     zx, xyz) exactly;
   * a correlate volume that is the reference volume moved by whole voxels
     is matched exactly: the search returns that translation, no rotation or
-    strain, and an objective of zero.
+    strain, and an objective of zero;
+  * the strain fit of a displacement field linear in the position recovers
+    its gradient, hence both strain measures and their principal values.
 Volumes are stored z, y, x (x fastest); positions are (x, y, z).
 """
 import numpy as np
@@ -100,3 +102,77 @@ def test_whole_voxel_translation_found_exactly_reference(oracle, reference, dof,
     p, ref, cor, pts = _shift_case(dof, geom)
     order, neigh = oracle.order_neighbours(pts)
     _check_shift(reference.process(p, ref, cor, pts, order, neigh), dof)
+
+
+# ----------------------------------------------------------------- strain ---
+# A displacement field linear in the position, u = A X + b: every strain
+# window's least-squares fit recovers the displacement gradient A and the
+# displacement itself exactly, so the engineering strain is (A + A')/2 and
+# the Lagrangian strain (A + A' + A'A)/2, each with its eigenvalues in
+# descending order. Integer grid positions and A, b in multiples of 1e-3 keep
+# u exact in the .disp file's six decimals.
+A_LIN = np.array([[0.010, 0.002, -0.003], [0.001, -0.006, 0.004], [0.002, 0.003, 0.008]])
+B_LIN = np.array([1.5, -0.7, 0.3])
+
+
+def _linear_field():
+    from digitalvolumecorrelation_gb300 import synth
+    pts = synth.grid_points((6, 6, 6), 8.0, (48.0, 48.0, 48.0))
+    assert np.all(pts == np.round(pts))
+    return pts, pts @ A_LIN.T + B_LIN
+
+
+def _strain_rows(S):
+    comps = [S[0, 0], S[1, 1], S[2, 2], S[0, 1], S[1, 2], S[0, 2]]
+    return np.array(comps + sorted(np.linalg.eigvalsh(S), reverse=True))
+
+
+E_LIN = _strain_rows(0.5 * (A_LIN + A_LIN.T))
+L_LIN = _strain_rows(0.5 * (A_LIN + A_LIN.T + A_LIN.T @ A_LIN))
+
+
+@pytest.mark.parametrize("ndp,refill", [(25, False), (25, True), (60, False)])
+def test_strain_of_a_linear_field_oracle(oracle, ndp, refill):
+    """(Windows of about 10 points on this lattice can be rank-deficient,
+    where no fit recovers A: 25 is the reference's default.)"""
+    pts, disp = _linear_field()
+    n = len(pts)
+    _, neigh = oracle.order_neighbours(pts)
+    r = oracle.strain(pts, np.zeros(n, np.int32), np.full(n, 0.01), disp, neigh, ndp, 1.0, refill)
+    assert np.abs(r["dgrad"] - A_LIN.ravel()).max() <= 1e-12
+    assert np.abs(r["u_fit"] - disp).max() <= 1e-10
+    assert np.abs(r["e_strain"] - E_LIN).max() <= 1e-12
+    assert np.abs(r["l_strain"] - L_LIN).max() <= 1e-12
+
+
+def test_strain_of_a_linear_field_reference_program(tmp_path):
+    """The reference's own `strain` program (oracle/_ref) on the same field
+    written as a .disp file: its Lagrangian, engineering and gradient CSVs
+    carry the exact values to their six printed digits."""
+    import os
+    import subprocess
+    exe = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "strain")
+    if not os.path.exists(exe):
+        pytest.skip("the reference's strain is built only where its sources are (oracle/build_ref.sh)")
+    pts, disp = _linear_field()
+    with open(os.path.join(str(tmp_path), "lin.disp"), "w") as f:
+        f.write("n\tx\ty\tz\tstatus\tobjmin\tu\tv\tw\n")
+        for k, (p, u) in enumerate(zip(pts, disp)):
+            f.write(f"{k + 1}\t{p[0]:g}\t{p[1]:g}\t{p[2]:g}\t0\t0.01\t{u[0]:.6f}\t{u[1]:.6f}\t{u[2]:.6f}\n")
+    r = subprocess.run([exe, "lin.disp", "-E", "-D"], cwd=str(tmp_path), capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+    def rows(name):
+        lines = open(os.path.join(str(tmp_path), name)).read().strip().split("\n")[1:]
+        return np.array([[float(v) for v in l.split(",")] for l in lines])
+
+    def sig6(actual, printed):
+        mag = np.where(printed == 0, 1e-300, np.abs(printed))
+        tol = np.maximum(0.5001 * 10.0 ** (np.floor(np.log10(mag)) - 5), 1e-12)
+        assert np.all(np.abs(actual - printed) <= tol), np.max(np.abs(actual - printed) / tol)
+    Lr, Er, Dr = rows("lin-sw25.Lstr.csv"), rows("lin-sw25.Estr.csv"), rows("lin-sw25.dgrd.csv")
+    assert len(Lr) == len(pts)
+    sig6(np.broadcast_to(L_LIN, Lr[:, 9:18].shape), Lr[:, 9:18])
+    sig6(np.broadcast_to(E_LIN, Er[:, 9:18].shape), Er[:, 9:18])
+    sig6(np.broadcast_to(A_LIN.ravel(), Dr[:, 9:18].shape), Dr[:, 9:18])

@@ -12,7 +12,9 @@ from the mathematics of the method:
     is matched exactly: the search returns that translation, no rotation or
     strain, and an objective of zero;
   * the strain fit of a displacement field linear in the position recovers
-    its gradient, hence both strain measures and their principal values.
+    its gradient, hence both strain measures and their principal values;
+  * each objective is zero for identical signals and blind exactly to what
+    its normalisation removes (offset, scale).
 Volumes are stored z, y, x (x fastest); positions are (x, y, z).
 """
 import numpy as np
@@ -176,3 +178,42 @@ def test_strain_of_a_linear_field_reference_program(tmp_path):
     sig6(np.broadcast_to(L_LIN, Lr[:, 9:18].shape), Lr[:, 9:18])
     sig6(np.broadcast_to(E_LIN, Er[:, 9:18].shape), Er[:, 9:18])
     sig6(np.broadcast_to(A_LIN.ravel(), Dr[:, 9:18].shape), Dr[:, 9:18])
+
+
+# -------------------------------------------------------------- objectives ---
+# What each objective's definition (Core/ObjectiveFunctions.cpp:24-263)
+# makes it blind to: ZSSD to an offset of the target, NSSD to a positive
+# scale, ZNSSD to both; every objective is zero for identical signals.
+OBJ = {"sad": 0, "ssd": 1, "zssd": 2, "nssd": 3, "znssd": 4}
+INVARIANT = {"zssd": [(1.0, 30.0)], "nssd": [(2.5, 0.0)], "znssd": [(2.5, 0.0), (1.0, 30.0), (0.4, -3.0)]}
+
+
+def _signals():
+    rng = np.random.default_rng(3)
+    r = rng.uniform(10.0, 200.0, 500)
+    return r, r + rng.normal(0.0, 5.0, 500)
+
+
+def _check_objective(obj, name):
+    r, t = _signals()
+    f = OBJ[name]
+    base = obj(f, r, t)
+    assert base > 0.0
+    assert abs(obj(f, r, r)) <= 1e-12 * max(1.0, abs(base))
+    for a, b in INVARIANT.get(name, []):
+        assert abs(obj(f, r, a * t + b) - base) <= 1e-12 * abs(base), (name, a, b)
+    # and not blind to what its definition does not remove
+    if name in ("sad", "ssd", "nssd"):
+        assert abs(obj(f, r, t + 30.0) - base) > 1e-3 * abs(base)
+    if name in ("sad", "ssd", "zssd"):
+        assert abs(obj(f, r, 2.5 * t) - base) > 1e-3 * abs(base)
+
+
+@pytest.mark.parametrize("name", list(OBJ))
+def test_objective_invariances_oracle(oracle, name):
+    _check_objective(oracle.objective, name)
+
+
+@pytest.mark.parametrize("name", list(OBJ))
+def test_objective_invariances_reference(reference, name):
+    _check_objective(reference.objective, name)

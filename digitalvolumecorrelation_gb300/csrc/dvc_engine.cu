@@ -1060,10 +1060,16 @@ static void touch_pages(const void *buf, size_t bytes) {
     run(0, bytes);
     return;
   }
+  // (no exception may leave a C entry point: pieces whose thread cannot be
+  // started are read by the calling thread)
   std::vector<std::thread> th;
   for (int t = 0; t < nt; t++) {
     const size_t lo = pages * t / nt * step, hi = std::min(bytes, pages * (t + 1) / nt * step);
-    th.emplace_back(run, lo, hi);
+    try {
+      th.emplace_back(run, lo, hi);
+    } catch (...) {
+      run(lo, hi);
+    }
   }
   for (auto &x : th) x.join();
 }

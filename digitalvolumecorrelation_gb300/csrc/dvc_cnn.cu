@@ -932,7 +932,7 @@ extern "C" {
 
 int dvc_cnn_param_count(void) { return (int)kLay.total; }
 
-int dvc_cnn_create(dvc_cnn **out, unsigned seed) {
+int dvc_cnn_create(dvc_cnn **out, unsigned seed) try {
   if (!out) return dvc_internal_set_error(DVC_E_ARG, "null argument");
   // the largest layer's weight group (64 x 27 x 8 floats) exceeds the default
   // 48 KB of dynamic shared memory
@@ -976,9 +976,11 @@ int dvc_cnn_create(dvc_cnn **out, unsigned seed) {
   cudaMemset(c->v, 0, n * 4);
   *out = c;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-void dvc_cnn_destroy(dvc_cnn *c) {
+void dvc_cnn_destroy(dvc_cnn *c) try {
   if (!c) return;
   cudaFree(c->p);
   cudaFree(c->g);
@@ -993,16 +995,20 @@ void dvc_cnn_destroy(dvc_cnn *c) {
     cudaFree(c->dact[l]);
   }
   delete c;
+} catch (...) {
+  dvc_internal_host_exception();
 }
 
-int dvc_cnn_get_weights(dvc_cnn *c, float *host, int n) {
+int dvc_cnn_get_weights(dvc_cnn *c, float *host, int n) try {
   if (!c || !host || n != (int)kLay.total) return dvc_internal_set_error(DVC_E_ARG, "bad weight buffer");
   if (cudaMemcpy(host, c->p, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
     return dvc_internal_set_error(DVC_E_CUDA, "weight copy");
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_cnn_set_weights(dvc_cnn *c, const float *host, int n) {
+int dvc_cnn_set_weights(dvc_cnn *c, const float *host, int n) try {
   if (!c || !host || n != (int)kLay.total) return dvc_internal_set_error(DVC_E_ARG, "bad weight buffer");
   if (cudaMemcpy(c->p, host, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
     return dvc_internal_set_error(DVC_E_CUDA, "weight copy");
@@ -1011,9 +1017,11 @@ int dvc_cnn_set_weights(dvc_cnn *c, const float *host, int n) {
   c->step = 0;
   c->wb_valid = false;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_cnn_forward(dvc_cnn *c, int batch, const float *patches_dev, float *out_dev, void *stream) {
+int dvc_cnn_forward(dvc_cnn *c, int batch, const float *patches_dev, float *out_dev, void *stream) try {
   if (!c || batch <= 0 || !patches_dev || !out_dev) return dvc_internal_set_error(DVC_E_ARG, "bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
   int rc = ensure_batch(c, batch);
@@ -1024,10 +1032,12 @@ int dvc_cnn_forward(dvc_cnn *c, int batch, const float *patches_dev, float *out_
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_cnn_gradients(dvc_cnn *c, int batch, const float *patches_dev, const float *targets_dev,
-                      float *grad_host, float *loss) {
+                      float *grad_host, float *loss) try {
   if (!c || batch <= 0 || !patches_dev || !targets_dev) return dvc_internal_set_error(DVC_E_ARG, "bad arguments");
   int rc = ensure_batch(c, batch);
   if (rc) return rc;
@@ -1042,10 +1052,12 @@ int dvc_cnn_gradients(dvc_cnn *c, int batch, const float *patches_dev, const flo
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
   return tc_status();
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_cnn_train_step(dvc_cnn *c, int batch, const float *patches_dev, const float *targets_dev,
-                       float lr, float *loss) {
+                       float lr, float *loss) try {
   int rc = dvc_cnn_gradients(c, batch, patches_dev, targets_dev, nullptr, loss);
   if (rc) return rc;
   c->step += 1;
@@ -1057,6 +1069,8 @@ int dvc_cnn_train_step(dvc_cnn *c, int batch, const float *patches_dev, const fl
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(e));
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 }  // extern "C"

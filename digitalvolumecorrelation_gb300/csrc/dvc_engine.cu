@@ -32,7 +32,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <random>
+#include <stdexcept>
 #include <string>
 #include <thread>
 #include <vector>
@@ -54,6 +56,19 @@ static int set_error(int code, const std::string &msg) {
   return code;
 }
 int dvc_internal_set_error(int code, const char *msg) { return set_error(code, msg); }
+// Called from the catch clause of a C entry point: the exception in flight
+// becomes the call's error code and message.
+int dvc_internal_host_exception() {
+  try {
+    throw;
+  } catch (const std::bad_alloc &) {
+    return set_error(DVC_E_NOMEM, "host memory allocation failed");
+  } catch (const std::exception &x) {
+    return set_error(DVC_E_ARG, std::string("host error: ") + x.what());
+  } catch (...) {
+    return set_error(DVC_E_ARG, "host error");
+  }
+}
 #define CUDA_TRY(expr)                                                                 \
   do {                                                                                 \
     cudaError_t _e = (expr);                                                           \
@@ -1075,7 +1090,7 @@ static void touch_pages(const void *buf, size_t bytes) {
 }
 
 int dvc_gpu_create(dvc_engine **out, const dvc_params *p, const void *ref_vox, const void *cor_vox,
-                   int big_endian) {
+                   int big_endian) try {
   if (!out || !ref_vox || !cor_vox) return set_error(DVC_E_ARG, "null argument");
   *out = nullptr;
   int rc = validate(p);
@@ -1128,10 +1143,12 @@ int dvc_gpu_create(dvc_engine **out, const dvc_params *p, const void *ref_vox, c
   }
   *out = e;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_create_from_files(dvc_engine **out, const dvc_params *p, const char *ref_path,
-                              const char *cor_path, long long header_bytes, int big_endian) {
+                              const char *cor_path, long long header_bytes, int big_endian) try {
   if (!out || !ref_path || !cor_path) return set_error(DVC_E_ARG, "null argument");
   *out = nullptr;
   int rc = validate(p);
@@ -1161,10 +1178,12 @@ int dvc_gpu_create_from_files(dvc_engine **out, const dvc_params *p, const char 
   }
   *out = e;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_create_device(dvc_engine **out, const dvc_params *p, const void *ref_vox_dev,
-                          const void *cor_vox_dev) {
+                          const void *cor_vox_dev) try {
   if (!out || !ref_vox_dev || !cor_vox_dev) return set_error(DVC_E_ARG, "null argument");
   *out = nullptr;
   int rc = validate(p);
@@ -1181,9 +1200,11 @@ int dvc_gpu_create_device(dvc_engine **out, const dvc_params *p, const void *ref
   }
   *out = e;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-void dvc_gpu_destroy(dvc_engine *e) {
+void dvc_gpu_destroy(dvc_engine *e) try {
   if (!e) return;
   if (e->owns_volumes) {
     if (e->ref) cudaFree(e->ref);
@@ -1194,6 +1215,8 @@ void dvc_gpu_destroy(dvc_engine *e) {
   if (e->d_rand_off) cudaFree(e->d_rand_off);
   if (e->ws) cudaFree(e->ws);
   delete e;
+} catch (...) {
+  dvc_internal_host_exception();
 }
 
 // The search launch with one configuration (the engine's). Scratch (done
@@ -1335,10 +1358,12 @@ static int process_device_ws(dvc_engine *e, int n_points, const double *points_d
 int dvc_gpu_process_device(dvc_engine *e, int n_points, const double *points_dev, int n_process,
                            const int *order_dev, int n_neigh, const int *neigh_dev, int seed_mode,
                            const double *seeds_dev, int *status_dev, double *objmin_dev,
-                           double *params_dev, int *gn_iters_dev, void *stream) {
+                           double *params_dev, int *gn_iters_dev, void *stream) try {
   return process_device_ws(e, n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev,
                            seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev,
                            stream, nullptr);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 // ---- allocation-free search -------------------------------------------------
@@ -1381,7 +1406,7 @@ int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *po
                                    int n_process, const int *order_dev, int n_neigh,
                                    const int *neigh_dev, int seed_mode, const double *seeds_dev,
                                    int *status_dev, double *objmin_dev, double *params_dev,
-                                   int *gn_iters_dev, void *stream) {
+                                   int *gn_iters_dev, void *stream) try {
   if (n_points > DVC_NOALLOC_MAX_POINTS)
     return set_error(DVC_E_ARG, "dvc_gpu_process_device_noalloc: n_points exceeds "
                                 "DVC_NOALLOC_MAX_POINTS (" + std::to_string(DVC_NOALLOC_MAX_POINTS) +
@@ -1392,6 +1417,8 @@ int dvc_gpu_process_device_noalloc(dvc_engine *e, int n_points, const double *po
   return process_device_ws(e, n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev,
                            seed_mode, seeds_dev, status_dev, objmin_dev, params_dev, gn_iters_dev,
                            stream, ws, kNoallocBytes);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 // The error flag of engine e's last search launch, which has finished:
@@ -1522,9 +1549,11 @@ static int host_process(dvc_engine *e, dvc_plan *plan, const int *point_cfg, int
 int dvc_gpu_process(dvc_engine *e, int n_points, const double *points, int n_process,
                     const int *order, int n_neigh, const int *neigh, int seed_mode,
                     const double *seeds, int *status, double *objmin, double *params, int *gn_iters,
-                    dvc_stats *stats) {
+                    dvc_stats *stats) try {
   return host_process(e, nullptr, nullptr, n_points, points, n_process, order, n_neigh, neigh, seed_mode,
                       seeds, status, objmin, params, gn_iters, stats);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 // ---- several configurations in one launch ------------------------------------
@@ -1594,7 +1623,7 @@ static int plan_build(dvc_plan *pl, int C, int staging) {
   return DVC_OK;
 }
 
-int dvc_gpu_plan_create(dvc_plan **out, dvc_engine *const *configs, int n_configs, int cluster) {
+int dvc_gpu_plan_create(dvc_plan **out, dvc_engine *const *configs, int n_configs, int cluster) try {
   if (!out || !configs) return set_error(DVC_E_ARG, "null argument");
   *out = nullptr;
   if (n_configs < 1) return set_error(DVC_E_ARG, "a plan needs at least one configuration");
@@ -1632,34 +1661,42 @@ int dvc_gpu_plan_create(dvc_plan **out, dvc_engine *const *configs, int n_config
   }
   *out = pl;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-void dvc_gpu_plan_destroy(dvc_plan *plan) {
+void dvc_gpu_plan_destroy(dvc_plan *plan) try {
   if (!plan) return;
   if (plan->d_cfgs) cudaFree(plan->d_cfgs);
   if (plan->d_tmaps) cudaFree(plan->d_tmaps);
   delete plan;
+} catch (...) {
+  dvc_internal_host_exception();
 }
 
-int dvc_gpu_plan_info(const dvc_plan *plan, int *cluster, int *staging, int *n_staged, long long *smem_bytes) {
+int dvc_gpu_plan_info(const dvc_plan *plan, int *cluster, int *staging, int *n_staged, long long *smem_bytes) try {
   if (!plan) return set_error(DVC_E_ARG, "null plan");
   if (cluster) *cluster = plan->cluster;
   if (staging) *staging = plan->staging;
   if (n_staged) *n_staged = plan->n_staged;
   if (smem_bytes) *smem_bytes = (long long)plan->smem_dyn;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_plan_set_shape(dvc_plan *plan, int cluster, int staging) {
+int dvc_gpu_plan_set_shape(dvc_plan *plan, int cluster, int staging) try {
   if (!plan) return set_error(DVC_E_ARG, "null plan");
   return plan_build(plan, cluster, staging ? 1 : 0);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_points,
                                 const double *points_dev, int n_process, const int *order_dev,
                                 int n_neigh, const int *neigh_dev, int seed_mode,
                                 const double *seeds_dev, int *status_dev, double *objmin_dev,
-                                double *params_dev, int *gn_iters_dev, void *stream) {
+                                double *params_dev, int *gn_iters_dev, void *stream) try {
   if (!plan) return set_error(DVC_E_ARG, "null plan");
   dvc_engine *e = plan->cfgs[0];
   const RunIO io{n_points, points_dev, n_process, order_dev, n_neigh, neigh_dev, seed_mode,
@@ -1697,22 +1734,26 @@ int dvc_gpu_plan_process_device(dvc_plan *plan, const int *point_cfg_dev, int n_
   CUtensorMap tm0;
   memset(&tm0, 0, sizeof tm0);
   return dispatch_launch(e->p.bytes_per_voxel, e->p.interp_type, a, tm0, tm0, plan->smem_dyn, grid, C, st, nullptr);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_plan_process(dvc_plan *plan, const int *point_cfg, int n_points, const double *points,
                          int n_process, const int *order, int n_neigh, const int *neigh,
                          int seed_mode, const double *seeds, int *status, double *objmin,
-                         double *params, int *gn_iters, dvc_stats *stats) {
+                         double *params, int *gn_iters, dvc_stats *stats) try {
   if (!plan) return set_error(DVC_E_ARG, "null plan");
   return host_process(plan->cfgs[0], plan, point_cfg, n_points, points, n_process, order, n_neigh, neigh,
                       seed_mode, seeds, status, objmin, params, gn_iters, stats);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_plan_autotune(dvc_plan *plan, const int *point_cfg_dev, int n_points,
                           const double *points_dev, int n_process, const int *order_dev,
                           int n_neigh, const int *neigh_dev, int seed_mode,
                           const double *seeds_dev, int *status_dev, double *objmin_dev,
-                          double *params_dev, int reps, double ms_out[8]) {
+                          double *params_dev, int reps, double ms_out[8]) try {
   if (!plan) return set_error(DVC_E_ARG, "null plan");
   if (reps < 1) return set_error(DVC_E_ARG, "reps must be >= 1");
   const int C0 = plan->cluster, S0 = plan->staging;
@@ -1755,32 +1796,40 @@ int dvc_gpu_plan_autotune(dvc_plan *plan, const int *point_cfg_dev, int n_points
   cudaEventDestroy(ev1);
   const int rc2 = plan_build(plan, rc == DVC_OK ? bestC : C0, rc == DVC_OK ? bestS : S0);
   return rc ? rc : rc2;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_last_launch(dvc_engine *e, int out[4]) {
+int dvc_gpu_last_launch(dvc_engine *e, int out[4]) try {
   if (!e || !out) return set_error(DVC_E_ARG, "null argument");
   out[0] = e->last_cluster;
   out[1] = e->last_grid;
   out[2] = e->last_staged;
   out[3] = e->last_smem;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_last_windows(dvc_engine *e, int out[3]) {
+int dvc_gpu_last_windows(dvc_engine *e, int out[3]) try {
   if (!e || !out) return set_error(DVC_E_ARG, "null argument");
   for (int k = 0; k < 3; k++) out[k] = e->last_windows[k];
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_set_cluster(dvc_engine *e, int cluster) {
+int dvc_gpu_set_cluster(dvc_engine *e, int cluster) try {
   if (!e) return set_error(DVC_E_ARG, "null engine");
   if (cluster != 0 && cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8)
     return set_error(DVC_E_ARG, "cluster must be 0, 1, 2, 4 or 8");
   e->cluster = cluster;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_last_counters(dvc_engine *e, long long out[3]) {
+int dvc_gpu_last_counters(dvc_engine *e, long long out[3]) try {
   if (!e || !out) return set_error(DVC_E_ARG, "null argument");
   out[0] = out[1] = out[2] = 0;
   if (e->counts_host) {
@@ -1793,22 +1842,28 @@ int dvc_gpu_last_counters(dvc_engine *e, long long out[3]) {
   CUDA_TRY(cudaMemcpy(c, e->last_ctl + kCountersOff, sizeof c, cudaMemcpyDeviceToHost));
   for (int k = 0; k < 3; k++) out[k] = (long long)c[k];
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_set_wait_limit(dvc_engine *e, long long polls) {
+int dvc_gpu_set_wait_limit(dvc_engine *e, long long polls) try {
   if (!e) return set_error(DVC_E_ARG, "null engine");
   e->wait_polls = polls < 0 ? -1 : polls;
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_last_status(dvc_engine *e) {
+int dvc_gpu_last_status(dvc_engine *e) try {
   if (!e) return set_error(DVC_E_ARG, "null engine");
   if (!e->last_ctl) return DVC_OK;
   CUDA_TRY(cudaDeviceSynchronize());
   return launch_error(e);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]) {
+int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]) try {
   if (!e || !out) return set_error(DVC_E_ARG, "null argument");
   for (int k = 0; k < DVC_N_PHASES; k++) out[k] = 0;
   if (!e->last_ctl) return DVC_OK;
@@ -1828,6 +1883,8 @@ int dvc_gpu_last_phase_cycles(dvc_engine *e, long long out[DVC_N_PHASES]) {
             "%llu Gauss-Newton systems used the FP64 factorisation\n", slow, fp64);
   }
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 // ------------------------------------------------------ learned search ---
@@ -1894,15 +1951,17 @@ __global__ void merge_kernel(int n, const int *list, const int *st2, const doubl
 }  // namespace
 
 int dvc_cnn_patches(dvc_engine *e, int n, const double *points_dev, const int *idx_dev, float *patches_dev,
-                    void *stream) {
+                    void *stream) try {
   if (!e || n < 0 || (n > 0 && (!points_dev || !patches_dev))) return set_error(DVC_E_ARG, "bad arguments");
   return dvc_internal_patches(e->ref, e->cor, e->p.bytes_per_voxel, e->p.vol_wide, e->p.vol_high,
                               e->p.vol_tall, n, points_dev, idx_dev, patches_dev, (cudaStream_t)stream);
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const double *points_dev, int n_process,
                             const int *order_dev, double obj_threshold, int *status_dev, double *objmin_dev,
-                            double *params_dev, int *gn_iters_dev, int *n_fallback, void *stream) {
+                            double *params_dev, int *gn_iters_dev, int *n_fallback, void *stream) try {
   if (!e || !net) return set_error(DVC_E_ARG, "null engine or network");
   if (n_points < 0 || n_process < 0 || n_process > n_points) return set_error(DVC_E_ARG, "bad sizes");
   if (n_fallback) *n_fallback = 0;
@@ -2014,10 +2073,12 @@ int dvc_gpu_process_learned(dvc_engine *e, dvc_cnn *net, int n_points, const dou
   if (!rc && n_fallback) *n_fallback = nfb;
   cleanup();
   return rc;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_interpolate(dvc_engine *e, int volume, const double center[3], int n, const double *pts,
-                        int interp_type, double *out) {
+                        int interp_type, double *out) try {
   if (!e || !center || (n > 0 && (!pts || !out))) return set_error(DVC_E_ARG, "null argument");
   if (interp_type < 0 || interp_type > 2) return set_error(DVC_E_ARG, "bad interp_type");
   if (n <= 0) return DVC_OK;
@@ -2068,10 +2129,12 @@ int dvc_gpu_interpolate(dvc_engine *e, int volume, const double center[3], int n
   cudaFree(d_out);
   cudaFree(d_und);
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 int dvc_gpu_objective(int obj_function, int n, const double *ref, const double *tar, double *obj,
-                      double *residual) {
+                      double *residual) try {
   if (obj_function < 0 || obj_function > 4) return set_error(DVC_E_ARG, "bad obj_function");
   if (n <= 0 || !ref || !tar || !obj) return set_error(DVC_E_ARG, "bad arguments");
   double *d_r = nullptr, *d_t = nullptr, *d_o = nullptr, *d_res = nullptr;
@@ -2090,6 +2153,8 @@ int dvc_gpu_objective(int obj_function, int n, const double *ref, const double *
   cudaFree(d_o);
   cudaFree(d_res);
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 }  // extern "C"

@@ -6,6 +6,11 @@
 #include "../../include/dvc_gpu.h"
 
 int dvc_internal_set_error(int code, const char *msg);
+// No C++ exception leaves an entry point of the C ABI: each is a function
+// try block whose catch clause returns this (the exception in flight as an
+// error code: DVC_E_NOMEM for a failed allocation, else DVC_E_ARG, with its
+// message for dvc_gpu_last_error)
+int dvc_internal_host_exception();
 
 // patches [n][2][32^3] of points idx[0..n) (or 0..n) of a volume pair
 int dvc_internal_patches(const void *ref, const void *cor, int bpv, int nx, int ny, int nz, int n,

@@ -48,7 +48,7 @@ std::string trim(const std::string &s) {
 extern "C" {
 
 int dvc_gpu_load_raw(void *vol_dev, const char *path, long long header_bytes, int nx, int ny, int nz,
-                     int bytes_per_voxel, int big_endian, void *stream) {
+                     int bytes_per_voxel, int big_endian, void *stream) try {
   if (!vol_dev || !path || header_bytes < 0 || nx <= 0 || ny <= 0 || nz <= 0 ||
       (bytes_per_voxel != 1 && bytes_per_voxel != 2))
     return io_error(DVC_E_ARG, "dvc_gpu_load_raw: bad arguments");
@@ -129,9 +129,11 @@ int dvc_gpu_load_raw(void *vol_dev, const char *path, long long header_bytes, in
   std::fclose(f);
   if (rc != DVC_OK) return io_error(rc, "dvc_gpu_load_raw: " + err);
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
-int dvc_gpu_read_mhd(const char *mhd_path, dvc_volume_info *out) {
+int dvc_gpu_read_mhd(const char *mhd_path, dvc_volume_info *out) try {
   if (!mhd_path || !out) return io_error(DVC_E_ARG, "null argument");
   std::memset(out, 0, sizeof *out);
   std::ifstream f(mhd_path);
@@ -198,6 +200,8 @@ int dvc_gpu_read_mhd(const char *mhd_path, dvc_volume_info *out) {
   out->header_bytes = header;
   std::strcpy(out->data_file, path.c_str());
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }
 
 }  // extern "C"

@@ -192,7 +192,7 @@ __global__ void order_out(int n, const Key *keys, int *order) {
 }  // namespace
 
 extern "C" int dvc_gpu_order_neighbours(int n, const double *points, const double start[3], int k,
-                                        int *order, int *neigh) {
+                                        int *order, int *neigh) try {
   if (n <= 0 || !points || !start || k <= 0 || !order || !neigh)
     return dvc_internal_set_error(DVC_E_ARG, "bad arguments");
   // grid: about k / 8 points per cell over the cloud's bounding box
@@ -280,4 +280,6 @@ extern "C" int dvc_gpu_order_neighbours(int n, const double *points, const doubl
   cudaFree(d_cursor); cudaFree(d_neigh); cudaFree(d_todo); cudaFree(d_redo); cudaFree(d_nredo);
   cudaFree(d_order); cudaFree(d_keys);
   return rc;
+} catch (...) {
+  return dvc_internal_host_exception();
 }

@@ -264,7 +264,7 @@ extern "C" int dvc_gpu_strain(int n, const double *pts, const int *status, const
                               const double *disp, int n_neigh, const int *neigh, int ndp,
                               double objt, int refill, int planar, double *u_fit, int *pts_in_sw,
                               double *sw_radius, double *e_strain, double *l_strain,
-                              double *dgrad) {
+                              double *dgrad) try {
   if (n < 0 || n_neigh < 0 || ndp < 0) return dvc_internal_set_error(DVC_E_ARG, "bad sizes");
   if (n == 0) return DVC_OK;
   if (!pts || !status || !objmin || !disp || !neigh || !u_fit || !pts_in_sw || !sw_radius ||
@@ -301,4 +301,6 @@ extern "C" int dvc_gpu_strain(int n, const double *pts, const int *status, const
   cudaFree(buf);
   if (err != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(err));
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }

@@ -153,7 +153,7 @@ __global__ void synth_kernel(SynthArgs a) {
 extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int bytes_per_voxel,
                                     int n_blobs, const float *blobs, int deform,
                                     const double *coef, float background, float noise_sigma,
-                                    unsigned long long noise_seed, float vmax, void *stream) {
+                                    unsigned long long noise_seed, float vmax, void *stream) try {
   if (!vol_dev || nx <= 0 || ny <= 0 || nz <= 0 || (bytes_per_voxel != 1 && bytes_per_voxel != 2) ||
       n_blobs < 0 || (n_blobs > 0 && !blobs) || deform < 0 || deform > 5 || (deform && !coef))
     return dvc_internal_set_error(DVC_E_ARG, "bad synth arguments");
@@ -317,4 +317,6 @@ extern "C" int dvc_gpu_synth_volume(void *vol_dev, int nx, int ny, int nz, int b
   cudaFree(d_start);
   if (err != cudaSuccess) return dvc_internal_set_error(DVC_E_CUDA, cudaGetErrorString(err));
   return DVC_OK;
+} catch (...) {
+  return dvc_internal_host_exception();
 }

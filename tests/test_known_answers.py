@@ -14,7 +14,9 @@ from the mathematics of the method:
   * the strain fit of a displacement field linear in the position recovers
     its gradient, hence both strain measures and their principal values;
   * each objective is zero for identical signals and blind exactly to what
-    its normalisation removes (offset, scale).
+    its normalisation removes (offset, scale);
+  * Nelder-Mead and random_global followed by Gauss-Newton find the
+    whole-voxel translation too.
 Volumes are stored z, y, x (x fastest); positions are (x, y, z).
 """
 import numpy as np
@@ -217,3 +219,40 @@ def test_objective_invariances_oracle(oracle, name):
 @pytest.mark.parametrize("name", list(OBJ))
 def test_objective_invariances_reference(reference, name):
     _check_objective(reference.objective, name)
+
+
+# The search stages the reference's source holds but never selects
+# (Core/Search.cpp:150-181, 379-440, 680-932, 1045-1098) meet the same answer:
+# Nelder-Mead from the start, and random_global's translations before
+# Gauss-Newton, find the whole-voxel translation with a zero objective.
+STAGES = [("nelder_mead", 3, "cube", dict(refine_method="nelder_mead")),
+          ("nelder_mead", 6, "sphere", dict(refine_method="nelder_mead")),
+          ("random_global", 6, "cube", dict(coarse_method="random", coarse_seed=11, basin_radius=2.0))]
+
+
+def _stage_case(dof, geom, kw):
+    p, ref, cor, pts = _shift_case(dof, geom)
+    q = make_params(ref.shape, subvol_geom=geom, subvol_size=11, subvol_npts=400, num_srch_dof=dof, disp_max=4,
+                    rigid_trans=tuple(SHIFT + [0.3, -0.2, 0.4]), **dict(dict(basin_radius=0.0), **kw))
+    return q, ref, cor, pts
+
+
+def _check_stage(r, tol_u, tol_obj):
+    assert np.all(r["status"] == 0), r["status"]
+    assert np.abs(r["params"][:, :3] - SHIFT).max() <= tol_u
+    assert np.abs(r["objmin"]).max() <= tol_obj
+
+
+@pytest.mark.parametrize("stage,dof,geom,kw", STAGES, ids=[f"{s[0]}-{s[1]}" for s in STAGES])
+def test_search_stages_find_whole_voxel_translation(oracle, reference, stage, dof, geom, kw):
+    p, ref, cor, pts = _stage_case(dof, geom, kw)
+    order, neigh = oracle.order_neighbours(pts)
+    o = oracle.process(p, ref, cor, pts, order=order, neigh=neigh)
+    r = reference.process_stages(p, ref, cor, pts, order, neigh)
+    # Gauss-Newton from a random translation up to disp_max away stops by
+    # its rule (update below 0.01 voxel) a few millionths of a voxel short
+    tol_u, tol_obj = (1e-6, 1e-10) if stage == "nelder_mead" else (1e-4, 1e-8)
+    _check_stage(o, tol_u, tol_obj)
+    _check_stage(r, tol_u, tol_obj)
+    np.testing.assert_array_equal(o["status"], r["status"])
+    assert np.abs(o["params"] - r["params"]).max() <= 1e-9
